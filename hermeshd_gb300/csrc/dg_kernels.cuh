@@ -1,0 +1,650 @@
+// dg_kernels.cuh -- the CUDA kernels of one SSP-RK stage of the HERMESHD DG
+// step, templated on the arithmetic type T and the basis (NB, NQD):
+//
+//   k_limit  positivity limiter, in place on the stage input (flux.f90:1077-1164)
+//   k_face   traces + point fluxes + central/LLF + HLLC at every face point of
+//            one direction (flux.f90:197-450,466-647; boundary ghosts of
+//            prepare_step.f90:20-179 and boundary.f90:40-338 synthesised in place)
+//   k_cell   volume quadrature + surface assembly + sources + forward-Euler
+//            update + RK combination (flux.f90:751-1022, sources.f90:12-84,
+//            integrator.f90:62-252), one write of the stage output
+//   k_mindt  CFL time step (hermeshd.f90:145-199), FP64 in every precision
+//
+// Basis and quadrature tables are compile-time constants (dg_tables_gen.cuh)
+// and every zero entry is skipped at compile time: on GB300 the FP64 pipe is
+// the binding resource of the FP64 path, so each skipped term is time saved.
+#pragma once
+
+#include <cfloat>
+
+#include "dg_physics.cuh"
+
+namespace hermes {
+
+constexpr int LIMIT_TPB = 128;
+constexpr int FACE_TPB = 128;
+constexpr int CELL_TPB = 64;
+constexpr int DT_TPB = 256;
+
+// stage combination of integrator.f90:62-86
+enum Comb { COMB_NONE = 0, COMB_HALF = 1, COMB_34 = 2, COMB_13 = 3 };
+enum CellMode { MODE_RHS = 0, MODE_STAGE = 1 };
+
+struct Geom {
+    const Box* boxes;
+    int nbox;
+    long long ncell;          // all boxes
+    long long nface[3];       // all boxes, per direction
+};
+
+// face tables of one direction and side (0 = minus face, 1 = plus face)
+template <class TB, int DIR, int SIDE>
+__host__ __device__ constexpr double ftab(int p, int b) {
+    if constexpr (DIR == 0) return SIDE ? TB::XP(p, b) : TB::XM(p, b);
+    else if constexpr (DIR == 1) return SIDE ? TB::YP(p, b) : TB::YM(p, b);
+    else return SIDE ? TB::ZP(p, b) : TB::ZM(p, b);
+}
+template <class TB, int DIR, int SIDE>
+__host__ __device__ constexpr double stab(int p, int b) {
+    if constexpr (DIR == 0) return SIDE ? TB::SXP(p, b) : TB::SXM(p, b);
+    else if constexpr (DIR == 1) return SIDE ? TB::SYP(p, b) : TB::SYM(p, b);
+    else return SIDE ? TB::SZP(p, b) : TB::SZM(p, b);
+}
+template <class TB, int DIR>
+__host__ __device__ constexpr double vtab(int g, int b) {
+    if constexpr (DIR == 0) return TB::VX(g, b);
+    else if constexpr (DIR == 1) return TB::VY(g, b);
+    else return TB::VZ(g, b);
+}
+
+// trace of all NQ variables of one cell at face point P: sum_b phi_b(P) Q(b,v)
+template <class TB, int DIR, int SIDE, int P, class T>
+__device__ __forceinline__ void trace_pt(const T* __restrict__ Qb, long long ncell, long long cell, T out[NQ]) {
+    sfor<NQ>([&](auto vv) {
+        constexpr int v = decltype(vv)::value;
+        T acc = T(0);
+        sfor<TB::NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            constexpr double c = ftab<TB, DIR, SIDE>(P, b);
+            if constexpr (c != 0.0) acc = fma(T(c), __ldg(Qb + (long long)(b * NQ + v) * ncell + cell), acc);
+        });
+        out[v] = acc;
+    });
+}
+
+// trace of a single variable at face point P
+template <class TB, int DIR, int SIDE, int P, int V, class T>
+__device__ __forceinline__ T trace_var(const T* __restrict__ Qb, long long ncell, long long cell) {
+    T acc = T(0);
+    sfor<TB::NB>([&](auto bb) {
+        constexpr int b = decltype(bb)::value;
+        constexpr double c = ftab<TB, DIR, SIDE>(P, b);
+        if constexpr (c != 0.0) acc = fma(T(c), __ldg(Qb + (long long)(b * NQ + V) * ncell + cell), acc);
+    });
+    return acc;
+}
+
+// ===========================================================================
+// k_limit: flux.f90:1077-1164, in place.  One thread per cell.
+// Fast path: a bound on every face-point value, |sum_{b>0} phi_b q_b| <=
+// sum_{b>0} max_p|phi_b(p)| |q_b|, proves that no point can trigger the
+// density or pressure branch; the cell is then left untouched, which is what
+// the full evaluation would do.  Only cells the bound cannot clear run the
+// point-by-point evaluation.  For T = float the evaluation near the floors
+// runs in FP64.
+// ===========================================================================
+template <class TB>
+__host__ __device__ constexpr double lim_maxabs(int b) {
+    double m = 0.0;
+    for (int p = 0; p < TB::NPGE; ++p) {
+        double a = TB::LIM(p, b) < 0 ? -TB::LIM(p, b) : TB::LIM(p, b);
+        if (a > m) m = a;
+    }
+    return m;
+}
+
+template <class TB, class U>
+__device__ __forceinline__ bool limit_cell(const Phys& ph, U q[5][TB::NB]) {
+    // returns true if q was modified
+    constexpr int NB = TB::NB;
+    const U rh_floor = U(ph.rh_floor), epsi = U(ph.rh_floor), epsiP = U(ph.rh_floor) * U(ph.T_floor);
+    const U aindm1 = U(ph.aindm1);
+    if (q[RH][0] < rh_floor) {
+        sfor<NB - 1>([&](auto bb) {
+            constexpr int b = decltype(bb)::value + 1;
+            q[RH][b] = U(0); q[MX][b] = U(0); q[MY][b] = U(0); q[MZ][b] = U(0); q[EN][b] = U(0);
+        });
+        q[RH][0] = rh_floor;
+        return true;
+    }
+    bool changed = false;
+    // density at the npge face points
+    U Qrhmin = U(0);
+    sfor<TB::NPGE>([&](auto pp) {
+        constexpr int p = decltype(pp)::value;
+        U s = U(0);
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            constexpr double c = TB::LIM(p, b);
+            if constexpr (c != 0.0) s = fma(U(c), q[RH][b], s);
+        });
+        if (p == 0 || s < Qrhmin) Qrhmin = s;
+    });
+    if (Qrhmin < epsi) {
+        U theta = (epsi - q[RH][0]) / (Qrhmin - q[RH][0]);
+        if (theta > U(1)) theta = U(1);
+        if (theta < U(0)) theta = U(0);
+        sfor<NB - 1>([&](auto bb) {
+            constexpr int b = decltype(bb)::value + 1;
+            q[RH][b] = fabs(theta) * q[RH][b];
+        });
+        changed = true;
+    }
+    const U Pave = aindm1 * (q[EN][0] - U(0.5) * (q[MX][0] * q[MX][0] + q[MY][0] * q[MY][0] + q[MZ][0] * q[MZ][0]) / q[RH][0]);
+    if (Pave < epsiP) {
+        sfor<NB - 1>([&](auto bb) {
+            constexpr int b = decltype(bb)::value + 1;
+            q[RH][b] = U(0); q[MX][b] = U(0); q[MY][b] = U(0); q[MZ][b] = U(0); q[EN][b] = U(0);
+        });
+        return true;
+    }
+    U theta = U(1);
+    sfor<TB::NPGE>([&](auto pp) {
+        constexpr int p = decltype(pp)::value;
+        U e[5];
+        sfor<5>([&](auto vv) {
+            constexpr int v = decltype(vv)::value;
+            U s = U(0);
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr double c = TB::LIM(p, b);
+                if constexpr (c != 0.0) s = fma(U(c), q[v][b], s);
+            });
+            e[v] = s;
+        });
+        U dni = U(1) / e[RH];
+        U P = aindm1 * (e[EN] - U(0.5) * dni * (e[MX] * e[MX] + e[MY] * e[MY] + e[MZ] * e[MZ]));
+        if (P < epsiP) {
+            if (Pave != P) theta = fmin(theta, (Pave - epsiP) / (Pave - P));
+        }
+    });
+    if (theta > U(1)) theta = U(1);
+    if (theta < U(0)) theta = U(0);
+    if (theta != U(1)) {
+        sfor<NB - 1>([&](auto bb) {
+            constexpr int b = decltype(bb)::value + 1;
+            sfor<5>([&](auto vv) { q[decltype(vv)::value][b] = theta * q[decltype(vv)::value][b]; });
+        });
+        changed = true;
+    }
+    return changed;
+}
+
+template <class TB, class U>
+__device__ __forceinline__ bool limit_bound_clear(const Phys& ph, const U q[5][TB::NB]) {
+    // true if no face point can fall below the density or pressure floor
+    constexpr int NB = TB::NB;
+    U B[5];
+    sfor<5>([&](auto vv) {
+        constexpr int v = decltype(vv)::value;
+        U s = U(0);
+        sfor<NB - 1>([&](auto bb) {
+            constexpr int b = decltype(bb)::value + 1;
+            constexpr double m = lim_maxabs<TB>(b);
+            if constexpr (m != 0.0) s = fma(U(m), fabs(q[v][b]), s);
+        });
+        B[v] = s;
+    });
+    const U tol = U(std::is_same<U, double>::value ? 1e-10 : 1e-4);
+    const U epsi = U(ph.rh_floor), epsiP = U(ph.rh_floor) * U(ph.T_floor);
+    U rlo = q[RH][0] - B[RH];
+    if (!(rlo >= epsi + tol * (q[RH][0] + B[RH]))) return false;
+    U Elo = q[EN][0] - B[EN];
+    U m0 = fabs(q[MX][0]) + B[MX], m1 = fabs(q[MY][0]) + B[MY], m2 = fabs(q[MZ][0]) + B[MZ];
+    U ke = U(0.5) * (m0 * m0 + m1 * m1 + m2 * m2) / rlo;
+    U Plo = U(ph.aindm1) * (Elo - ke);
+    return Plo >= epsiP + tol * (fabs(q[EN][0]) + B[EN] + ke);
+}
+
+template <class T, class TB>
+__global__ void __launch_bounds__(LIMIT_TPB) k_limit(T* __restrict__ Q, Geom G, Phys ph) {
+    constexpr int NB = TB::NB;
+    long long gc = (long long)blockIdx.x * LIMIT_TPB + threadIdx.x;
+    if (gc >= G.ncell) return;
+    int bx = find_box(G.boxes, G.nbox, gc, [](const Box& b) { return b.cell0; });
+    const Box& B = G.boxes[bx];
+    const long long le = gc - B.cell0, nc = B.ncell;
+    T* Qb = Q + B.q0;
+    T q[5][NB];
+    sfor<5>([&](auto vv) {
+        constexpr int v = decltype(vv)::value;
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            q[v][b] = Qb[(long long)(b * NQ + v) * nc + le];
+        });
+    });
+    if (q[RH][0] >= T(ph.rh_floor) && limit_bound_clear<TB, T>(ph, q)) return;
+    bool changed;
+    if constexpr (std::is_same<T, double>::value) {
+        changed = limit_cell<TB, double>(ph, q);
+    } else {
+        // FP64 positivity fix for the FP32 path
+        double qd[5][NB];
+        sfor<5>([&](auto vv) { sfor<NB>([&](auto bb) { qd[decltype(vv)::value][decltype(bb)::value] = (double)q[decltype(vv)::value][decltype(bb)::value]; }); });
+        changed = limit_cell<TB, double>(ph, qd);
+        sfor<5>([&](auto vv) { sfor<NB>([&](auto bb) { q[decltype(vv)::value][decltype(bb)::value] = (T)qd[decltype(vv)::value][decltype(bb)::value]; }); });
+    }
+    if (!changed) return;
+    sfor<5>([&](auto vv) {
+        constexpr int v = decltype(vv)::value;
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            Qb[(long long)(b * NQ + v) * nc + le] = q[v][b];
+        });
+    });
+}
+
+// ===========================================================================
+// k_face: one thread per (face, point).  blockIdx.y = face point P.
+// ===========================================================================
+struct FaceArgs {
+    Geom G;
+    Phys ph;
+    const unsigned long long* step;  // noise step counter (device)
+    unsigned stage;
+};
+
+template <class T, class TB, int DIR, int P>
+__device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restrict__ flux, const FaceArgs& a, long long gf) {
+    const Geom& G = a.G;
+    const Phys& ph = a.ph;
+    int bx = find_box(G.boxes, G.nbox, gf, [](const Box& b) { return b.face0[DIR]; });
+    const Box& B = G.boxes[bx];
+    const long long lf = gf - B.face0[DIR];
+    const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
+    const int ex = DIR == 0 ? B.nfp[0] : n0, ey = DIR == 1 ? B.nfp[1] : n1;
+    const int i = (int)(lf % ex);
+    const int j = (int)((lf / ex) % ey);
+    const int k = (int)(lf / ((long long)ex * ey));
+    const int n = B.n[DIR];
+    const int s = DIR == 0 ? i : DIR == 1 ? j : k;       // face plane
+    const bool dedup = B.nfp[DIR] == n;                    // both ends periodic: n planes
+    const long long nc = B.ncell;
+    const T* Qb = Q + B.q0;
+    auto cell_at = [&](int c) -> long long {              // cell with plane coordinate c
+        int ci = DIR == 0 ? c : i, cj = DIR == 1 ? c : j, ck = DIR == 2 ? c : k;
+        return (long long)ci + (long long)n0 * (cj + (long long)n1 * ck);
+    };
+    constexpr int MN = DIR == 0 ? MX : DIR == 1 ? MY : MZ;   // normal momentum
+    T qL[NQ], qR[NQ];
+    if (dedup || (s > 0 && s < n)) {
+        const int lo = s > 0 ? s - 1 : n - 1;
+        trace_pt<TB, DIR, 1, P>(Qb, nc, cell_at(lo), qL);
+        trace_pt<TB, DIR, 0, P>(Qb, nc, cell_at(s), qR);
+    } else if (s == 0) {
+        // low boundary: ghost from the first cell's minus trace (boundary.f90:40-244)
+        const long long c0 = cell_at(0);
+        trace_pt<TB, DIR, 0, P>(Qb, nc, c0, qR);
+        const int code = B.bc[2 * DIR];
+        if (code == BC_PERIODIC) {
+            // topology not periodic (the hi flag is not): the ghost is the never-received zero trace
+            for (int v = 0; v < NQ; ++v) qL[v] = T(0);
+        } else {
+            for (int v = 0; v < NQ; ++v) qL[v] = qR[v];
+            if (code == BC_NOSLIP) { qL[MX] = T(0); qL[MY] = T(0); qL[MZ] = T(0); }
+            else if (code == BC_WALL) { qL[MN] = T(0); }
+            else if (code == BC_OUTFLOW) {
+                T mmax = -T(INFINITY);
+                sfor<TB::NF>([&](auto pp) {
+                    mmax = fmax(mmax, trace_var<TB, DIR, 0, decltype(pp)::value, MN>(Qb, nc, c0));
+                });
+                if (mmax > T(0)) qL[MN] = T(0);
+            }
+        }
+    } else {
+        // high boundary (s == n)
+        const long long cl = cell_at(n - 1);
+        trace_pt<TB, DIR, 1, P>(Qb, nc, cl, qL);
+        const int code = B.bc[2 * DIR + 1];
+        if (code == BC_PERIODIC) {
+            // periodic topology with a non-periodic low flag: the ghost is the
+            // first cell's raw minus trace (prepare_step.f90:75-104 self-send)
+            trace_pt<TB, DIR, 0, P>(Qb, nc, cell_at(0), qR);
+        } else if (code == BC_OUTFLOW && DIR == 0) {
+            // boundary.f90:246-282 never copies the interior trace: from a zero
+            // ghost array the result stays zero
+            for (int v = 0; v < NQ; ++v) qR[v] = T(0);
+        } else {
+            for (int v = 0; v < NQ; ++v) qR[v] = qL[v];
+            if (code == BC_NOSLIP) { qR[MX] = T(0); qR[MY] = T(0); qR[MZ] = T(0); }
+            else if (code == BC_WALL) { qR[MN] = T(0); }
+            else if (code == BC_OUTFLOW) {
+                T mmin = T(INFINITY);
+                sfor<TB::NF>([&](auto pp) {
+                    mmin = fmin(mmin, trace_var<TB, DIR, 1, decltype(pp)::value, MN>(Qb, nc, cl));
+                });
+                if (mmin < T(0)) qR[MN] = T(0);
+            }
+        }
+    }
+    // point fluxes of both sides (flux.f90:240), stochastic stress per side
+    T SL[6] = {T(0), T(0), T(0), T(0), T(0), T(0)}, SR[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    if (ph.llns) {
+        NoiseCtr nc_{*a.step, a.stage};
+        random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P, SL);
+        random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P + TB::NF, SR);
+    }
+    T fL[NQ], fR[NQ], F[NQ];
+    {
+        Prim<T> wL = primitives(ph, qL);
+        point_flux<T, DIR>(ph, qL, wL, SL, fL);
+        Prim<T> wR = primitives(ph, qR);
+        point_flux<T, DIR>(ph, qR, wR, SR, fR);
+    }
+    // flux.f90:243-262: central flux, LLF with the freezing speed for ivis 2
+    if (ph.ivis == 2) {
+        const T cfr = fmax(cfcal<T, DIR>(ph, qL), cfcal<T, DIR>(ph, qR));
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]) - T(0.5) * cfr * (qR[v] - qL[v]);
+    } else {
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]);
+    }
+    if (ph.ihllc) {
+        T rho_i_last = T(0);
+        if (ph.ieos == 2) {
+            // 1/rho of the last point of the reference's call: the right state at point NF-1
+            T rlast;
+            if (dedup || s < n) rlast = trace_var<TB, DIR, 0, TB::NF - 1, RH>(Qb, nc, cell_at(s));
+            else if (B.bc[2 * DIR + 1] == BC_PERIODIC) rlast = trace_var<TB, DIR, 0, TB::NF - 1, RH>(Qb, nc, cell_at(0));
+            else if (B.bc[2 * DIR + 1] == BC_OUTFLOW && DIR == 0) rlast = T(0);
+            else rlast = trace_var<TB, DIR, 1, TB::NF - 1, RH>(Qb, nc, cell_at(n - 1));
+            rho_i_last = T(1) / rlast;
+        }
+        hllc<T, DIR>(ph, qL, qR, fL, fR, rho_i_last, F);
+    }
+    // store, scaled by the inverse spacing of this direction
+    const T sc = T(B.di[DIR]);
+    const long long nfd = (long long)ex * ey * (DIR == 2 ? B.nfp[2] : n2);
+    T* fb = flux + B.fbase[DIR];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) fb[(long long)(v * TB::NF + P) * nfd + lf] = F[v] * sc;
+}
+
+template <class T, class TB, int DIR>
+__global__ void __launch_bounds__(FACE_TPB) k_face(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
+    long long gf = (long long)blockIdx.x * FACE_TPB + threadIdx.x;
+    if (gf >= a.G.nface[DIR]) return;
+    const int p = blockIdx.y;
+    sfor<TB::NF>([&](auto pp) {
+        constexpr int P = decltype(pp)::value;
+        if (p == P) face_point<T, TB, DIR, P>(Q, flux, a, gf);
+    });
+}
+
+// ===========================================================================
+// k_cell: one thread per cell; the cell's coefficients and volume
+// accumulators live in the thread's own column of shared memory.
+// ===========================================================================
+struct CellArgs {
+    Geom G;
+    Phys ph;
+    const BoxState* st;               // dt per box
+    const unsigned long long* step;   // noise step counter
+    int* flags;
+    unsigned stage;
+    int mode, comb;
+};
+
+template <class T, class TB>
+__global__ void __launch_bounds__(CELL_TPB) k_cell(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux, CellArgs a) {
+    // Qin, Q0 and out may alias (the RK stages write in place); each thread
+    // reads its own cell's elements before writing them.
+    constexpr int NB = TB::NB, NF = TB::NF, NPG = TB::NPG;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* qs = reinterpret_cast<T*>(smem_raw);           // [NB*NQ][CELL_TPB]
+    T* acc = qs + NB * NQ * CELL_TPB;                  // [NB*NQ][CELL_TPB]
+    const int tid = threadIdx.x;
+    const long long gc = (long long)blockIdx.x * CELL_TPB + tid;
+    if (gc >= a.G.ncell) return;
+    const Phys& ph = a.ph;
+    const int bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
+    const Box& B = a.G.boxes[bx];
+    const long long le = gc - B.cell0, nc = B.ncell;
+    const T* Qb = Qin + B.q0;
+#define QS(b, v) qs[((b) * NQ + (v)) * CELL_TPB + tid]
+#define ACC(b, v) acc[((b) * NQ + (v)) * CELL_TPB + tid]
+#pragma unroll
+    for (int bv = 0; bv < NB * NQ; ++bv) {
+        qs[bv * CELL_TPB + tid] = Qb[(long long)bv * nc + le];
+        acc[bv * CELL_TPB + tid] = T(0);
+    }
+    const T di[3] = {T(B.di[0]), T(B.di[1]), T(B.di[2])};
+    const bool noise = ph.llns != 0;
+    const NoiseCtr nctr{noise ? *a.step : 0ull, a.stage};
+    const bool src_lin = (ph.ivis == 0), src_tenm = (ph.ivis == 2), src_bf = (ph.body_force != 0.0);
+
+    // ---- volume quadrature and point sources (flux.f90:751-928, sources.f90:28-78)
+    sfor<NPG>([&](auto gg) {
+        constexpr int g = decltype(gg)::value;
+        T u[NQ];
+        sfor<NQ>([&](auto vv) {
+            constexpr int v = decltype(vv)::value;
+            T s = T(0);
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr double c = TB::INT(g, b);
+                if constexpr (c != 0.0) s = fma(T(c), QS(b, v), s);
+            });
+            u[v] = s;
+        });
+        const Prim<T> w = primitives(ph, u);
+        sfor<3>([&](auto dd) {
+            constexpr int d = decltype(dd)::value;
+            T S[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+            if (noise) random_stress<T>(ph, B.seed, nctr, 3 + d, (unsigned long long)le, g, S);
+            T f[NQ];
+            point_flux<T, d>(ph, u, w, S, f);
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) f[v] *= di[d];
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr double c = vtab<TB, d>(g, b);
+                if constexpr (c != 0.0) {
+#pragma unroll
+                    for (int v = 0; v < NQ; ++v) ACC(b, v) = fma(T(c), f[v], ACC(b, v));
+                }
+            });
+        });
+        if (src_lin || src_tenm || src_bf) {
+            T s[NQ];
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) s[v] = T(0);
+            if (src_bf) {   // body force (no reference counterpart)
+                s[MX] = u[RH] * T(ph.body_force);
+                s[EN] = u[MX] * T(ph.body_force);
+            }
+            if (src_lin) {  // sources.f90:37-43
+                const T coll = T(ph.coll);
+#pragma unroll
+                for (int v = PXX; v <= PYZ; ++v) s[v] = -coll * u[v];
+            } else if (src_tenm) {  // sources.f90:51-69
+                const T vx2 = w.vx * w.vx, vy2 = w.vy * w.vy, vz2 = w.vz * w.vz;
+                const T colldn = T(ph.coll) * w.dn, c1d3 = T(1.0 / 3.0);
+                s[PXX] = colldn * (T(2) * vx2 - vy2 - vz2) * c1d3;
+                s[PYY] = colldn * (T(2) * vy2 - vz2 - vx2) * c1d3;
+                s[PZZ] = colldn * (T(2) * vz2 - vx2 - vy2) * c1d3;
+                s[PXY] = colldn * w.vx * w.vy;
+                s[PXZ] = colldn * w.vx * w.vz;
+                s[PYZ] = colldn * w.vy * w.vz;
+            }
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr double c = TB::SRC(g, b);
+                if constexpr (c != 0.0) {
+                    if (src_bf) {
+                        ACC(b, MX) = fma(T(c), s[MX], ACC(b, MX));
+                        ACC(b, EN) = fma(T(c), s[EN], ACC(b, EN));
+                    }
+                    if (src_lin || src_tenm) {
+#pragma unroll
+                        for (int v = PXX; v <= PYZ; ++v) ACC(b, v) = fma(T(c), s[v], ACC(b, v));
+                    }
+                }
+            });
+        }
+    });
+
+    // ---- surface assembly, update and RK combination, one variable at a time
+    const int n0 = B.n[0], n1 = B.n[1];
+    const int ci = (int)(le % n0), cj = (int)((le / n0) % n1), ck = (int)(le / ((long long)n0 * n1));
+    long long fm[3], fp[3], nfd[3];
+    {
+        const int c[3] = {ci, cj, ck};
+        for (int d = 0; d < 3; ++d) {
+            int e0 = d == 0 ? B.nfp[0] : B.n[0], e1 = d == 1 ? B.nfp[1] : B.n[1], e2 = d == 2 ? B.nfp[2] : B.n[2];
+            nfd[d] = (long long)e0 * e1 * e2;
+            int hi = c[d] + 1;
+            if (B.nfp[d] == B.n[d] && hi == B.n[d]) hi = 0;
+            int lo = c[d];
+            int a0 = d == 0 ? lo : ci, a1 = d == 1 ? lo : cj, a2 = d == 2 ? lo : ck;
+            fm[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
+            a0 = d == 0 ? hi : ci; a1 = d == 1 ? hi : cj; a2 = d == 2 ? hi : ck;
+            fp[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
+        }
+    }
+    const T dt = T(a.st[bx].dt);
+    const T faci = T(1) / (T(1) + dt * T(ph.coll));
+    T* ob = out + B.q0;
+    const T* q0b = Q0 ? Q0 + B.q0 : nullptr;
+    bool bad = false;
+    T rs[3][NB];   // rhs of pxx, pyy, pzz, kept for the coupled ivis-2 update
+
+    auto finish = [&](int v, const T* r) {
+        // r[b] = glflux - source of variable v
+        if (a.mode == MODE_RHS) {
+#pragma unroll
+            for (int b = 0; b < NB; ++b) ob[(long long)(b * NQ + v) * nc + le] = r[b];
+            return;
+        }
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            T e = QS(b, v) - dt * r[b];                    // integrator.f90:147-149,171-173
+            if (ph.ivis != 0 && v >= PXX) e = faci * e;    // integrator.f90:174,220-224
+            T o = e;
+            if (a.comb != COMB_NONE) {
+                const T q0 = q0b[(long long)(b * NQ + v) * nc + le];
+                if (a.comb == COMB_HALF) o = T(0.5) * (q0 + e);                           // integrator.f90:70
+                else if (a.comb == COMB_34) o = T(0.75) * q0 + T(0.25) * e;               // integrator.f90:82
+                else o = T(1.0 / 3.0) * q0 + T(2.0 / 3.0) * e;                            // integrator.f90:85
+            }
+            if (b == 0 && o != o) bad = true;
+            ob[(long long)(b * NQ + v) * nc + le] = o;
+        }
+    };
+
+    sfor<NQ>([&](auto vv) {
+        constexpr int v = decltype(vv)::value;
+        T r[NB];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) r[b] = -ACC(b, v);
+        sfor<3>([&](auto dd) {
+            constexpr int d = decltype(dd)::value;
+            const T* fb = flux + a.G.boxes[bx].fbase[d] + (long long)v * NF * nfd[d];
+            sfor<NF>([&](auto pp) {
+                constexpr int p = decltype(pp)::value;
+                const T Fp = __ldg(fb + (long long)p * nfd[d] + fp[d]);
+                const T Fm = __ldg(fb + (long long)p * nfd[d] + fm[d]);
+                sfor<NB>([&](auto bb) {
+                    constexpr int b = decltype(bb)::value;
+                    constexpr double cp = stab<TB, d, 1>(p, b);
+                    constexpr double cm = stab<TB, d, 0>(p, b);
+                    if constexpr (cp != 0.0) r[b] = fma(T(cp), Fp, r[b]);
+                    if constexpr (cm != 0.0) r[b] = fma(T(cm), Fm, r[b]);
+                });
+            });
+        });
+        if constexpr (v >= PXX && v <= PZZ) {
+#pragma unroll
+            for (int b = 0; b < NB; ++b) rs[v - PXX][b] = r[b];
+            if constexpr (v == PZZ) {
+                if (ph.ivis == 2 && a.mode == MODE_STAGE) {
+                    // integrator.f90:207-218: trace-coupled semi-implicit update
+                    const T coll = T(ph.coll), c1d3 = T(1.0 / 3.0);
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) {
+                        const T Q_sum = coll * dt * (QS(b, PXX) + QS(b, PYY) + QS(b, PZZ)) * c1d3;
+                        const T R_sum = coll * (dt * dt) * (rs[0][b] + rs[1][b] + rs[2][b]) * c1d3;
+                        T e3[3];
+#pragma unroll
+                        for (int m = 0; m < 3; ++m) e3[m] = faci * (QS(b, PXX + m) - dt * rs[m][b] + Q_sum - R_sum);
+#pragma unroll
+                        for (int m = 0; m < 3; ++m) {
+                            T o = e3[m];
+                            if (a.comb != COMB_NONE) {
+                                const T q0 = q0b[(long long)(b * NQ + PXX + m) * nc + le];
+                                if (a.comb == COMB_HALF) o = T(0.5) * (q0 + e3[m]);
+                                else if (a.comb == COMB_34) o = T(0.75) * q0 + T(0.25) * e3[m];
+                                else o = T(1.0 / 3.0) * q0 + T(2.0 / 3.0) * e3[m];
+                            }
+                            if (b == 0 && o != o) bad = true;
+                            ob[(long long)(b * NQ + PXX + m) * nc + le] = o;
+                        }
+                    }
+                } else {
+                    finish(PXX, rs[0]);
+                    finish(PYY, rs[1]);
+                    finish(PZZ, rs[2]);
+                }
+            }
+        } else {
+            finish(v, r);
+        }
+    });
+    if (bad) a.flags[0] |= FLAG_NONFINITE;   // integrator.f90:234-250 (the reference exits)
+#undef QS
+#undef ACC
+}
+
+// ===========================================================================
+// k_mindt: hermes.f90:145-199 get_min_dt over the cell averages, FP64.
+// ===========================================================================
+struct DtArgs {
+    Geom G;
+    Phys ph;
+    BoxState* st;
+};
+
+template <class T>
+__global__ void __launch_bounds__(DT_TPB) k_mindt(const T* __restrict__ Q, DtArgs a) {
+    const long long gc = (long long)blockIdx.x * DT_TPB + threadIdx.x;
+    const bool act = gc < a.G.ncell;
+    int bx = 0;
+    double vmag0 = 0.0;
+    if (act) {
+        bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
+        const Box& B = a.G.boxes[bx];
+        const long long le = gc - B.cell0, nc = B.ncell;
+        const T* Qb = Q + B.q0;
+        const double dn = (double)Qb[RH * nc + le], dni = 1.0 / dn;
+        const double vx = (double)Qb[MX * nc + le] * dni, vy = (double)Qb[MY * nc + le] * dni, vz = (double)Qb[MZ * nc + le] * dni;
+        double cs;
+        if (a.ph.ieos == 1) cs = sqrt(a.ph.aindex * ((double)Qb[EN * nc + le] * dni - 0.5 * (vx * vx + vy * vy + vz * vz)));
+        else cs = sqrt(7.2 * a.ph.P_1 * pow(dn, 6.2) + a.ph.T_floor);
+        const double v0 = fmax(fmax(fabs(vx) + cs, fabs(vy) + cs), fabs(vz) + cs);
+        if (v0 > 0.0 && dn > a.ph.rh_mult * a.ph.rh_floor) vmag0 = v0;   // NaN never qualifies
+        if (le == nc - 1) a.st[bx].cs_last = cs;
+    }
+    // warp max when the warp lies in one box, else one atomic per thread
+    const unsigned full = 0xffffffffu;
+    const int bx0 = __shfl_sync(full, bx, 0);
+    const bool same = __all_sync(full, bx == bx0 || !act);
+    if (same) {
+        for (int o = 16; o > 0; o >>= 1) vmag0 = fmax(vmag0, __shfl_xor_sync(full, vmag0, o));
+        if ((threadIdx.x & 31) == 0 && vmag0 > 0.0) atomicMax(&a.st[bx0].vmag_bits, (unsigned long long)__double_as_longlong(vmag0));
+    } else if (act && vmag0 > 0.0) {
+        atomicMax(&a.st[bx].vmag_bits, (unsigned long long)__double_as_longlong(vmag0));
+    }
+}
+
+}  // namespace hermes

@@ -1,0 +1,289 @@
+// dg_physics.cuh -- point-wise physics of the DG step: the 5/10-moment point
+// flux (flux.f90:23-193), the HLLC Riemann solver (flux.f90:466-647), the
+// freezing speed (flux.f90:1029-1072) and the stochastic stress
+// (random.f90:106-145, with a counter-based Philox generator).
+//
+// Everything here is evaluated at one quadrature point by one thread.  T is
+// the arithmetic type of the bulk path (double, or float for the FP32 path).
+#pragma once
+
+#include "hermes_common.cuh"
+
+namespace hermes {
+
+// ---------------------------------------------------------------------------
+// Philox-4x32-10 (Salmon et al., SC'11).  Counter scheme:
+//   key = seed, counter = (site, pt | kind<<8 | sub<<12 | stage<<16, step_lo, step_hi)
+// kind: 0..2 face call in x/y/z, 3..5 interior call in x/y/z.  Nine normals per
+// point come from five blocks, one Box-Muller pair per block.
+// ---------------------------------------------------------------------------
+struct NoiseCtr {
+    unsigned long long step;
+    unsigned stage;
+};
+
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+        uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void normals9(unsigned long long seed, NoiseCtr nc, unsigned kind, unsigned long long site,
+                                         unsigned pt, T G[9]) {
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int sub = 0; sub < 5; ++sub) {
+        uint32_t c[4];
+        c[0] = (uint32_t)site;
+        c[1] = (pt & 0xFFu) | ((kind & 0xFu) << 8) | (((unsigned)sub & 0xFu) << 12) | ((nc.stage & 0xFFFFu) << 16);
+        c[2] = (uint32_t)nc.step;
+        c[3] = (uint32_t)(nc.step >> 32);
+        philox4x32_10(c, k0, k1);
+        T z0, z1;
+        if constexpr (std::is_same<T, double>::value) {
+            // 53-bit uniforms in (0,1)
+            unsigned long long m1 = ((unsigned long long)c[0] << 21) | (unsigned long long)(c[1] >> 11);
+            unsigned long long m2 = ((unsigned long long)c[2] << 21) | (unsigned long long)(c[3] >> 11);
+            double u1 = ((double)m1 + 0.5) * (1.0 / 9007199254740992.0);
+            double u2 = ((double)m2 + 0.5) * (1.0 / 9007199254740992.0);
+            double r = sqrt(-2.0 * log(u1)), s, co;
+            sincos(6.283185307179586476925286766559 * u2, &s, &co);
+            z0 = r * co; z1 = r * s;
+        } else {
+            // the top 24 bits of the same words
+            float u1 = ((float)(c[0] >> 8) + 0.5f) * (1.0f / 16777216.0f);
+            float u2 = ((float)(c[2] >> 8) + 0.5f) * (1.0f / 16777216.0f);
+            float r = sqrtf(-2.0f * logf(u1)), s, co;
+            sincosf(6.2831853071795864769f * u2, &s, &co);
+            z0 = r * co; z1 = r * s;
+        }
+        if (2 * sub < 9) G[2 * sub] = z0;
+        if (2 * sub + 1 < 9) G[2 * sub + 1] = z1;
+    }
+}
+
+// random.f90:106-145: S = eta (sym G - tr G/3 I) + zeta tr G I, the
+// amplitudes already carrying 1/sqrt(dV dt).  S = {xx, yy, zz, xy, xz, yz}.
+template <class T>
+__device__ __forceinline__ void random_stress(const Phys& ph, unsigned long long seed, NoiseCtr nc, unsigned kind,
+                                              unsigned long long site, unsigned pt, T S[6]) {
+    T G[9];
+    normals9<T>(seed, nc, kind, site, pt, G);
+    const T s2i = T(0.70710678118654752440);
+    const T eta = T(ph.eta_sd), zeta = T(ph.zeta_sd);
+    T Gxy = s2i * (G[1] + G[3]), Gxz = s2i * (G[2] + G[6]), Gyz = s2i * (G[5] + G[7]);
+    T trG = G[0] + G[4] + G[8], trGd3 = trG / T(3), trGz = zeta * trG;
+    S[0] = eta * (G[0] - trGd3) + trGz;
+    S[1] = eta * (G[4] - trGd3) + trGz;
+    S[2] = eta * (G[8] - trGd3) + trGz;
+    S[3] = eta * Gxy;
+    S[4] = eta * Gxz;
+    S[5] = eta * Gyz;
+}
+
+// ---------------------------------------------------------------------------
+// flux.f90:23-193 flux_calc_pnts_r at one point, direction DIR (0 x, 1 y, 2 z)
+// ---------------------------------------------------------------------------
+template <class T>
+struct Prim {
+    T dn, dni, vx, vy, vz, P, P_10;
+};
+
+template <class T>
+__device__ __forceinline__ Prim<T> primitives(const Phys& ph, const T q[NQ]) {
+    Prim<T> w;
+    w.dn = q[RH];
+    w.dni = T(1) / w.dn;
+    w.vx = q[MX] * w.dni;
+    w.vy = q[MY] * w.dni;
+    w.vz = q[MZ] * w.dni;
+    T smsq = q[MX] * q[MX] + q[MY] * q[MY] + q[MZ] * q[MZ];
+    w.P = T(ph.aindm1) * (q[EN] - T(0.5) * w.dni * smsq);
+    w.P_10 = T(1.0 / 3.0) * (q[PXX] + q[PYY] + q[PZZ] - w.dni * smsq);
+    if (ph.ieos == 2) w.P = T(ph.P_1) * (pow(w.dn, T(7.2)) - T(1)) + T(ph.P_base) + w.P;
+    const T Pf = T(ph.P_floor);
+    if (w.P < Pf) w.P = Pf;
+    if (w.P_10 < Pf) w.P_10 = Pf;
+    return w;
+}
+
+// S = {Sxx, Syy, Szz, Sxy, Sxz, Syz} (zero without noise)
+template <class T, int DIR>
+__device__ __forceinline__ void point_flux(const Phys& ph, const T q[NQ], const Prim<T>& w, const T S[6], T f[NQ]) {
+    const T colvis = T(ph.colvis);
+    const T c2d3cv = T(2.0 / 3.0) * colvis, c4d3cv = T(4.0 / 3.0) * colvis;
+    const T M_x = q[MX], M_y = q[MY], M_z = q[MZ], Ener = q[EN];
+    const T P_xx = q[PXX], P_yy = q[PYY], P_zz = q[PZZ], P_xy = q[PXY], P_xz = q[PXZ], P_yz = q[PYZ];
+    const T vx = w.vx, vy = w.vy, vz = w.vz, P = w.P, P_10 = w.P_10, P_5 = w.P;
+    const T Sxx = S[0], Syy = S[1], Szz = S[2], Sxy = S[3], Sxz = S[4], Syz = S[5];
+    const bool tenm = (ph.ivis == 2);
+    if constexpr (DIR == 0) {
+        f[RH] = M_x;
+        if (!tenm) {
+            f[MX] = M_x * vx + P + P_xx - Sxx;
+            f[MY] = M_y * vx + P_xy - Sxy;
+            f[MZ] = M_z * vx + P_xz - Sxz;
+        } else {
+            f[MX] = P_xx - P_10 + P_5;
+            f[MY] = P_xy;
+            f[MZ] = P_xz;
+        }
+        f[EN] = (Ener + P) * vx + (P_xx - Sxx) * vx + (P_xy - Sxy) * vy + (P_xz - Sxz) * vz;
+        if (!tenm) {
+            f[PXX] = c4d3cv * vx; f[PYY] = -c2d3cv * vx; f[PZZ] = -c2d3cv * vx;
+            f[PXY] = colvis * vy; f[PXZ] = colvis * vz; f[PYZ] = T(0);
+        } else {
+            f[PXX] = vx * (T(3) * P_xx - T(2) * vx * M_x);
+            f[PYY] = T(2) * vy * (P_xy - vy * M_x) + vx * P_yy;
+            f[PZZ] = T(2) * vz * (P_xz - vz * M_x) + vx * P_zz;
+            f[PXY] = T(2) * vx * (P_xy - vy * M_x) + vy * P_xx;
+            f[PXZ] = T(2) * vx * (P_xz - vz * M_x) + vz * P_xx;
+            f[PYZ] = vx * P_yz + vy * P_xz + vz * P_xy - T(2) * vy * vz * M_x;
+        }
+    } else if constexpr (DIR == 1) {
+        f[RH] = M_y;
+        if (!tenm) {
+            f[MX] = M_x * vy + P_xy - Sxy;
+            f[MY] = M_y * vy + P + P_yy - Syy;
+            f[MZ] = M_z * vy + P_yz - Syz;
+        } else {
+            f[MX] = P_xy;
+            f[MY] = P_yy - P_10 + P_5;
+            f[MZ] = P_yz;
+        }
+        f[EN] = (Ener + P) * vy + (P_yy - Syy) * vy + (P_xy - Sxy) * vx + (P_yz - Syz) * vz;
+        if (!tenm) {
+            f[PXX] = -c2d3cv * vy; f[PYY] = c4d3cv * vy; f[PZZ] = -c2d3cv * vy;
+            f[PXY] = colvis * vx; f[PXZ] = T(0); f[PYZ] = colvis * vz;
+        } else {
+            f[PXX] = T(2) * vx * (P_xy - vx * M_y) + vy * P_xx;
+            f[PYY] = vy * (T(3) * P_yy - T(2) * vy * M_y);
+            f[PZZ] = T(2) * vz * (P_yz - vz * M_y) + vy * P_zz;
+            f[PXY] = T(2) * vy * (P_xy - vx * M_y) + vx * P_yy;
+            f[PXZ] = vx * P_yz + vy * P_xz + vz * P_xy - T(2) * vx * vz * M_y;
+            f[PYZ] = T(2) * vy * (P_yz - vz * M_y) + vz * P_yy;
+        }
+    } else {
+        f[RH] = M_z;
+        if (!tenm) {
+            f[MX] = M_x * vz + P_xz - Sxz;
+            f[MY] = M_y * vz + P_yz - Syz;
+            f[MZ] = M_z * vz + P + P_zz - Szz;
+        } else {
+            f[MX] = P_xz;
+            f[MY] = P_yz;
+            f[MZ] = P_zz - P_10 + P_5;
+        }
+        f[EN] = (Ener + P) * vz + (P_zz - Szz) * vz + (P_xz - Sxz) * vx + (P_yz - Syz) * vy;
+        if (!tenm) {
+            f[PXX] = -c2d3cv * vz; f[PYY] = -c2d3cv * vz; f[PZZ] = c4d3cv * vz;
+            f[PXY] = T(0); f[PXZ] = colvis * vx; f[PYZ] = colvis * vy;
+        } else {
+            f[PXX] = T(2) * vx * (P_xz - vx * M_z) + vz * P_xx;
+            f[PYY] = T(2) * vy * (P_yz - vy * M_z) + vz * P_yy;
+            f[PZZ] = vz * (T(3) * P_zz - T(2) * vz * M_z);
+            f[PXY] = vx * P_yz + vy * P_xz + vz * P_xy - T(2) * vx * vy * M_z;
+            f[PXZ] = T(2) * vz * (P_xz - vx * M_z) + vx * P_zz;
+            f[PYZ] = T(2) * vz * (P_yz - vy * M_z) + vy * P_zz;
+        }
+    }
+}
+
+// flux.f90:1029-1072 cfcal: freezing speed |v_d| + c
+template <class T, int DIR>
+__device__ __forceinline__ T cfcal(const Phys& ph, const T q[NQ]) {
+    T dn = q[RH], dni = T(1) / dn;
+    T vx = q[MX] * dni, vy = q[MY] * dni, vz = q[MZ] * dni;
+    T P;
+    if (ph.ivis == 0 || ph.ivis == 1) P = T(ph.aindm1) * (q[EN] - T(0.5) * dn * (vx * vx + vy * vy + vz * vz));
+    else P = T(1.0 / 3.0) * (q[PXX] + q[PYY] + q[PZZ] - dn * (vx * vx + vy * vy + vz * vz));
+    T cs;
+    if (ph.ieos == 1) cs = sqrt(T(ph.aindex) * P * dni);
+    else cs = sqrt(T(7.2) * T(ph.P_1) * pow(dn, T(6.2)));
+    T vd = DIR == 0 ? vx : DIR == 1 ? vy : vz;
+    return fabs(vd) + cs;
+}
+
+// ---------------------------------------------------------------------------
+// flux.f90:466-647 flux_hllc (ibatten = 0) at one face point.  qL/qR, fL/fR:
+// left/right states and point fluxes.  rho_i_last: 1/rho of the last point of
+// the call (the reference's ieos-2 branch uses it for every point,
+// flux.f90:533-534,570-571); unused for ieos 1.  Writes rh..en of F.
+// ---------------------------------------------------------------------------
+template <class T, int DIR>
+__device__ __forceinline__ void hllc(const Phys& ph, const T qL[NQ], const T qR[NQ], const T fL[NQ], const T fR[NQ],
+                                     T rho_i_last, T F[NQ]) {
+    constexpr int IPAR = DIR == 0 ? MX : DIR == 1 ? MY : MZ;
+    constexpr int IP1 = DIR == 0 ? MY : DIR == 1 ? MZ : MX;
+    constexpr int IP2 = DIR == 0 ? MZ : DIR == 1 ? MX : MY;
+    const T aindex = T(ph.aindex), aindm1 = T(ph.aindm1);
+    const T rhoL = qL[RH], rhoR = qR[RH];
+    T ri = T(1) / rhoL;
+    const T uL = qL[IPAR] * ri, vL = qL[IP1] * ri, wL = qL[IP2] * ri;
+    ri = T(1) / rhoR;
+    const T uR = qR[IPAR] * ri, vR = qR[IP1] * ri, wR = qR[IP2] * ri;
+    T pL = aindm1 * (qL[EN] - T(0.5) * rhoL * (uL * uL + vL * vL + wL * wL));
+    T pR = aindm1 * (qR[EN] - T(0.5) * rhoR * (uR * uR + vR * vR + wR * wR));
+    T cL, cR;
+    if (ph.ieos == 2) {
+        pL = T(ph.P_1) * (pow(rhoL, T(7.2)) - T(1)) + T(ph.P_base) + pL;
+        pR = T(ph.P_1) * (pow(rhoR, T(7.2)) - T(1)) + T(ph.P_base) + pR;
+        cL = sqrt(T(7.2) * T(ph.P_1) * pow(rhoL, T(6.2)) + pL * rho_i_last);
+        cR = sqrt(T(7.2) * T(ph.P_1) * pow(rhoR, T(6.2)) + pR * rho_i_last);
+    } else {
+        cL = sqrt(aindex * pL / rhoL);
+        cR = sqrt(aindex * pR / rhoR);
+    }
+    // S_L = min(lambda_M(Q_l), lambda_M(Q_r)); S_R = max(lambda_P(Q_r), lambda_P(Q_l))
+    const T sL = fmin(uL - cL, uR - cR);
+    const T sR = fmax(uR + cR, uL + cL);
+    T sm_num = rhoR * uR * (sR - uR) - rhoL * uL * (sL - uL);
+    sm_num = sm_num + pL - pR;
+    T sm_den = rhoR * (sR - uR) - rhoL * (sL - uL);
+    if (sm_den == T(0)) sm_den = T(ph.rh_floor);
+    const T sM = sm_num / sm_den;
+    const T pstar = rhoL * (uL - sL) * (uL - sM) + pL;
+    // flux.f90:623-643: the last true condition wins
+    int which = -1;
+    if (sL > T(0)) which = 0;
+    if (sL <= T(0) && T(0) < sM) which = 1;
+    if (sM <= T(0) && T(0) <= sR) which = 2;
+    if (sR < T(0)) which = 3;
+    T out[5];
+    if (which == 0 || which == 3) {
+        const T* ff = which == 0 ? fL : fR;
+        out[0] = ff[RH]; out[1] = ff[IPAR]; out[2] = ff[IP1]; out[3] = ff[IP2]; out[4] = ff[EN];
+    } else if (which >= 0) {
+        const bool left = which == 1;
+        const T* q = left ? qL : qR;
+        const T* ff = left ? fL : fR;
+        const T s = left ? sL : sR, rho = left ? rhoL : rhoR, u = left ? uL : uR, p = left ? pL : pR;
+        T den = s - sM;
+        if (den == T(0)) den = T(ph.rh_floor);
+        const T slrm_i = T(1) / den;
+        const T sq = s - u;
+        const T Q0 = rho * sq * slrm_i;
+        const T Q1 = (sq * q[IPAR] + pstar - p) * slrm_i;
+        const T Q2 = sq * q[IP1] * slrm_i;
+        const T Q3 = sq * q[IP2] * slrm_i;
+        const T Q4 = (sq * q[EN] - p * u + pstar * sM) * slrm_i;
+        out[0] = ff[RH] + s * (Q0 - q[RH]);
+        out[1] = ff[IPAR] + s * (Q1 - q[IPAR]);
+        out[2] = ff[IP1] + s * (Q2 - q[IP1]);
+        out[3] = ff[IP2] + s * (Q3 - q[IP2]);
+        out[4] = ff[EN] + s * (Q4 - q[EN]);
+    } else {
+        const T nan = T(NAN);
+        out[0] = out[1] = out[2] = out[3] = out[4] = nan;
+    }
+    F[RH] = out[0]; F[IPAR] = out[1]; F[IP1] = out[2]; F[IP2] = out[3]; F[EN] = out[4];
+}
+
+}  // namespace hermes

@@ -1,0 +1,552 @@
+// hermes_api.cu -- the C ABI (include/hermes_gb300.h): contexts, stage and
+// step orchestration on one CUDA stream, CUDA-graph replay of whole steps.
+//
+// A step is (hermeshd.f90:53-62, integrator.f90:62-122):
+//   k_mindt + k_dt_finalize            dt from the cell averages of q (FP64)
+//   per RK stage: k_limit (in place)   prep_advance's limiter
+//                 k_face x, y, z       traces, boundary ghosts, Riemann fluxes
+//                 k_cell               quadrature, sources, update, RK combination
+// RK2: q1 = E(q); q = (q + E(q1))/2.  RK3: q1 = E(q); q1 = 3/4 q + 1/4 E(q1);
+// q = 1/3 q + 2/3 E(q1) -- the reference's arrays, with its Q_2 never needed
+// because each combination is fused into the stage that produces it.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "dg_launch.cuh"
+#include "hermes_gb300.h"
+
+using namespace hermes;
+
+namespace {
+
+struct GraphEntry {
+    const void* q;
+    const void* q1;
+    cudaGraphExec_t exec;
+};
+
+__global__ void k_set_dt(BoxState* st, int nbox, double dt) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nbox) st[b].dt = dt;
+}
+__global__ void k_set_t(BoxState* st, int nbox, double t) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nbox) st[b].t = t;
+}
+__global__ void k_set_step(unsigned long long* step, unsigned long long s) {
+    step[0] = s;
+    step[1] = s;
+}
+// dt = cflm / ((vmag + cs_last) * dxi); t += dt; one thread per box
+__global__ void k_dt_finalize(const Box* __restrict__ boxes, int nbox, BoxState* st, unsigned long long* step) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b == 0) { step[0] = step[1]; step[1] = step[1] + 1; }
+    if (b >= nbox) return;
+    const double vmag = __longlong_as_double((long long)st[b].vmag_bits);
+    const double vmax = (vmag + st[b].cs_last) * boxes[b].di[0];   // hermeshd.f90:174 uses dxi only
+    const double dt = boxes[b].cflm / vmax;
+    st[b].dt = dt;
+    st[b].t = st[b].t + dt;
+    st[b].vmag_bits = 0ull;
+}
+
+__global__ void k_dt_finalize_only(const Box* __restrict__ boxes, int nbox, BoxState* st) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbox) return;
+    const double vmag = __longlong_as_double((long long)st[b].vmag_bits);
+    st[b].dt = boxes[b].cflm / ((vmag + st[b].cs_last) * boxes[b].di[0]);
+    st[b].vmag_bits = 0ull;
+}
+
+}  // namespace
+
+struct hermes_ctx {
+    hermes_config cfg;
+    KernelSet K;
+    int device = 0;
+    cudaStream_t stream = nullptr;       // private stream (graph capture needs a non-legacy stream)
+    cudaStream_t user_stream = nullptr;  // the caller's stream; work is ordered against it both ways
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    std::vector<Box> h_boxes;
+    Box* d_boxes = nullptr;
+    Geom G{};
+    Phys ph{};
+    BoxState* d_st = nullptr;
+    unsigned long long* d_step = nullptr;
+    int* d_flags = nullptr;
+    void* d_flux = nullptr;
+    size_t flux_elems = 0;
+    size_t q_elems = 0;
+    void* d_q[2] = {nullptr, nullptr};
+    std::vector<GraphEntry> graphs;
+    std::string err;
+};
+
+namespace {
+
+int fail(hermes_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(hermes_ctx* c, const char* what, cudaError_t e) {
+    return fail(c, HERMES_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define HCK(ctx, call)                                               \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), #call, e_);   \
+    } while (0)
+
+bool pick_kernels(const hermes_config& c, KernelSet& K) {
+    if (c.precision == 64) {
+        if (c.nbasis == 4 && c.iquad == 2) { K = kernels_f64_nb4(); return true; }
+        if (c.nbasis == 8 && c.iquad == 2) { K = kernels_f64_nb8(); return true; }
+        if (c.nbasis == 10 && c.iquad == 3) { K = kernels_f64_nb10(); return true; }
+    } else if (c.precision == 32) {
+        if (c.nbasis == 4 && c.iquad == 2) { K = kernels_f32_nb4(); return true; }
+        if (c.nbasis == 8 && c.iquad == 2) { K = kernels_f32_nb8(); return true; }
+        if (c.nbasis == 10 && c.iquad == 3) { K = kernels_f32_nb10(); return true; }
+    }
+    return false;
+}
+
+std::string check_config(const hermes_config& c) {
+    if (!((c.nbasis == 4 && c.iquad == 2) || (c.nbasis == 8 && c.iquad == 2) || (c.nbasis == 10 && c.iquad == 3)))
+        return "unsupported (nbasis, iquad): supported are (4,2), (8,2), (10,3)";
+    if (c.precision != 64 && c.precision != 32) return "precision must be 64 or 32";
+    if (c.nx < 1 || c.ny < 1 || c.nz < 1) return "grid dimensions must be >= 1";
+    if (c.ivis < 0 || c.ivis > 2) return "ivis must be 0, 1 or 2";
+    if (c.ieos != 1 && c.ieos != 2) return "ieos must be 1 or 2";
+    if (c.iorder != 2 && c.iorder != 3) return "iorder must be 2 or 3";
+    for (int i = 0; i < 6; ++i)
+        if (c.bc[i] < 0 || c.bc[i] > 3) return "boundary codes must be 0..3";
+    if (!(c.lx > 0 && c.ly > 0 && c.lz > 0)) return "domain lengths must be positive";
+    return "";
+}
+
+double default_cflm(int iquad) {  // initialize.f90:104-122
+    return iquad == 2 ? 0.14 : iquad == 3 ? 0.08 : iquad == 4 ? 0.05 : 0.14;
+}
+
+Phys make_phys(const hermes_config& c) {
+    Phys p{};
+    p.aindex = c.aindex;
+    p.aindm1 = c.aindex - 1.0;
+    p.rh_floor = c.rh_floor;
+    p.T_floor = c.T_floor;
+    p.P_floor = c.T_floor * c.rh_floor;
+    p.rh_mult = c.rh_mult;
+    p.coll = c.coll;
+    p.colvis = c.colvis;
+    p.P_1 = c.P_1;
+    p.P_base = c.P_base;
+    p.eta_sd = c.eta_sd;
+    p.zeta_sd = c.zeta_sd;
+    p.body_force = c.body_force;
+    p.ivis = c.ivis;
+    p.ieos = c.ieos;
+    p.ihllc = c.ihllc ? 1 : 0;
+    p.llns = c.llns ? 1 : 0;
+    return p;
+}
+
+// geometry of nbox boxes; sizes in elements
+void make_boxes(const hermes_config& c, int nbox, const int32_t* dims, const double* lengths, const uint64_t* seeds,
+                int nf, std::vector<Box>& boxes, long long& ncell, long long nface[3], size_t& q_elems, size_t& flux_elems) {
+    boxes.resize(nbox);
+    ncell = 0;
+    nface[0] = nface[1] = nface[2] = 0;
+    for (int i = 0; i < nbox; ++i) {
+        Box& b = boxes[i];
+        std::memset(&b, 0, sizeof(Box));
+        b.n[0] = dims ? dims[3 * i] : c.nx;
+        b.n[1] = dims ? dims[3 * i + 1] : c.ny;
+        b.n[2] = dims ? dims[3 * i + 2] : c.nz;
+        for (int k = 0; k < 6; ++k) b.bc[k] = c.bc[k];
+        for (int d = 0; d < 3; ++d)
+            b.nfp[d] = (c.bc[2 * d] == HERMES_BC_PERIODIC && c.bc[2 * d + 1] == HERMES_BC_PERIODIC) ? b.n[d] : b.n[d] + 1;
+        b.ncell = (long long)b.n[0] * b.n[1] * b.n[2];
+        b.cell0 = ncell;
+        b.q0 = ncell * (long long)c.nbasis * NQ;
+        ncell += b.ncell;
+        const double L[3] = {lengths ? lengths[3 * i] : c.lx, lengths ? lengths[3 * i + 1] : c.ly,
+                             lengths ? lengths[3 * i + 2] : c.lz};
+        for (int d = 0; d < 3; ++d) b.di[d] = (double)b.n[d] / L[d];   // initialize.f90:317-319
+        b.cflm = c.cflm > 0 ? c.cflm : default_cflm(c.iquad);
+        b.seed = seeds ? seeds[i] : c.seed + (uint64_t)i;
+        for (int d = 0; d < 3; ++d) {
+            long long f = 1;
+            for (int e = 0; e < 3; ++e) f *= (e == d ? b.nfp[e] : b.n[e]);
+            b.face0[d] = nface[d];
+            nface[d] += f;
+        }
+    }
+    q_elems = (size_t)ncell * c.nbasis * NQ;
+    // flux buffer: all x faces, then all y faces, then all z faces
+    long long start[3];
+    start[0] = 0;
+    start[1] = nface[0] * NQ * nf;
+    start[2] = start[1] + nface[1] * NQ * nf;
+    flux_elems = (size_t)(start[2] + nface[2] * NQ * nf);
+    for (int i = 0; i < nbox; ++i)
+        for (int d = 0; d < 3; ++d) boxes[i].fbase[d] = start[d] + boxes[i].face0[d] * NQ * nf;
+}
+
+void destroy_graphs(hermes_ctx* c) {
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+}
+
+// ---- enqueue helpers ---------------------------------------------------
+void enq_limit(hermes_ctx* c, void* q) {
+    if (c->cfg.ieos == 1 || c->cfg.ieos == 2) c->K.limit(q, c->G, c->ph, c->stream);   // integrator.f90:110
+}
+void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
+    FaceArgs a{c->G, c->ph, c->d_step, stage};
+    for (int d = 0; d < 3; ++d) c->K.face(d, q, c->d_flux, a, c->stream);
+}
+void enq_cell(hermes_ctx* c, const void* qin, const void* q0, void* out, int mode, int comb, unsigned stage) {
+    CellArgs a{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb};
+    c->K.cell(qin, q0, out, c->d_flux, a, c->stream);
+}
+void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, unsigned stage) {
+    enq_limit(c, qin);
+    enq_faces(c, qin, stage);
+    enq_cell(c, qin, q0, out, MODE_STAGE, comb, stage);
+}
+void enq_mindt(hermes_ctx* c, const void* q, bool advance) {
+    DtArgs a{c->G, c->ph, c->d_st};
+    c->K.mindt(q, a, c->stream);
+    const int nb = c->G.nbox, tpb = 128;
+    if (advance) k_dt_finalize<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st, c->d_step);
+    else k_dt_finalize_only<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st);
+}
+void enq_step(hermes_ctx* c, void* q, void* q1) {
+    enq_mindt(c, q, true);                           // hermeshd.f90:59
+    enq_stage(c, q, nullptr, q1, COMB_NONE, 0);      // Q_1 = E(Q)
+    if (c->cfg.iorder == 3) {
+        enq_stage(c, q1, q, q1, COMB_34, 1);         // Q_1 = 3/4 Q + 1/4 E(Q_1)
+        enq_stage(c, q1, q, q, COMB_13, 2);          // Q = 1/3 Q + 2/3 E(Q_1)
+    } else {
+        enq_stage(c, q1, q, q, COMB_HALF, 1);        // Q = (Q + E(Q_1))/2
+    }
+}
+
+int launch_status(hermes_ctx* c) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, "kernel launch", e);
+    return HERMES_OK;
+}
+
+// order the private stream after the caller's stream, and back
+int enter(hermes_ctx* c) {
+    HCK(c, cudaSetDevice(c->device));
+    HCK(c, cudaEventRecord(c->ev_in, c->user_stream));
+    HCK(c, cudaStreamWaitEvent(c->stream, c->ev_in, 0));
+    return HERMES_OK;
+}
+int leave(hermes_ctx* c, int rc) {
+    if (cudaEventRecord(c->ev_out, c->stream) != cudaSuccess ||
+        cudaStreamWaitEvent(c->user_stream, c->ev_out, 0) != cudaSuccess) {
+        cudaGetLastError();
+        if (rc == HERMES_OK) return fail(c, HERMES_ERR_CUDA, "stream ordering");
+    }
+    return rc;
+}
+
+int read_back(hermes_ctx* c, double* t, double* dt) {
+    BoxState s0;
+    int flags = 0;
+    HCK(c, cudaMemcpyAsync(&s0, c->d_st, sizeof(BoxState), cudaMemcpyDeviceToHost, c->stream));
+    HCK(c, cudaMemcpyAsync(&flags, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    HCK(c, cudaStreamSynchronize(c->stream));
+    if (t) *t = s0.t;
+    if (dt) *dt = s0.dt;
+    if (flags & FLAG_NONFINITE) {
+        HCK(c, cudaMemsetAsync(c->d_flags, 0, sizeof(int), c->stream));
+        return fail(c, HERMES_ERR_NONFINITE, "NaN cell average produced by the step (integrator.f90:234-250)");
+    }
+    return HERMES_OK;
+}
+
+int get_graph(hermes_ctx* c, void* q, void* q1, cudaGraphExec_t* out) {
+    for (auto& g : c->graphs)
+        if (g.q == q && g.q1 == q1) { *out = g.exec; return HERMES_OK; }
+    cudaGraph_t graph;
+    HCK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enq_step(c, q, q1);
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
+    if (le != cudaSuccess) { if (ee == cudaSuccess) cudaGraphDestroy(graph); return cuda_fail(c, "launch in capture", le); }
+    HCK(c, ee);
+    cudaGraphExec_t exec;
+    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    HCK(c, ie);
+    if (c->graphs.size() >= 8) destroy_graphs(c);
+    c->graphs.push_back(GraphEntry{q, q1, exec});
+    *out = exec;
+    return HERMES_OK;
+}
+
+int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const double* lengths, const uint64_t* seeds,
+                void* stream, hermes_ctx** out) {
+    if (!cfg || !out) return HERMES_ERR_ARG;
+    *out = nullptr;
+    std::string msg = check_config(*cfg);
+    if (!msg.empty()) { fprintf(stderr, "hermes_create: %s\n", msg.c_str()); return HERMES_ERR_CONFIG; }
+    if (nbox < 1) return HERMES_ERR_ARG;
+    if (dims)
+        for (int i = 0; i < 3 * nbox; ++i)
+            if (dims[i] < 1) return HERMES_ERR_CONFIG;
+    hermes_ctx* c = new (std::nothrow) hermes_ctx();
+    if (!c) return HERMES_ERR_ALLOC;
+    c->cfg = *cfg;
+    pick_kernels(*cfg, c->K);
+    cudaGetDevice(&c->device);
+    c->ph = make_phys(*cfg);
+    long long ncell, nface[3];
+    make_boxes(*cfg, nbox, dims, lengths, seeds, c->K.nf, c->h_boxes, ncell, nface, c->q_elems, c->flux_elems);
+    c->G.nbox = nbox;
+    c->G.ncell = ncell;
+    for (int d = 0; d < 3; ++d) c->G.nface[d] = nface[d];
+    auto bail = [&](int code) { hermes_destroy(c); return code; };
+    c->user_stream = static_cast<cudaStream_t>(stream);
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming);
+        if (e != cudaSuccess) { fprintf(stderr, "hermes_create: %s\n", cudaGetErrorString(e)); return bail(HERMES_ERR_CUDA); }
+    }
+    if (cudaMalloc(&c->d_boxes, sizeof(Box) * nbox) != cudaSuccess ||
+        cudaMalloc(&c->d_st, sizeof(BoxState) * nbox) != cudaSuccess ||
+        cudaMalloc(&c->d_step, sizeof(unsigned long long) * 2) != cudaSuccess ||
+        cudaMalloc(&c->d_flags, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&c->d_flux, c->flux_elems * c->K.elem_size) != cudaSuccess) {
+        cudaGetLastError();
+        fprintf(stderr, "hermes_create: device allocation of %zu bytes failed\n", c->flux_elems * c->K.elem_size);
+        return bail(HERMES_ERR_ALLOC);
+    }
+    c->G.boxes = c->d_boxes;
+    if (cudaMemcpy(c->d_boxes, c->h_boxes.data(), sizeof(Box) * nbox, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(c->d_st, 0, sizeof(BoxState) * nbox) != cudaSuccess ||
+        cudaMemset(c->d_step, 0, sizeof(unsigned long long) * 2) != cudaSuccess ||
+        cudaMemset(c->d_flags, 0, sizeof(int)) != cudaSuccess ||
+        c->K.prepare() != cudaSuccess) {
+        cudaGetLastError();
+        return bail(HERMES_ERR_CUDA);
+    }
+    // initial dt of initialize.f90:343 is superseded by get_min_dt in step
+    *out = c;
+    return HERMES_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int hermes_abi_version(void) { return HERMES_ABI_VERSION; }
+
+int hermes_config_size(void) { return (int)sizeof(hermes_config); }
+
+int hermes_sizes(const hermes_config* cfg, size_t* q_elems, size_t* scratch_bytes) {
+    if (!cfg) return HERMES_ERR_ARG;
+    if (!check_config(*cfg).empty()) return HERMES_ERR_CONFIG;
+    KernelSet K;
+    pick_kernels(*cfg, K);
+    std::vector<Box> boxes;
+    long long ncell, nface[3];
+    size_t qe, fe;
+    make_boxes(*cfg, 1, nullptr, nullptr, nullptr, K.nf, boxes, ncell, nface, qe, fe);
+    if (q_elems) *q_elems = qe;
+    if (scratch_bytes) *scratch_bytes = fe * K.elem_size;
+    return HERMES_OK;
+}
+
+int hermes_create(const hermes_config* cfg, void* stream, hermes_ctx** out) {
+    return create_impl(cfg, 1, nullptr, nullptr, nullptr, stream, out);
+}
+
+int hermes_ensemble_create(const hermes_config* cfg, int nbox, const int32_t* dims, const double* lengths,
+                           const uint64_t* seeds, void* stream, hermes_ctx** out) {
+    if (!dims) return HERMES_ERR_ARG;
+    return create_impl(cfg, nbox, dims, lengths, seeds, stream, out);
+}
+
+int hermes_box_offsets(hermes_ctx* c, int64_t* offsets) {
+    if (!c || !offsets) return HERMES_ERR_ARG;
+    for (int i = 0; i < c->G.nbox; ++i) offsets[i] = c->h_boxes[i].q0;
+    offsets[c->G.nbox] = (int64_t)c->q_elems;
+    return HERMES_OK;
+}
+
+int hermes_destroy(hermes_ctx* c) {
+    if (!c) return HERMES_ERR_ARG;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    destroy_graphs(c);
+    cudaFree(c->d_boxes);
+    cudaFree(c->d_st);
+    cudaFree(c->d_step);
+    cudaFree(c->d_flags);
+    cudaFree(c->d_flux);
+    cudaFree(c->d_q[0]);
+    cudaFree(c->d_q[1]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->ev_in) cudaEventDestroy(c->ev_in);
+    if (c->ev_out) cudaEventDestroy(c->ev_out);
+    delete c;
+    return HERMES_OK;
+}
+
+const char* hermes_last_error(hermes_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+void* hermes_stream(hermes_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int hermes_get_min_dt(hermes_ctx* c, const void* q, double* dt_out) {
+    if (!c || !q || !dt_out) return fail(c, HERMES_ERR_ARG, "null argument");
+    int rc = enter(c);
+    if (rc) return rc;
+    enq_mindt(c, q, false);
+    rc = launch_status(c);
+    if (rc) return leave(c, rc);
+    BoxState s0;
+    HCK(c, cudaMemcpyAsync(&s0, c->d_st, sizeof(BoxState), cudaMemcpyDeviceToHost, c->stream));
+    HCK(c, cudaStreamSynchronize(c->stream));
+    *dt_out = s0.dt;
+    return leave(c, HERMES_OK);
+}
+
+int hermes_limiter(hermes_ctx* c, void* q) {
+    if (!c || !q) return fail(c, HERMES_ERR_ARG, "null argument");
+    int rc = enter(c);
+    if (rc) return rc;
+    c->K.limit(q, c->G, c->ph, c->stream);
+    return leave(c, launch_status(c));
+}
+
+int hermes_rhs(hermes_ctx* c, void* q, void* rhs, int apply_limiter) {
+    if (!c || !q || !rhs) return fail(c, HERMES_ERR_ARG, "null argument");
+    if (q == rhs) return fail(c, HERMES_ERR_ARG, "rhs must not alias q");
+    int rc = enter(c);
+    if (rc) return rc;
+    if (apply_limiter) enq_limit(c, q);
+    enq_faces(c, q, 0);
+    enq_cell(c, q, nullptr, rhs, MODE_RHS, COMB_NONE, 0);
+    return leave(c, launch_status(c));
+}
+
+int hermes_euler_stage(hermes_ctx* c, void* q_in, void* q_out, double dt) {
+    if (!c || !q_in || !q_out) return fail(c, HERMES_ERR_ARG, "null argument");
+    int rc = enter(c);
+    if (rc) return rc;
+    const int nb = c->G.nbox;
+    k_set_dt<<<(nb + 127) / 128, 128, 0, c->stream>>>(c->d_st, nb, dt);
+    enq_stage(c, q_in, nullptr, q_out, COMB_NONE, 0);
+    return leave(c, launch_status(c));
+}
+
+int hermes_set_time(hermes_ctx* c, double t) {
+    if (!c) return HERMES_ERR_ARG;
+    int rc = enter(c);
+    if (rc) return rc;
+    const int nb = c->G.nbox;
+    k_set_t<<<(nb + 127) / 128, 128, 0, c->stream>>>(c->d_st, nb, t);
+    return leave(c, launch_status(c));
+}
+
+int hermes_step(hermes_ctx* c, void* q, void* q1, void* q2, double* t, double* dt) {
+    (void)q2;
+    if (!c || !q || !q1) return fail(c, HERMES_ERR_ARG, "null argument");
+    if (q == q1) return fail(c, HERMES_ERR_ARG, "q and q1 must be distinct arrays");
+    int rc = enter(c);
+    if (rc) return rc;
+    if (t && c->G.nbox == 1) k_set_t<<<1, 32, 0, c->stream>>>(c->d_st, 1, *t);
+    enq_step(c, q, q1);
+    rc = launch_status(c);
+    if (rc == HERMES_OK) rc = read_back(c, t, dt);
+    return leave(c, rc);
+}
+
+namespace {
+int advance_impl(hermes_ctx* c, void* q, void* q1, int nsteps, double* t, double* dt) {
+    if (t && c->G.nbox == 1) k_set_t<<<1, 32, 0, c->stream>>>(c->d_st, 1, *t);
+    int rc = launch_status(c);
+    if (rc) return rc;
+    cudaGraphExec_t exec;
+    rc = get_graph(c, q, q1, &exec);
+    if (rc) return rc;
+    for (int s = 0; s < nsteps; ++s) HCK(c, cudaGraphLaunch(exec, c->stream));
+    return read_back(c, t, dt);
+}
+}  // namespace
+
+int hermes_advance(hermes_ctx* c, void* q, void* q1, void* q2, int nsteps, double* t, double* dt) {
+    (void)q2;
+    if (!c || !q || !q1 || nsteps < 0) return fail(c, HERMES_ERR_ARG, "bad argument");
+    if (q == q1) return fail(c, HERMES_ERR_ARG, "q and q1 must be distinct arrays");
+    int rc = enter(c);
+    if (rc) return rc;
+    return leave(c, advance_impl(c, q, q1, nsteps, t, dt));
+}
+
+int hermes_advance_host(hermes_ctx* c, void* q_host, int nsteps, double* t, double* dt) {
+    if (!c || !q_host || nsteps < 0) return fail(c, HERMES_ERR_ARG, "bad argument");
+    int rc = enter(c);
+    if (rc) return rc;
+    const size_t bytes = c->q_elems * c->K.elem_size;
+    for (int i = 0; i < 2; ++i)
+        if (!c->d_q[i] && cudaMalloc(&c->d_q[i], bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return leave(c, fail(c, HERMES_ERR_ALLOC, "device buffers for host-array stepping"));
+        }
+    HCK(c, cudaMemcpyAsync(c->d_q[0], q_host, bytes, cudaMemcpyHostToDevice, c->stream));
+    rc = advance_impl(c, c->d_q[0], c->d_q[1], nsteps, t, dt);
+    if (rc) return leave(c, rc);
+    HCK(c, cudaMemcpyAsync(q_host, c->d_q[0], bytes, cudaMemcpyDeviceToHost, c->stream));
+    HCK(c, cudaStreamSynchronize(c->stream));
+    return leave(c, HERMES_OK);
+}
+
+int hermes_box_times(hermes_ctx* c, double* t, double* dt) {
+    if (!c) return HERMES_ERR_ARG;
+    int rc = enter(c);
+    if (rc) return rc;
+    std::vector<BoxState> s(c->G.nbox);
+    HCK(c, cudaMemcpyAsync(s.data(), c->d_st, sizeof(BoxState) * s.size(), cudaMemcpyDeviceToHost, c->stream));
+    HCK(c, cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < s.size(); ++i) {
+        if (t) t[i] = s[i].t;
+        if (dt) dt[i] = s[i].dt;
+    }
+    return leave(c, HERMES_OK);
+}
+
+int hermes_set_noise_step(hermes_ctx* c, uint64_t step) {
+    if (!c) return HERMES_ERR_ARG;
+    int rc = enter(c);
+    if (rc) return rc;
+    k_set_step<<<1, 1, 0, c->stream>>>(c->d_step, (unsigned long long)step);
+    return leave(c, launch_status(c));
+}
+
+int hermes_check(hermes_ctx* c) {
+    if (!c) return HERMES_ERR_ARG;
+    int rc = enter(c);
+    if (rc) return rc;
+    rc = launch_status(c);
+    if (rc == HERMES_OK) rc = read_back(c, nullptr, nullptr);
+    return leave(c, rc);
+}
+
+}  // extern "C"

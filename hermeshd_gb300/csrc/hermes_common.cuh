@@ -1,0 +1,77 @@
+// hermes_common.cuh -- shared device types and compile-time helpers of the
+// GB300 DG step.  Layout of one grid ("box"): the reference's Fortran
+// Q(nx,ny,nz,nQ,nbasis), i.e. element (b, v, cell) at (b*NQ + v)*ncell + cell
+// with cell = i + nx*(j + ny*k).  An ensemble stores its boxes back to back.
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+#include <utility>
+
+#include "dg_tables_gen.cuh"
+
+namespace hermes {
+
+constexpr int NQ = 11;  // params.f90:47
+enum Var { RH = 0, MX, MY, MZ, EN, PXX, PYY, PZZ, PXY, PXZ, PYZ };
+enum Bc { BC_PERIODIC = 0, BC_OUTFLOW = 1, BC_WALL = 2, BC_NOSLIP = 3 };
+
+// device error flags (plain stores; read by the host after a step)
+enum Flag { FLAG_NONFINITE = 1 };
+
+// compile-time loop: f(std::integral_constant<int, i>) for i in [0, N)
+template <class F, int... I>
+__device__ __forceinline__ void sfor_impl(F&& f, std::integer_sequence<int, I...>) {
+    (f(std::integral_constant<int, I>{}), ...);
+}
+template <int N, class F>
+__device__ __forceinline__ void sfor(F&& f) {
+    sfor_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+// physics constants (params.f90 / input.f90), identical for every box
+struct Phys {
+    double aindex, aindm1, rh_floor, T_floor, P_floor, rh_mult;
+    double coll, colvis, P_1, P_base;
+    double eta_sd, zeta_sd, body_force;
+    int ivis, ieos, ihllc, llns;
+};
+
+// one grid of the run (one realisation of an ensemble)
+struct Box {
+    int n[3];                 // nx, ny, nz
+    int nfp[3];               // face planes per direction: n (both ends periodic) or n+1
+    int bc[6];                // xlo, xhi, ylo, yhi, zlo, zhi
+    int pad_;
+    long long ncell;          // nx*ny*nz
+    long long cell0;          // first cell of this box in the global cell numbering
+    long long q0;             // first element of this box in a Q buffer
+    long long face0[3];       // first face of this box in the global face numbering, per direction
+    long long fbase[3];       // first element of this box's face-flux array, per direction
+    double di[3];             // dxi, dyi, dzi
+    double cflm;
+    unsigned long long seed;  // Philox key of the stochastic stress
+};
+
+// per-box device scalars
+struct BoxState {
+    double dt, t;
+    unsigned long long vmag_bits;  // max wave speed (bit pattern of a non-negative double)
+    double cs_last;                // sound speed of the last cell (hermeshd.f90:174)
+};
+
+// box of a global index: boxes sorted by `first`, binary search
+template <class Getter>
+__device__ __forceinline__ int find_box(const Box* __restrict__ boxes, int nbox, long long idx, Getter first) {
+    int lo = 0, hi = nbox - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (first(boxes[mid]) <= idx) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <class T>
+__device__ __forceinline__ T tfma(T a, T b, T c) { return fma(a, b, c); }
+
+}  // namespace hermes

@@ -1,0 +1,145 @@
+"""The reference's Python call surface (src/hermeshd.py:5-120), over the GB300 path.
+
+Usage mirrors src/test_hermeshd.py:37-83::
+
+    from hermeshd_gb300 import hermeshd, config
+    hermeshd.hermeshd.configure(config.sod_1d())       # the reference: compile time
+    setup, step = hermeshd.hermeshd.setup, hermeshd.hermeshd.step
+    Qio = np.empty((nx, ny, nz, nQ, nB), order='F', dtype=np.float64)
+    Q1, Q2 = np.empty_like(Qio), np.empty_like(Qio)
+    t, dt = np.array(0.0), np.array(0.0)
+    ...
+    setup(Qio, t, dt, t1, t_start, dtout, nout, comm)
+    while t < tf:
+        step(Qio, Q1, Q2, t, dt)
+        generate_output(Qio, t, dt, t1, dtout, nout)
+    cleanup(t_start)
+
+Arrays may be numpy Fortran-ordered host arrays (copied to the device and
+back around each call, as the f2py extension works on host memory) or torch
+CUDA tensors of shape (nbasis, nQ, nz, ny, nx) (no copies).  Scalars are 0-d
+numpy arrays mutated in place, as in the reference, and are also returned.
+``comm`` is accepted and ignored (one GPU, no MPI).
+"""
+from __future__ import annotations
+
+import time
+from typing import Optional
+
+import numpy as np
+
+from . import ic as _ic
+from .config import Config
+from .solver import Solver
+
+
+def _set0d(a, v):
+    if isinstance(a, np.ndarray) and a.ndim == 0:
+        a[...] = v
+    return v
+
+
+def _get0d(a):
+    return float(a) if a is not None else 0.0
+
+
+class Hermeshd:
+    """Module hermeshd (src/hermeshd.f90:2-269)."""
+
+    def __init__(self):
+        self.cfg: Optional[Config] = None
+        self.icid: int = 3
+        self.solver: Optional[Solver] = None
+        self._dev = None
+
+    # ---- configuration (compile-time constants in the reference) --------
+    def configure(self, cfg: Config, icid: Optional[int] = None):
+        """Select the problem: src/input.f90 and src/params.f90 at run time.
+        icid follows initialcon.f90:41-69 (1/2 isentropic vortex v0/v1,
+        3/4 Sod v0/v1); other problems set their own initial state."""
+        cfg.validate()
+        self.cfg = cfg
+        if icid is not None:
+            self.icid = icid
+        if self.solver is not None:
+            self.solver.close()
+            self.solver = None
+
+    def _need(self):
+        if self.cfg is None:
+            raise RuntimeError("hermeshd: configure(cfg) before setup (the reference fixes it at compile time)")
+        if self.solver is None:
+            self.solver = Solver(self.cfg)
+        return self.solver
+
+    # ---- the wrapped subprograms (CMakeLists.txt:161) ---------------------
+    def main(self, comm=0):
+        """hermeshd.f90:26-48: setup; while t < tf: step, generate_output; cleanup."""
+        cfg = self.cfg
+        Q = np.zeros(cfg.shape_f, order="F", dtype=np.float64)
+        Q1, Q2 = np.zeros_like(Q), np.zeros_like(Q)
+        t, dt, t1, t_start, dtout, nout = (np.array(0.0), np.array(0.0), np.array(0.0), np.array(0.0),
+                                            np.array(0.0), np.array(0))
+        self.setup(Q, t, dt, t1, t_start, dtout, nout, comm)
+        while float(t) < cfg.tf:
+            self.step(Q, Q1, Q2, t, dt)
+            self.generate_output(Q, t, dt, t1, dtout, nout)
+        self.cleanup(t_start)
+        return Q
+
+    def setup(self, q_io, t, dt, t1, t_start, dtout, nout, comm=0):
+        """hermeshd.f90:67-114: initializer (tables, spacing, dt), initial
+        condition into q_io, integrator and boundary selection."""
+        s = self._need()
+        cfg = self.cfg
+        _set0d(t, 0.0)
+        _set0d(dt, cfg.cflm_eff * (cfg.lx / cfg.nx) / 2.0)      # initialize.f90:343 with clt = 2
+        _set0d(nout, 0)
+        now = time.time()
+        _set0d(t_start, now)
+        _set0d(dtout, cfg.tf / cfg.ntout)                      # hermeshd.f90:84
+        Q = {1: lambda: _ic.isentropic_vortex(cfg, 0), 2: lambda: _ic.isentropic_vortex(cfg, 1),
+             3: lambda: _ic.sod(cfg), 4: lambda: _ic.sod(cfg)}.get(self.icid, lambda: _ic.equilibrium(cfg))()
+        self._write(q_io, Q)
+        _set0d(t1, time.time())
+        s.set_time(0.0)
+        return t, dt
+
+    def _write(self, dst, Qf):
+        if isinstance(dst, np.ndarray):
+            dst[...] = Qf.astype(dst.dtype)
+        else:
+            dst.copy_(self.solver.from_numpy(Qf))
+
+    def step(self, q_io, q_1, q_2, t, dt):
+        """hermeshd.f90:53-62: dt = get_min_dt(Q); update(Q, Q1, Q2, dt); t += dt."""
+        s = self._need()
+        if isinstance(q_io, np.ndarray):
+            # host arrays: copy in, step, copy back (Q_1 returned as well)
+            dq, d1 = s.from_numpy(q_io), s.from_numpy(q_1)
+            tn, dtn = s.step(dq, d1, None, _get0d(t))
+            q_io[...] = s.to_numpy(dq)
+            q_1[...] = s.to_numpy(d1)
+        else:
+            tn, dtn = s.step(q_io, q_1, q_2, _get0d(t))
+        _set0d(t, tn)
+        _set0d(dt, dtn)
+        return tn, dtn
+
+    def generate_output(self, q_r, t, dt, t1, dtout, nout):
+        """hermeshd.f90:206-266: the output cadence (VTK writing is out of
+        scope; the cadence counter advances as in the reference)."""
+        if _get0d(t) >= _get0d(nout) * _get0d(dtout):
+            _set0d(nout, int(_get0d(nout)) + 1)
+        return nout
+
+    def cleanup(self, t_start):
+        """hermeshd.f90:119-138: release resources, report wall time."""
+        wall = time.time() - _get0d(t_start)
+        if self.solver is not None:
+            self.solver.close()
+            self.solver = None
+        return wall
+
+
+hermeshd = Hermeshd()

@@ -1,0 +1,156 @@
+"""Initial conditions (host side, numpy).
+
+These build the caller-owned state array ``Q(nx,ny,nz,nQ,nbasis)`` (Fortran
+order, float64) that ``setup``/``step`` then advance.  They are fixtures for
+the benchmark problems, not part of the hot path.  Where the reference has the
+problem, the routine follows ``src/initialcon.f90`` line by line; only the
+cell averages (basis function 1) are set, as there.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .config import Config, NQ
+
+RH, MX, MY, MZ, EN, PXX, PYY, PZZ, PXY, PXZ, PYZ = range(NQ)
+
+
+def empty_state(cfg: Config, dtype=np.float64) -> np.ndarray:
+    return np.zeros(cfg.shape_f, dtype=dtype, order="F")
+
+
+def cell_centres(cfg: Config):
+    """params.f90:212-227 xc/yc/zc with the domain centred at the origin
+    (initialize.f90:310-326): xc(i) = -lx/2 + (i - 1/2) dx."""
+    dx, dy, dz = cfg.lx / cfg.nx, cfg.ly / cfg.ny, cfg.lz / cfg.nz
+    xc = -cfg.lx / 2 + (np.arange(1, cfg.nx + 1) - 0.5) * dx
+    yc = -cfg.ly / 2 + (np.arange(1, cfg.ny + 1) - 0.5) * dy
+    zc = -cfg.lz / 2 + (np.arange(1, cfg.nz + 1) - 0.5) * dz
+    return xc, yc, zc
+
+
+def _background(cfg: Config) -> np.ndarray:
+    """initialcon.f90:35-37: zero state with floor density and energy."""
+    Q = empty_state(cfg)
+    Q[:, :, :, RH, 0] = cfg.rh_floor
+    Q[:, :, :, EN, 0] = cfg.T_floor * cfg.rh_floor / (cfg.aindex - 1.0)
+    return Q
+
+
+def _set_hydro(Q, dn, vx, vy, vz, pr, gamma):
+    Q[:, :, :, RH, 0] = dn
+    Q[:, :, :, MX, 0] = dn * vx
+    Q[:, :, :, MY, 0] = dn * vy
+    Q[:, :, :, MZ, 0] = dn * vz
+    Q[:, :, :, EN, 0] = pr / (gamma - 1.0) + 0.5 * dn * (vx ** 2 + vy ** 2 + vz ** 2)
+
+
+def sod(cfg: Config, p_hi: float = 1.0, p_lo: float = 0.1, rh_hi: float = 1.0, rh_lo: float = 0.125) -> np.ndarray:
+    """initialcon.f90:190-235 sod_shock_tube_1d, version 0 (diaphragm at
+    xc = 0, i.e. x = 0.5 of [0, 1])."""
+    Q = _background(cfg)
+    xc, yc, zc = cell_centres(cfg)
+    X = np.broadcast_to(xc[:, None, None], (cfg.nx, cfg.ny, cfg.nz))
+    left = X <= 0
+    dn = np.where(left, rh_hi, rh_lo)
+    pr = np.where(left, p_hi, p_lo)
+    z = np.zeros_like(dn)
+    _set_hydro(Q, dn, z, z, z, pr, cfg.aindex)
+    return Q
+
+
+def isentropic_vortex(cfg: Config, ver: int = 1, beta: float = 5.0) -> np.ndarray:
+    """initialcon.f90:128-183 isentropic_vortex."""
+    Q = _background(cfg)
+    g = cfg.aindex
+    aindm1 = g - 1.0
+    vx_amb, vy_amb, Rgsqi = (1.0, 0.0, 1.0) if ver == 0 else (1.0, 1.0, 0.5)
+    xc, yc, zc = cell_centres(cfg)
+    X, Y = np.meshgrid(xc, yc, indexing="ij")
+    X = np.broadcast_to(X[:, :, None], (cfg.nx, cfg.ny, cfg.nz))
+    Y = np.broadcast_to(Y[:, :, None], (cfg.nx, cfg.ny, cfg.nz))
+    r2 = X ** 2 + Y ** 2
+    pi = math.pi
+    dvx = -Y * beta / (2 * pi) * np.exp(Rgsqi * (1 - r2))
+    dvy = X * beta / (2 * pi) * np.exp(Rgsqi * (1 - r2))
+    dT = -(aindm1 * beta ** 2) / (16 * Rgsqi * g * pi ** 2) * np.exp(2 * Rgsqi * (1 - r2))
+    vx, vy = vx_amb + dvx, vy_amb + dvy
+    te = 1.0 + dT
+    dn = te ** (1.0 / aindm1)
+    pr = dn ** g
+    _set_hydro(Q, dn, vx, vy, np.zeros_like(vx), pr, g)
+    return Q
+
+
+def isentropic_vortex_exact(cfg: Config, t: float, ver: int = 1, beta: float = 5.0) -> np.ndarray:
+    """Cell-average density of the exactly advected vortex at time t (the IC
+    shifted by the mean flow, periodically wrapped), sampled at cell centres."""
+    vx_amb, vy_amb, Rgsqi = (1.0, 0.0, 1.0) if ver == 0 else (1.0, 1.0, 0.5)
+    g = cfg.aindex
+    xc, yc, zc = cell_centres(cfg)
+    X, Y = np.meshgrid(xc, yc, indexing="ij")
+    Xs = (X - vx_amb * t + cfg.lx / 2) % cfg.lx - cfg.lx / 2
+    Ys = (Y - vy_amb * t + cfg.ly / 2) % cfg.ly - cfg.ly / 2
+    r2 = Xs ** 2 + Ys ** 2
+    dT = -((g - 1) * beta ** 2) / (16 * Rgsqi * g * math.pi ** 2) * np.exp(2 * Rgsqi * (1 - r2))
+    return (1.0 + dT) ** (1.0 / (g - 1))
+
+
+def taylor_green(cfg: Config, rho: float = 1.0, V0: float = 1.0) -> np.ndarray:
+    """Taylor-Green vortex on [0, 2 pi]^3 (no reference IC): vx = V0 sin x cos y
+    cos z, vy = -V0 cos x sin y cos z, vz = 0, rho = 1, p = colvis (= rho
+    c^2/gamma), evaluated at cell centres shifted to [0, L)."""
+    Q = _background(cfg)
+    xc, yc, zc = cell_centres(cfg)
+    x, y, z = xc + cfg.lx / 2, yc + cfg.ly / 2, zc + cfg.lz / 2
+    X, Y, Z = np.meshgrid(x, y, z, indexing="ij")
+    vx = V0 * np.sin(X) * np.cos(Y) * np.cos(Z)
+    vy = -V0 * np.cos(X) * np.sin(Y) * np.cos(Z)
+    vz = np.zeros_like(vx)
+    p = cfg.colvis if cfg.colvis > 0 else 1.0
+    _set_hydro(Q, np.full_like(vx, rho), vx, vy, vz, np.full_like(vx, p), cfg.aindex)
+    return Q
+
+
+def equilibrium(cfg: Config, rho: float = 1.0, T: float = 1.0) -> np.ndarray:
+    """Uniform fluid at rest, p = rho T (fluctuating-hydro equilibrium)."""
+    Q = _background(cfg)
+    sh = (cfg.nx, cfg.ny, cfg.nz)
+    z = np.zeros(sh)
+    _set_hydro(Q, np.full(sh, rho), z, z, z, np.full(sh, rho * T), cfg.aindex)
+    return Q
+
+
+def channel(cfg: Config, amplitude: float = 1.0e-3, seed: int = 0, rho: float = 1.0, p: float = 1.0) -> np.ndarray:
+    """Channel at rest plus a seeded Gaussian velocity perturbation of the
+    given amplitude (cell averages of vx, vy).  No reference IC: the
+    reference's poiseuille_flow (initialcon.f90:244-284) starts at rest and is
+    driven by inflow."""
+    Q = _background(cfg)
+    rng = np.random.default_rng(seed)
+    sh = (cfg.nx, cfg.ny, cfg.nz)
+    vx = amplitude * rng.standard_normal(sh)
+    vy = amplitude * rng.standard_normal(sh)
+    _set_hydro(Q, np.full(sh, rho), vx, vy, np.zeros(sh), np.full(sh, p), cfg.aindex)
+    return Q
+
+
+def random_smooth(cfg: Config, seed: int = 0, amp: float = 0.05, stress_amp: float = 0.0) -> np.ndarray:
+    """A positive, smooth-ish random state with all basis modes populated;
+    used by parity tests to exercise every term of the operator."""
+    rng = np.random.default_rng(seed)
+    Q = equilibrium(cfg)
+    nb = cfg.nbasis
+    sh = (cfg.nx, cfg.ny, cfg.nz)
+    Q[:, :, :, RH, 0] = 1.0 + amp * rng.standard_normal(sh)
+    v = amp * rng.standard_normal((3,) + sh)
+    Q[:, :, :, MX:MZ + 1, 0] = np.moveaxis(v * Q[:, :, :, RH, 0], 0, -1)
+    Q[:, :, :, EN, 0] = (1.0 + amp * rng.standard_normal(sh)) / (cfg.aindex - 1) + \
+        0.5 * (Q[:, :, :, MX, 0] ** 2 + Q[:, :, :, MY, 0] ** 2 + Q[:, :, :, MZ, 0] ** 2) / Q[:, :, :, RH, 0]
+    if stress_amp > 0:
+        Q[:, :, :, PXX:PYZ + 1, 0] = stress_amp * rng.standard_normal(sh + (6,))
+    for b in range(1, nb):
+        Q[:, :, :, :, b] = 0.1 * amp * rng.standard_normal(sh + (NQ,)) * np.abs(Q[:, :, :, :, 0]).mean(axis=(0, 1, 2))
+    return Q

@@ -1,0 +1,162 @@
+/*
+ * hermes_gb300.h -- C ABI of the GB300 DG right-hand side and SSP-RK time
+ * step of HERMESHD (5- and 10-moment systems).
+ *
+ * This is the drop-in boundary for the reference's step path.  The
+ * reference exposes that path to Python through an f2py/f90wrap extension
+ * (src/hermeshd.py:5-120, wrapping src/hermeshd.f90:26-199); the Python
+ * package hermeshd_gb300 binds the functions below with ctypes and keeps the
+ * reference's call surface on top of them.
+ *
+ * Conventions
+ *  - Field arrays use the reference layout Q(nx,ny,nz,nQ,nbasis) in Fortran
+ *    order (x fastest, basis slowest), nQ = 11 variables rh, mx, my, mz, en,
+ *    pxx, pyy, pzz, pxy, pxz, pyz (params.f90:42-47).  Element type is double
+ *    when cfg->precision == 64 and float when it is 32.
+ *  - Pointers named q* are device pointers unless the function name ends in
+ *    _host.  Device work is ordered after, and before, the caller's stream.
+ *  - Every function returns a hermes_status code; the reference returns none
+ *    and calls exit(-1) on a NaN (integrator.f90:234-250).  The message of
+ *    the last failure is hermes_last_error(ctx).
+ *  - No entry point exits, traps or aborts the process.
+ */
+#ifndef HERMES_GB300_H
+#define HERMES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HERMES_ABI_VERSION 1
+
+typedef enum hermes_status {
+    HERMES_OK = 0,
+    HERMES_ERR_CONFIG = 1,     /* unsupported or inconsistent configuration */
+    HERMES_ERR_SHAPE = 2,      /* array size does not match the configuration */
+    HERMES_ERR_DTYPE = 3,      /* element type does not match cfg->precision */
+    HERMES_ERR_NONFINITE = 4,  /* a NaN cell average appeared (integrator.f90:234-250) */
+    HERMES_ERR_TIMEOUT = 5,    /* a bounded device wait ran out */
+    HERMES_ERR_CUDA = 6,       /* a CUDA runtime call failed */
+    HERMES_ERR_ALLOC = 7,      /* device or host allocation failed */
+    HERMES_ERR_ARG = 8         /* null pointer or invalid argument */
+} hermes_status;
+
+/* boundary condition codes: boundary.f90:789-880 ('periodic', 'outflow',
+ * 'wall', 'noslip'; any other name selects periodic there, and here) */
+enum { HERMES_BC_PERIODIC = 0, HERMES_BC_OUTFLOW = 1, HERMES_BC_WALL = 2, HERMES_BC_NOSLIP = 3 };
+
+/* The run-time form of the reference's compile-time configuration
+ * (src/input.f90, src/params.f90, tests/<problem>/input_*.f90). */
+typedef struct hermes_config {
+    int32_t nx, ny, nz;        /* cells; input.f90 nx, ny, nz with one MPI domain */
+    int32_t nbasis, iquad;     /* (4,2), (8,2) or (10,3): input.f90 nbasis, iquad */
+    int32_t iorder;            /* 2 'heun' or 3 'shu-osher': integrator.f90:39-55 */
+    int32_t ivis;              /* 0, 1, 2: input.f90 ivis */
+    int32_t ieos;              /* 1 ideal gas, 2 Murnaghan-Tait */
+    int32_t ihllc;             /* nonzero: HLLC for rh..en (flux.f90:264-271) */
+    int32_t bc[6];             /* xlo, xhi, ylo, yhi, zlo, zhi: HERMES_BC_* */
+    int32_t precision;         /* 64 (FP64) or 32 (FP32 bulk, FP64 CFL and limiter fixes) */
+    int32_t llns;              /* nonzero: stochastic stress (random.f90:106-145) */
+    double lx, ly, lz;         /* domain lengths; the domain is centred at 0 */
+    double aindex;             /* gamma */
+    double rh_floor, T_floor;  /* params.f90:93-95 */
+    double rh_mult;            /* params.f90:105 */
+    double coll, colvis;       /* relaxation rate, coll*viscosity (params.f90:115) */
+    double cflm;               /* <= 0: initialize.f90:104-122 default for iquad */
+    double P_1, P_base;        /* Tait EOS constants (params.f90:104) */
+    double eta_sd, zeta_sd;    /* stochastic stress amplitudes per unit normal */
+    uint64_t seed;             /* Philox key of the stochastic stress */
+    double body_force;         /* uniform x body force (no reference counterpart) */
+} hermes_config;
+
+typedef struct hermes_ctx hermes_ctx;
+
+/* ABI version of the loaded library (HERMES_ABI_VERSION). */
+int hermes_abi_version(void);
+
+/* sizeof(hermes_config) as compiled into the library (binding check). */
+int hermes_config_size(void);
+
+/* Number of elements of one field array for cfg, and the device scratch the
+ * context allocates (face-flux buffers).  No device work. */
+int hermes_sizes(const hermes_config *cfg, size_t *q_elems, size_t *scratch_bytes);
+
+/* Create a context: the GB300 replacement of setup()'s discretisation part
+ * (hermeshd.f90:67-114 -> initialize.f90:24-61 initializer: basis tables,
+ * cbasis, cflm, grid spacing).  Initial conditions stay with the caller, as
+ * in the f90wrap interface where Q_io is caller-owned.  stream: the
+ * caller's cudaStream_t (NULL = the legacy default stream).  The context
+ * runs its kernels on a private stream that waits for the caller's stream at
+ * the start of every call and that the caller's stream waits for at the end,
+ * so calls are stream-ordered with the caller's own work. */
+int hermes_create(const hermes_config *cfg, void *stream, hermes_ctx **out);
+
+/* An ensemble of nbox independent grids sharing cfg's physics, advanced
+ * together: dims[3*i..3*i+2] = (nx, ny, nz) of box i, seeds[i] its Philox
+ * key (NULL: cfg->seed + i), lengths[3*i..] its domain lengths (NULL: cfg's).
+ * Field arrays hold the boxes back to back, box i starting at element
+ * offsets[i] (hermes_box_offsets).  No reference counterpart (batching). */
+int hermes_ensemble_create(const hermes_config *cfg, int nbox, const int32_t *dims, const double *lengths,
+                           const uint64_t *seeds, void *stream, hermes_ctx **out);
+int hermes_box_offsets(hermes_ctx *ctx, int64_t *offsets /* nbox+1 */);
+
+int hermes_destroy(hermes_ctx *ctx);
+
+/* Message of the last failure on this context (static storage of the ctx). */
+const char *hermes_last_error(hermes_ctx *ctx);
+
+/* The context's private CUDA stream (cudaStream_t) its kernels run on. */
+void *hermes_stream(hermes_ctx *ctx);
+
+/* get_min_dt (hermeshd.f90:145-199): CFL time step from the cell averages
+ * of q, in FP64, including the reference's use of the last cell's sound
+ * speed and of dxi only.  Synchronises; dt_out is a host pointer. */
+int hermes_get_min_dt(hermes_ctx *ctx, const void *q, double *dt_out);
+
+/* limiter (flux.f90:1077-1164), in place on q. */
+int hermes_limiter(hermes_ctx *ctx, void *q);
+
+/* calc_rhs (integrator.f90:116-122 -> glflux flux.f90:932-1022 and
+ * source_calc sources.f90:12-84) after prep_advance's limiter when
+ * apply_limiter is nonzero (integrator.f90:106-113): rhs = glflux_r -
+ * source_r, in the layout of q.  q is limited in place, as in the reference. */
+int hermes_rhs(hermes_ctx *ctx, void *q, void *rhs, int apply_limiter);
+
+/* euler_step (integrator.f90:93-102): q_out = advance_time_level(lim(q_in)). */
+int hermes_euler_stage(hermes_ctx *ctx, void *q_in, void *q_out, double dt);
+
+/* step (hermeshd.f90:53-62, f90wrap_step in hermeshd.py:31-47): dt =
+ * get_min_dt(q); update(q, q1, q2, dt) with RK2 or RK3 (integrator.f90:62-86);
+ * t += dt.  t and dt are host scalars, read and written as in the reference.
+ * q1 and q2 are caller-provided scratch, as there; q2 is left unwritten.
+ * Synchronises (to return dt and t). */
+int hermes_step(hermes_ctx *ctx, void *q, void *q1, void *q2, double *t, double *dt);
+
+/* nsteps of step() from one CUDA graph, one synchronisation at the end
+ * (the loop of hermeshd.f90:38-41 without output). */
+int hermes_advance(hermes_ctx *ctx, void *q, void *q1, void *q2, int nsteps, double *t, double *dt);
+
+/* The same with host buffers: q_host (nsteps of step() on a device copy,
+ * then copied back).  The reference's interface takes host arrays. */
+int hermes_advance_host(hermes_ctx *ctx, void *q_host, int nsteps, double *t, double *dt);
+
+/* Per-box time and last time step of an ensemble (nbox entries each). */
+int hermes_box_times(hermes_ctx *ctx, double *t, double *dt);
+/* Set the time of every box (device) */
+int hermes_set_time(hermes_ctx *ctx, double t);
+
+/* Step counter of the stochastic-stress Philox stream (the number of
+ * completed steps; stages are counted within a step). */
+int hermes_set_noise_step(hermes_ctx *ctx, uint64_t step);
+
+/* Device error flags raised since the last call (HERMES_ERR_NONFINITE if a
+ * NaN cell average was produced), cleared on read.  Synchronises. */
+int hermes_check(hermes_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

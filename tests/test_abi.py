@@ -1,0 +1,51 @@
+"""The C-ABI library loads and exports exactly what include/hermes_gb300.h
+declares; host-only entry points answer without a GPU."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from hermeshd_gb300 import _lib, config
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "hermes_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return set(re.findall(r"^\s*(?:const\s+)?[\w\s\*]*?\b(hermes_\w+)\s*\(", src, flags=re.M))
+
+
+def test_header_and_binding_agree():
+    assert header_functions() == set(_lib.EXPORTS)
+
+
+def test_library_exports_every_symbol(hermes_lib):
+    for name in _lib.EXPORTS:
+        assert hasattr(hermes_lib, name), name
+
+
+def test_abi_version_and_config_layout(hermes_lib):
+    assert hermes_lib.hermes_abi_version() == 1
+    assert hermes_lib.hermes_config_size() == C.sizeof(_lib.HermesConfig)
+
+
+@pytest.mark.parametrize("nb,nq", [(4, 2), (8, 2), (10, 3)])
+def test_sizes(hermes_lib, nb, nq):
+    cfg = config.Config(nx=7, ny=5, nz=3, nbasis=nb, iquad=nq, xlobc="wall", xhibc="wall")
+    qe, sb = C.c_size_t(), C.c_size_t()
+    assert hermes_lib.hermes_sizes(C.byref(_lib.to_c(cfg)), C.byref(qe), C.byref(sb)) == 0
+    assert qe.value == 7 * 5 * 3 * 11 * nb
+    nf = nq * nq
+    faces = (8 * 5 * 3) + (7 * 5 * 3) + (7 * 5 * 3)      # x has nx+1 planes (walls); y, z periodic
+    assert sb.value == faces * 11 * nf * 8
+
+
+def test_bad_config_rejected_without_gpu(hermes_lib):
+    cfg = _lib.to_c(config.Config(nbasis=27, iquad=3))
+    ctx = C.c_void_p()
+    assert hermes_lib.hermes_create(C.byref(cfg), None, C.byref(ctx)) == 1   # HERMES_ERR_CONFIG
+    cfg = _lib.to_c(config.Config(nx=0))
+    assert hermes_lib.hermes_create(C.byref(cfg), None, C.byref(ctx)) == 1
+    assert not ctx.value

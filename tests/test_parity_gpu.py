@@ -1,0 +1,224 @@
+"""GPU parity: the CUDA path (through the C ABI) against the FP64 oracle.
+
+Tolerances (relative L2 over the whole field array):
+  one right-hand side / one limiter pass     1e-12
+  100 steps of the FP64 step                 1e-11   (the stated FP64 bar)
+  FP32 path vs the FP64 oracle               1e-5
+"""
+import numpy as np
+import pytest
+
+from hermeshd_gb300 import config, ic
+from helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 1e-12
+STEP_TOL = 1e-11
+FP32_TOL = 1e-5
+
+
+def _solver(cfg):
+    from hermeshd_gb300.solver import Solver
+    return Solver(cfg)
+
+
+def _oracle(cfg):
+    import oracle as O
+    return O.Oracle(cfg)
+
+
+RHS_CASES = {
+    "nb4_3d_periodic_ivis0": (config.Config(nx=6, ny=5, nz=4, nbasis=4, iquad=2, ivis=0, coll=0.7, lx=1.3, ly=0.9, lz=1.1), 2.0),
+    "nb8_2d_wall_ivis1": (config.Config(nx=8, ny=7, nz=1, nbasis=8, iquad=2, ivis=1, coll=3.0, colvis=1.5,
+                                        xlobc="wall", xhibc="wall", ly=0.8), 1.0),
+    "nb10_2d_periodic": (config.Config(nx=6, ny=6, nz=1, nbasis=10, iquad=3, ivis=0, aindex=1.4), 0.0),
+    "nb10_3d_mixed_bc": (config.Config(nx=5, ny=4, nz=3, nbasis=10, iquad=3, ivis=1, coll=2.0, colvis=1.0,
+                                       xlobc="outflow", xhibc="wall", ylobc="noslip", yhibc="outflow",
+                                       zlobc="wall", zhibc="noslip"), 0.5),
+    "nb4_3d_ivis2": (config.Config(nx=5, ny=4, nz=3, nbasis=4, iquad=2, ivis=2, coll=1.5, colvis=1.0), 1.0),
+    "nb8_3d_noise": (config.Config(nx=4, ny=4, nz=4, nbasis=8, iquad=2, ivis=1, coll=1.0, colvis=1.0, llns=True,
+                                   eta_sd=0.05, zeta_sd=0.01, seed=1234), 0.5),
+    "nb4_2d_bodyforce_noslip": (config.Config(nx=6, ny=8, nz=1, nbasis=4, iquad=2, ivis=1, coll=5.0, colvis=1.0,
+                                              ylobc="noslip", yhibc="noslip", body_force=0.1), 0.0),
+    "nb4_x_periodic_hi_only": (config.Config(nx=6, ny=3, nz=2, nbasis=4, iquad=2, xlobc="wall", xhibc="periodic"), 0.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(RHS_CASES))
+def test_rhs_parity(name):
+    cfg, stress = RHS_CASES[name]
+    Q = ic.random_smooth(cfg, seed=7, amp=0.1, stress_amp=0.05 * stress)
+    o = _oracle(cfg)
+    Qo = Q.copy(order="F")
+    r_o = o.rhs(Qo, limit=True)
+    s = _solver(cfg)
+    q = s.from_numpy(Q)
+    r_g = s.to_numpy(s.rhs(q, limit=True))
+    # the limiter writes q in place on both sides
+    assert rel_l2(s.to_numpy(q), Qo) < RHS_TOL
+    err = rel_l2(r_g, r_o)
+    assert err < RHS_TOL, f"{name}: rel L2 {err:.3e}"
+
+
+def test_limiter_active_parity():
+    """A state whose face densities and pressures dip below the floors, so
+    every limiter branch runs (flux.f90:1077-1164)."""
+    cfg = config.Config(nx=16, ny=8, nz=2, nbasis=8, iquad=2, T_floor=2.0)
+    rng = np.random.default_rng(3)
+    Q = ic.random_smooth(cfg, seed=11, amp=0.2)
+    sh = (cfg.nx, cfg.ny, cfg.nz)
+    Q[:, :, :, 0, 1:] = 0.6 * rng.standard_normal(sh + (cfg.nbasis - 1,))   # big density slopes
+    Q[:, :, :, 4, 1:] = 1.5 * rng.standard_normal(sh + (cfg.nbasis - 1,))
+    Q[::5, :, :, 0, 0] = 1e-7                                                # below rh_floor
+    o = _oracle(cfg)
+    Qo = Q.copy(order="F")
+    o.limiter(Qo)
+    s = _solver(cfg)
+    q = s.from_numpy(Q)
+    s.limiter(q)
+    g = s.to_numpy(q)
+    assert not np.array_equal(Qo, Q)   # the limiter did something
+    assert rel_l2(g, Qo) < RHS_TOL
+
+
+def test_min_dt_parity():
+    cfg = config.isentropic_vortex_2d(n=16)
+    Q = ic.isentropic_vortex(cfg)
+    o = _oracle(cfg)
+    s = _solver(cfg)
+    dt_o = o.get_min_dt(Q.copy(order="F"))
+    dt_g = s.get_min_dt(s.from_numpy(Q))
+    assert abs(dt_g - dt_o) <= 1e-14 * dt_o
+
+
+STEP_CASES = {
+    "sod_256_rk2_nb4": (lambda: config.sod_1d(nx=256), lambda c: ic.sod(c)),
+    "vortex_16_rk3_nb10": (lambda: config.isentropic_vortex_2d(n=16), lambda c: ic.isentropic_vortex(c)),
+    "tgv_8_rk3_nb4_ivis1": (lambda: config.taylor_green_3d(n=8, precision="fp64"), lambda c: ic.taylor_green(c)),
+    "random_nb8_walls_rk2": (lambda: config.Config(nx=10, ny=6, nz=3, nbasis=8, iquad=2, ivis=1, coll=2.0, colvis=0.5,
+                                                   xlobc="wall", xhibc="noslip", zlobc="outflow", zhibc="wall"),
+                             lambda c: ic.random_smooth(c, seed=5, amp=0.05, stress_amp=0.01)),
+    "fh_noise_8_rk2_nb4": (lambda: config.fh_box(8, precision="fp64", seed=42), lambda c: ic.equilibrium(c)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(STEP_CASES))
+def test_100_steps_parity(name):
+    mk, icf = STEP_CASES[name]
+    cfg = mk()
+    Q = icf(cfg)
+    o = _oracle(cfg)
+    Qo = Q.copy(order="F")
+    t_o, dt_o = o.advance(Qo, 100)
+    s = _solver(cfg)
+    q, q1 = s.from_numpy(Q), s.new_state()
+    t_g, dt_g = s.advance(q, q1, 100, t=0.0)
+    err = rel_l2(s.to_numpy(q), Qo)
+    assert abs(t_g - t_o) <= 1e-11 * t_o
+    assert err < STEP_TOL, f"{name}: rel L2 after 100 steps {err:.3e}"
+
+
+def test_step_equals_graph_advance():
+    cfg = config.isentropic_vortex_2d(n=12)
+    Q = ic.isentropic_vortex(cfg)
+    s = _solver(cfg)
+    qa, qa1 = s.from_numpy(Q), s.new_state()
+    t = 0.0
+    for _ in range(7):
+        t, dt = s.step(qa, qa1, None, t)
+    qb, qb1 = s.from_numpy(Q), s.new_state()
+    tb, dtb = s.advance(qb, qb1, 7, t=0.0)
+    assert t == tb and dt == dtb
+    assert np.array_equal(s.to_numpy(qa), s.to_numpy(qb))
+
+
+def test_host_buffers_equal_device():
+    cfg = config.sod_1d(nx=64)
+    Q = ic.sod(cfg)
+    s = _solver(cfg)
+    q, q1 = s.from_numpy(Q), s.new_state()
+    t_d, _ = s.advance(q, q1, 12)
+    qh = np.ascontiguousarray(Q.T)          # (nb, nQ, nz, ny, nx) C order = the Fortran memory
+    t_h, _ = s.advance_host(qh, 12)
+    assert t_h == t_d
+    assert np.array_equal(qh, s.to_numpy(q).T)
+
+
+def test_fp32_path_against_fp64_oracle():
+    cfg = config.isentropic_vortex_2d(n=16, precision="fp32")
+    Q = ic.isentropic_vortex(cfg)
+    o = _oracle(cfg.replace(precision="fp64"))
+    Qo = Q.copy(order="F")
+    o.advance(Qo, 20)
+    s = _solver(cfg)
+    q, q1 = s.from_numpy(Q), s.new_state()
+    s.advance(q, q1, 20)
+    err = rel_l2(s.to_numpy(q), Qo)
+    assert err < FP32_TOL, err
+
+
+def test_nonfinite_is_reported_and_context_survives():
+    from hermeshd_gb300._lib import NonFiniteError
+    cfg = config.sod_1d(nx=32)
+    Q = ic.sod(cfg)
+    Qbad = Q.copy(order="F")
+    Qbad[5, 0, 0, 4, 0] = np.nan
+    s = _solver(cfg)
+    q, q1 = s.from_numpy(Qbad), s.new_state()
+    with pytest.raises(NonFiniteError):
+        s.step(q, q1, None, 0.0)
+    # the context and the GPU stay usable
+    q, q1 = s.from_numpy(Q), s.new_state()
+    t, dt = s.step(q, q1, None, 0.0)
+    assert np.isfinite(s.to_numpy(q)).all() and dt > 0
+
+
+def test_ensemble_equals_single_boxes():
+    import torch
+    from hermeshd_gb300.solver import Ensemble
+    base = config.fh_box(8, precision="fp64", seed=0)
+    dims = [(8, 8, 8), (6, 6, 6), (4, 5, 3)]
+    L = 10.0
+    lengths = [(d[0] * L, d[1] * L, d[2] * L) for d in dims]
+    seeds = [11, 22, 33]
+    ens = Ensemble(base, dims, lengths, seeds)
+    q, q1 = ens.new_state(), ens.new_state()
+    inits = []
+    for i, d in enumerate(dims):
+        c = base.replace(nx=d[0], ny=d[1], nz=d[2], lx=lengths[i][0], ly=lengths[i][1], lz=lengths[i][2], seed=seeds[i])
+        Qi = ic.random_smooth(c, seed=i, amp=0.02)
+        inits.append((c, Qi))
+        ens.box_view(q, i).copy_(torch.from_numpy(np.ascontiguousarray(Qi.T)).to(q.device))
+    ens.advance(q, q1, 5)
+    t_e, dt_e = ens.box_times()
+    for i, (c, Qi) in enumerate(inits):
+        s = _solver(c)
+        qs, qs1 = s.from_numpy(Qi), s.new_state()
+        t_s, dt_s = s.advance(qs, qs1, 5)
+        assert t_s == t_e[i]
+        assert np.array_equal(s.to_numpy(qs), s.to_numpy(ens.box_view(q, i)))
+
+
+def test_reference_front_end_step():
+    """hermeshd.hermeshd.setup/step with numpy Fortran arrays, as in
+    src/test_hermeshd.py:44-78."""
+    from hermeshd_gb300 import hermeshd as H
+    cfg = config.sod_1d(nx=50)
+    mod = H.Hermeshd()
+    mod.configure(cfg, icid=3)
+    Qio = np.empty(cfg.shape_f, order="F", dtype=np.float64)
+    Q1, Q2 = np.empty_like(Qio), np.empty_like(Qio)
+    t, dt, t1, t_start, dtout, nout = (np.array(0.0), np.array(0.0), np.array(0.0), np.array(0.0),
+                                        np.array(0.0), np.array(0))
+    mod.setup(Qio, t, dt, t1, t_start, dtout, nout, 0)
+    o = _oracle(cfg)
+    Qo = ic.sod(cfg)
+    to = 0.0
+    for _ in range(5):
+        mod.step(Qio, Q1, Q2, t, dt)
+        mod.generate_output(Qio, t, dt, t1, dtout, nout)
+        to, dto = o.step(Qo, o.new(), o.new(), to, 0.0)
+    assert abs(float(t) - to) <= 1e-14 * to
+    assert rel_l2(Qio, Qo) < STEP_TOL
+    mod.cleanup(t_start)
