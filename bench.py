@@ -1,0 +1,411 @@
+#!/usr/bin/env python
+"""Throughput of the HERMESHD DG step on GB300: DOF-updates/s per RK stage.
+
+Headline workload (one GPU): the 2-D isentropic vortex, 128x128x1 cells,
+5-moment Euler, quadratic Legendre basis (nbasis 10, iquad 3), HLLC, SSP-RK3,
+FP64 (the "plain" path).  A step is one SSP-RK3 time step (CFL reduction +
+three stages) of the whole grid; DOF = nx*ny*nz*nQ*nbasis with nQ = 11.
+Variants on the same JSON line: the same workload in FP32, and the FP32
+batched fluctuating-hydro ensemble (256 periodic boxes of sizes drawn from
+{16,24,32,48}^3, 10-moment + stochastic stress, nb 4) against the plain FP64
+path on one such box.  Inputs are synthetic (seeded initial conditions);
+between timed steps a 256 MiB buffer is written to flush L2 (129 MB).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU implementation (the
+FP64 C restatement in oracle/, all host threads) on the same workload.
+N > 1 (torchrun): replicas, one independent copy of the workload per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-updates/s per RK stage, FP64 plain vs FP32 batched at stated L2 error"
+UNIT = "DOF-updates/s"
+WORKLOAD = ("2D isentropic vortex 128x128x1 periodic, 5-moment Euler, quadratic Legendre basis "
+            "(nbasis 10, iquad 3), HLLC, SSP-RK3, FP64")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--n", type=int, default=128, help="vortex grid size (default 128)")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_init():
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait(timeout=10)
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        try:
+            os.unlink(self.f.name)
+        except OSError:
+            pass
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = {"hbm_gbs": FALLBACK_HBM_GBS, "source": "fallback"}
+    f = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(f):
+        d = json.load(open(f))
+        if d.get("hbm_gbs"):
+            p = {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return p
+
+
+def alu_peaks():
+    """FP64 and FP32 (non-tensor) GEMM throughput measured here with torch
+    (cuBLAS); MEASURED_PEAKS.json carries only HBM and bf16."""
+    import torch
+    out = {}
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, dt, n, reps in (("fp64_tflops", torch.float64, 4096, 3), ("fp32_tflops", torch.float32, 8192, 5)):
+        a = torch.randn(n, n, device="cuda", dtype=dt)
+        b = torch.randn(n, n, device="cuda", dtype=dt)
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) * 1e-3)
+        out[name] = 2 * n ** 3 / best / 1e12
+        del a, b
+    torch.cuda.empty_cache()
+    return out
+
+
+# ---------------------------------------------------------------------------
+def time_steps(solver, q, q1, steps, flush):
+    """Per-step device time (s) with CUDA events on the kernels' own stream,
+    an L2 flush on that stream before every step."""
+    import torch
+    st = torch.cuda.ExternalStream(solver.cuda_stream)
+    evs = []
+    with torch.cuda.stream(st):
+        for _ in range(steps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            solver.enqueue_steps(q, q1, 1)
+            e1.record(st)
+            evs.append((e0, e1))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) * 1e-3 for a, b in evs]
+
+
+def run_ours(args, rank, ws):
+    import numpy as np
+    import torch
+
+    from hermeshd_gb300 import config, ic, perfmodel
+    from hermeshd_gb300.solver import Ensemble, Solver
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    K, W = args.steps, args.warmup
+    cfg = config.isentropic_vortex_2d(n=args.n)
+    Q0 = ic.isentropic_vortex(cfg)
+    s = Solver(cfg)
+    q, q1 = s.from_numpy(Q0), s.new_state()
+    s.advance(q, q1, W)
+    barrier(ws)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        times = time_steps(s, q, q1, K, flush)
+    elapsed = max_over_ranks(sum(times), ws)
+    clocks = clk.summary()
+    dof_stage = cfg.dof * cfg.stages
+    value = ws * dof_stage * K / elapsed
+    ms_per_step = 1e3 * elapsed / K
+    launches_per_step = 2 + 5 * cfg.stages
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+           "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "nQ": 11, "nbasis": 10,
+                      "dof": cfg.dof, "rk_stages": cfg.stages, "l2": "flushed: 256 MiB write before every timed step",
+                      "parallelism": "replicas" if ws > 1 else "single GPU", "timing": "CUDA events per step on the kernels' stream"},
+           "clocks": clocks, "gpu_launches": launches_per_step * K}
+
+    # ---- end to end through the C ABI with host buffers -----------------
+    qh = torch.empty(cfg.shape_c, dtype=torch.float64, pin_memory=True)
+    qh.copy_(torch.from_numpy(np.ascontiguousarray(Q0.T)))
+    qhn = qh.numpy()
+    s.advance_host(qhn, 1)
+    Ke = max(3, K // 2)
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        s.advance_host(qhn, 1)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
+    qbytes = int(np.prod(cfg.shape_c)) * 8
+    out["e2e"] = {"value": ws * dof_stage * Ke / e2e_s, "unit": UNIT, "h2d_bytes_per_step": qbytes,
+                  "d2h_bytes_per_step": qbytes, "steps": Ke,
+                  "path": "hermes_advance_host (pinned host array -> H2D, one step, D2H, synchronise)"}
+
+    # ---- per-kernel device times (event pairs around every launch) ------
+    s.profile(True)
+    torch.cuda.synchronize()
+    st = torch.cuda.ExternalStream(s.cuda_stream)
+    with torch.cuda.stream(st):
+        for _ in range(K):
+            flush.fill_(1)
+            s.enqueue_steps(q, q1, 1)
+    prof = s.profile_read()
+    s.profile(False)
+    total = sum(v[0] for v in prof.values())
+    kern = {k: {"launches": n, "ms_total": ms, "ms_avg": ms / max(n, 1), "share": ms / total}
+            for k, (ms, n) in prof.items()}
+    top = max(kern, key=lambda k: kern[k]["ms_total"])
+    pk = peaks()
+    sbytes = perfmodel.bytes_per_dof_stage(cfg.precision, cfg.iorder)
+    # algorithmic bytes per launch: the cell kernel is the stage (reads the
+    # stage input and Q^n, writes the output); a face kernel reads the state
+    per_launch = {"cell": cfg.dof * sbytes, "face_x": cfg.dof * 8.0, "face_y": cfg.dof * 8.0,
+                  "face_z": cfg.dof * 8.0, "limiter": cfg.dof * 8.0 * 5 / 11, "cfl_dt": cfg.ncells * 5 * 8.0}
+    ach = per_launch[top] / (kern[top]["ms_avg"] * 1e-3) / 1e9
+    out["roofline"] = {"bound": "hbm", "kernel": top, "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                       "frac": ach / pk["hbm_gbs"], "peak_source": pk["source"], "traffic": None,
+                       "algorithmic_bytes_per_launch": per_launch[top], "kernels": kern}
+    fl = perfmodel.flops_per_cell_stage(cfg)
+    try:
+        ap = alu_peaks()
+    except Exception as e:  # pragma: no cover
+        ap = {"error": str(e)}
+    step_flops = fl["total"] * cfg.ncells * cfg.stages
+    out["alu"] = {"bound_by": "fp64 pipe", "flops_per_cell_stage": fl, "achieved_tflops": step_flops / (ms_per_step * 1e-3) / 1e12,
+                  "peak": ap, "frac_fp64": (step_flops / (ms_per_step * 1e-3) / 1e12) / ap["fp64_tflops"] if "fp64_tflops" in ap else None,
+                  "flop_model": "algorithmic: nonzero table products (FMA = 2), division/sqrt = 1"}
+    qg64 = q.clone()
+    s.close()
+
+    # ---- variants -------------------------------------------------------
+    if not args.no_variants:
+        out["variants"] = variants(args, cfg, Q0, qg64, flush, dev, ws, value)
+
+    # ---- CPU baseline: the oracle on this host's cores ------------------
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(cfg, Q0, steps=6)
+    return out
+
+
+def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
+    import numpy as np
+    import torch
+
+    from hermeshd_gb300 import config, ic
+    from hermeshd_gb300.solver import Ensemble, Solver
+
+    K, W = args.steps, args.warmup
+    res = {}
+    # FP32 vortex, error vs the FP64 GPU state after the same number of steps
+    c32 = cfg64.replace(precision="fp32")
+    s = Solver(c32)
+    q, q1 = s.from_numpy(Q0), s.new_state()
+    s.advance(q, q1, W)
+    times = time_steps(s, q, q1, K, flush)
+    el = max_over_ranks(sum(times), ws)
+    v32 = ws * c32.dof * c32.stages * K / el
+    e = (q.double() - qg64).norm() / qg64.norm()
+    res["fp32"] = {"value": v32, "unit": UNIT, "ms_per_step": 1e3 * el / K, "dtype": "f32",
+                   "rel_l2_vs_fp64": float(e), "speedup_vs_fp64": v32 / value64}
+    s.close()
+
+    # FP32 batched ensemble vs the plain FP64 path on one box of the same physics
+    rng = np.random.default_rng(0)
+    sizes = rng.choice([16, 24, 32, 48], size=256)
+    dims = [(int(n), int(n), int(n)) for n in sizes]
+    base = config.fh_box(48, precision="fp32", seed=0)
+    dx = base.lx / 48
+    lengths = [(n * dx, n * dx, n * dx) for (n, _, _) in dims]
+    ens = Ensemble(base, dims, lengths, seeds=list(range(256)))
+    qe, qe1 = ens.new_state(), ens.new_state()
+    # equilibrium rho = 1, T = 1, v = 0 in every box, set on the device
+    for i in range(ens.nbox):
+        v = ens.box_view(qe, i)
+        v.zero_()
+        v[0, 0].fill_(1.0)
+        v[0, 4].fill_(1.0 / (base.aindex - 1.0))
+    ens.advance(qe, qe1, 2)
+    Ke = max(2, K // 5)
+    times = time_steps(ens, qe, qe1, Ke, flush)
+    el = max_over_ranks(sum(times), ws)
+    dof = ens.dof
+    vens = ws * dof * base.stages * Ke / el
+    res["fp32_batched_ensemble"] = {
+        "value": vens, "unit": UNIT, "ms_per_step": 1e3 * el / Ke, "steps": Ke, "dtype": "f32",
+        "config": {"boxes": 256, "sizes": "uniform from {16,24,32,48}^3, seed 0", "cells": ens.ncells, "dof": dof,
+                   "nbasis": 4, "ivis": 1, "stochastic_stress": True, "rk": "SSP-RK2",
+                   "noise": "kT/(rho dV) = 1e-3, eta = 1, Philox key = realisation id"}}
+    ens.close()
+    del qe, qe1
+    torch.cuda.empty_cache()
+    # plain FP64 on one 48^3 box of the same physics
+    c64 = config.fh_box(48, precision="fp64", seed=0)
+    s = Solver(c64)
+    q = s.from_numpy(ic.equilibrium(c64))
+    q1 = s.new_state()
+    s.advance(q, q1, 2)
+    times = time_steps(s, q, q1, Ke, flush)
+    el = max_over_ranks(sum(times), ws)
+    v64 = ws * c64.dof * c64.stages * Ke / el
+    res["fp64_plain_fh_box48"] = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * el / Ke, "dtype": "f64"}
+    res["fp32_batched_ensemble"]["speedup_vs_fp64_plain"] = vens / v64
+    s.close()
+    return res
+
+
+def cpu_baseline(cfg, Q0, steps):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.set_num_threads(os.cpu_count() or 1)
+    o = O.Oracle(cfg)
+    Q = Q0.copy(order="F")
+    o.advance(Q, 1)
+    t0 = time.perf_counter()
+    o.advance(Q, steps)
+    el = time.perf_counter() - t0
+    return {"value": cfg.dof * cfg.stages * steps / el, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": f"{steps} SSP-RK3 steps of the same 128x128 vortex, FP64, OpenMP over the oracle's (k,j) loops"}
+
+
+def run_reference(args, rank, ws):
+    """The reference algorithm's CPU implementation (the C restatement of the
+    Fortran step; the Fortran itself needs ifort/gfortran, MPI and MKL, none of
+    which exist here) on all host threads, same workload and metric."""
+    from hermeshd_gb300 import config, ic
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cfg = config.isentropic_vortex_2d(n=args.n)
+    nthreads = os.cpu_count() or 1
+    O.set_num_threads(nthreads)
+    o = O.Oracle(cfg)
+    Q = ic.isentropic_vortex(cfg)
+    o.advance(Q, args.warmup)
+    t0 = time.perf_counter()
+    o.advance(Q, args.steps)
+    el = time.perf_counter() - t0
+    v = cfg.dof * cfg.stages * args.steps / el
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "dof": cfg.dof},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": f"{args.steps} full SSP-RK3 steps after {args.warmup} warm-up steps"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        ws = int(os.environ.get("WORLD_SIZE", "1"))
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args, rank, ws)))
+        return 0
+    rank, ws = dist_init()
+    from hermeshd_gb300 import build
+    build.build()
+    out = run_ours(args, rank, ws)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -12,10 +12,9 @@ from . import config, ic  # noqa: F401
 
 def __getattr__(name):
     # lazy: importing the package does not need torch or the CUDA library
+    import importlib
     if name in ("Solver", "Ensemble"):
-        from . import solver
-        return getattr(solver, name)
-    if name == "hermeshd":
-        from . import hermeshd as m
-        return m
+        return getattr(importlib.import_module(__name__ + ".solver"), name)
+    if name in ("hermeshd", "solver"):
+        return importlib.import_module(__name__ + "." + name)
     raise AttributeError(name)

@@ -21,6 +21,7 @@ STATUS = {0: "HERMES_OK", 1: "HERMES_ERR_CONFIG", 2: "HERMES_ERR_SHAPE", 3: "HER
 EXPORTS = ("hermes_abi_version", "hermes_config_size", "hermes_sizes", "hermes_create", "hermes_ensemble_create", "hermes_box_offsets",
            "hermes_destroy", "hermes_last_error", "hermes_stream", "hermes_get_min_dt", "hermes_limiter",
            "hermes_rhs", "hermes_euler_stage", "hermes_step", "hermes_advance", "hermes_advance_host",
+           "hermes_enqueue_steps", "hermes_profile_enable", "hermes_profile_read",
            "hermes_box_times", "hermes_set_time", "hermes_set_noise_step", "hermes_check")
 
 
@@ -101,6 +102,9 @@ def lib() -> C.CDLL:
         "hermes_step": (i32, [vp, vp, vp, vp, dp, dp]),
         "hermes_advance": (i32, [vp, vp, vp, vp, i32, dp, dp]),
         "hermes_advance_host": (i32, [vp, vp, i32, dp, dp]),
+        "hermes_enqueue_steps": (i32, [vp, vp, vp, i32]),
+        "hermes_profile_enable": (i32, [vp, i32]),
+        "hermes_profile_read": (i32, [vp, dp, C.POINTER(C.c_int64)]),
         "hermes_box_times": (i32, [vp, dp, dp]),
         "hermes_set_time": (i32, [vp, C.c_double]),
         "hermes_set_noise_step": (i32, [vp, C.c_uint64]),

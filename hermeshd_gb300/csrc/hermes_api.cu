@@ -85,6 +85,13 @@ struct hermes_ctx {
     void* d_q[2] = {nullptr, nullptr};
     std::vector<GraphEntry> graphs;
     std::string err;
+    // per-kernel event timing
+    bool profiling = false;
+    struct Rec { int kind; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    double prof_ms[6] = {0, 0, 0, 0, 0, 0};
+    long long prof_n[6] = {0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -204,16 +211,45 @@ void destroy_graphs(hermes_ctx* c) {
     c->graphs.clear();
 }
 
+// ---- per-kernel event timing -------------------------------------------
+cudaEvent_t pool_get(hermes_ctx* c) {
+    if (!c->pool.empty()) { cudaEvent_t e = c->pool.back(); c->pool.pop_back(); return e; }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+struct ProfScope {
+    hermes_ctx* c;
+    int kind;
+    cudaEvent_t a = nullptr;
+    ProfScope(hermes_ctx* c_, int kind_) : c(c_), kind(kind_) {
+        if (c->profiling) { a = pool_get(c); cudaEventRecord(a, c->stream); }
+    }
+    ~ProfScope() {
+        if (!c->profiling) return;
+        cudaEvent_t b = pool_get(c);
+        cudaEventRecord(b, c->stream);
+        c->recs.push_back(hermes_ctx::Rec{kind, a, b});
+    }
+};
+
 // ---- enqueue helpers ---------------------------------------------------
 void enq_limit(hermes_ctx* c, void* q) {
-    if (c->cfg.ieos == 1 || c->cfg.ieos == 2) c->K.limit(q, c->G, c->ph, c->stream);   // integrator.f90:110
+    if (c->cfg.ieos == 1 || c->cfg.ieos == 2) {   // integrator.f90:110
+        ProfScope ps(c, 1);
+        c->K.limit(q, c->G, c->ph, c->stream);
+    }
 }
 void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
     FaceArgs a{c->G, c->ph, c->d_step, stage};
-    for (int d = 0; d < 3; ++d) c->K.face(d, q, c->d_flux, a, c->stream);
+    for (int d = 0; d < 3; ++d) {
+        ProfScope ps(c, 2 + d);
+        c->K.face(d, q, c->d_flux, a, c->stream);
+    }
 }
 void enq_cell(hermes_ctx* c, const void* qin, const void* q0, void* out, int mode, int comb, unsigned stage) {
     CellArgs a{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb};
+    ProfScope ps(c, 5);
     c->K.cell(qin, q0, out, c->d_flux, a, c->stream);
 }
 void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, unsigned stage) {
@@ -223,6 +259,7 @@ void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, un
 }
 void enq_mindt(hermes_ctx* c, const void* q, bool advance) {
     DtArgs a{c->G, c->ph, c->d_st};
+    ProfScope ps(c, 0);
     c->K.mindt(q, a, c->stream);
     const int nb = c->G.nbox, tpb = 128;
     if (advance) k_dt_finalize<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st, c->d_step);
@@ -395,6 +432,8 @@ int hermes_destroy(hermes_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     destroy_graphs(c);
+    for (auto& r : c->recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    for (auto e : c->pool) cudaEventDestroy(e);
     cudaFree(c->d_boxes);
     cudaFree(c->d_st);
     cudaFree(c->d_step);
@@ -479,14 +518,24 @@ int hermes_step(hermes_ctx* c, void* q, void* q1, void* q2, double* t, double* d
 }
 
 namespace {
+int enqueue_steps_impl(hermes_ctx* c, void* q, void* q1, int nsteps) {
+    if (c->profiling) {
+        for (int s = 0; s < nsteps; ++s) enq_step(c, q, q1);
+        return launch_status(c);
+    }
+    cudaGraphExec_t exec;
+    int rc = get_graph(c, q, q1, &exec);
+    if (rc) return rc;
+    for (int s = 0; s < nsteps; ++s) HCK(c, cudaGraphLaunch(exec, c->stream));
+    return HERMES_OK;
+}
+
 int advance_impl(hermes_ctx* c, void* q, void* q1, int nsteps, double* t, double* dt) {
     if (t && c->G.nbox == 1) k_set_t<<<1, 32, 0, c->stream>>>(c->d_st, 1, *t);
     int rc = launch_status(c);
     if (rc) return rc;
-    cudaGraphExec_t exec;
-    rc = get_graph(c, q, q1, &exec);
+    rc = enqueue_steps_impl(c, q, q1, nsteps);
     if (rc) return rc;
-    for (int s = 0; s < nsteps; ++s) HCK(c, cudaGraphLaunch(exec, c->stream));
     return read_back(c, t, dt);
 }
 }  // namespace
@@ -498,6 +547,44 @@ int hermes_advance(hermes_ctx* c, void* q, void* q1, void* q2, int nsteps, doubl
     int rc = enter(c);
     if (rc) return rc;
     return leave(c, advance_impl(c, q, q1, nsteps, t, dt));
+}
+
+int hermes_enqueue_steps(hermes_ctx* c, void* q, void* q1, int nsteps) {
+    if (!c || !q || !q1 || nsteps < 0) return fail(c, HERMES_ERR_ARG, "bad argument");
+    if (q == q1) return fail(c, HERMES_ERR_ARG, "q and q1 must be distinct arrays");
+    int rc = enter(c);
+    if (rc) return rc;
+    return leave(c, enqueue_steps_impl(c, q, q1, nsteps));
+}
+
+int hermes_profile_enable(hermes_ctx* c, int enable) {
+    if (!c) return HERMES_ERR_ARG;
+    c->profiling = enable != 0;
+    return HERMES_OK;
+}
+
+int hermes_profile_read(hermes_ctx* c, double* ms, int64_t* launches) {
+    if (!c) return HERMES_ERR_ARG;
+    HCK(c, cudaSetDevice(c->device));
+    HCK(c, cudaStreamSynchronize(c->stream));
+    for (auto& r : c->recs) {
+        float m = 0.f;
+        if (cudaEventElapsedTime(&m, r.a, r.b) == cudaSuccess) {
+            c->prof_ms[r.kind] += m;
+            c->prof_n[r.kind] += 1;
+        }
+        c->pool.push_back(r.a);
+        c->pool.push_back(r.b);
+    }
+    c->recs.clear();
+    cudaGetLastError();
+    for (int k = 0; k < 6; ++k) {
+        if (ms) ms[k] = c->prof_ms[k];
+        if (launches) launches[k] = c->prof_n[k];
+        c->prof_ms[k] = 0;
+        c->prof_n[k] = 0;
+    }
+    return HERMES_OK;
 }
 
 int hermes_advance_host(hermes_ctx* c, void* q_host, int nsteps, double* t, double* dt) {

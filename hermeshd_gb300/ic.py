@@ -98,10 +98,18 @@ def isentropic_vortex_exact(cfg: Config, t: float, ver: int = 1, beta: float = 5
     return (1.0 + dT) ** (1.0 / (g - 1))
 
 
-def taylor_green(cfg: Config, rho: float = 1.0, V0: float = 1.0) -> np.ndarray:
+def taylor_green(cfg: Config, rho: float = 1.0, V0: float = 1.0, perturb: float = 0.0, seed: int = 0) -> np.ndarray:
     """Taylor-Green vortex on [0, 2 pi]^3 (no reference IC): vx = V0 sin x cos y
     cos z, vy = -V0 cos x sin y cos z, vz = 0, rho = 1, p = colvis (= rho
-    c^2/gamma), evaluated at cell centres shifted to [0, L)."""
+    c^2/gamma), evaluated at cell centres shifted to [0, L).
+
+    perturb > 0 adds seeded Gaussian noise of that amplitude to the velocity.
+    The exact field has zero normal velocity on its symmetry planes, where
+    the reference's HLLC with the stress-augmented point flux is
+    discontinuous (the star fluxes differ by P_dd,L - P_dd,R at S_M = 0,
+    flux.f90:87-89,623-643), so the unperturbed problem amplifies rounding
+    differences to O(1e-6) within a few steps; the perturbation moves S_M
+    off zero and makes trajectories comparable between implementations."""
     Q = _background(cfg)
     xc, yc, zc = cell_centres(cfg)
     x, y, z = xc + cfg.lx / 2, yc + cfg.ly / 2, zc + cfg.lz / 2
@@ -109,6 +117,11 @@ def taylor_green(cfg: Config, rho: float = 1.0, V0: float = 1.0) -> np.ndarray:
     vx = V0 * np.sin(X) * np.cos(Y) * np.cos(Z)
     vy = -V0 * np.cos(X) * np.sin(Y) * np.cos(Z)
     vz = np.zeros_like(vx)
+    if perturb > 0:
+        rng = np.random.default_rng(seed)
+        vx = vx + perturb * rng.standard_normal(vx.shape)
+        vy = vy + perturb * rng.standard_normal(vx.shape)
+        vz = vz + perturb * rng.standard_normal(vx.shape)
     p = cfg.colvis if cfg.colvis > 0 else 1.0
     _set_hydro(Q, np.full_like(vx, rho), vx, vy, vz, np.full_like(vx, p), cfg.aindex)
     return Q
@@ -153,4 +166,16 @@ def random_smooth(cfg: Config, seed: int = 0, amp: float = 0.05, stress_amp: flo
         Q[:, :, :, PXX:PYZ + 1, 0] = stress_amp * rng.standard_normal(sh + (6,))
     for b in range(1, nb):
         Q[:, :, :, :, b] = 0.1 * amp * rng.standard_normal(sh + (NQ,)) * np.abs(Q[:, :, :, :, 0]).mean(axis=(0, 1, 2))
+    return Q
+
+
+def ten_moment_stress(cfg: Config, Q: np.ndarray, p: float = 1.0, amp: float = 0.0, seed: int = 0) -> np.ndarray:
+    """Fill the stress slots with the full second-moment tensor of the
+    10-moment (ivis 2) form, P_ij = m_i m_j / rho + p delta_ij, plus seeded
+    noise of amplitude amp, on the cell averages."""
+    rng = np.random.default_rng(seed)
+    rho = Q[:, :, :, RH, 0]
+    m = [Q[:, :, :, MX, 0], Q[:, :, :, MY, 0], Q[:, :, :, MZ, 0]]
+    for v, (a, b) in zip((PXX, PYY, PZZ, PXY, PXZ, PYZ), ((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2))):
+        Q[:, :, :, v, 0] = m[a] * m[b] / rho + (p if a == b else 0.0) + amp * rng.standard_normal(rho.shape)
     return Q

@@ -106,6 +106,27 @@ class Solver:
                                    C.byref(dd)), self.ctx)
         return tt.value, dd.value
 
+    def enqueue_steps(self, q, q1, nsteps: int):
+        """nsteps steps enqueued on the context stream, no synchronisation."""
+        check(lib().hermes_enqueue_steps(self.ctx, self._ptr(q), self._ptr(q1), int(nsteps)), self.ctx)
+
+    @property
+    def cuda_stream(self) -> int:
+        """The private stream the kernels run on (cudaStream_t as int)."""
+        return int(lib().hermes_stream(self.ctx) or 0)
+
+    def profile(self, enable: bool = True):
+        check(lib().hermes_profile_enable(self.ctx, int(enable)), self.ctx)
+
+    KERNEL_KINDS = ("cfl_dt", "limiter", "face_x", "face_y", "face_z", "cell")
+
+    def profile_read(self):
+        ms = np.zeros(6)
+        n = np.zeros(6, dtype=np.int64)
+        check(lib().hermes_profile_read(self.ctx, ms.ctypes.data_as(C.POINTER(C.c_double)),
+                                        n.ctypes.data_as(C.POINTER(C.c_int64))), self.ctx)
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_KINDS)}
+
     def advance_host(self, q_host: np.ndarray, nsteps: int, t: float = 0.0):
         """nsteps on a host array (C-contiguous (nb,nQ,nz,ny,nx) or Fortran
         Q(nx,ny,nz,nQ,nb), dtype matching the precision), updated in place."""

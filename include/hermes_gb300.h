@@ -143,6 +143,18 @@ int hermes_advance(hermes_ctx *ctx, void *q, void *q1, void *q2, int nsteps, dou
  * then copied back).  The reference's interface takes host arrays. */
 int hermes_advance_host(hermes_ctx *ctx, void *q_host, int nsteps, double *t, double *dt);
 
+/* nsteps of step() enqueued on the context's stream from the CUDA graph,
+ * without synchronising; t and dt stay on the device (hermes_box_times). */
+int hermes_enqueue_steps(hermes_ctx *ctx, void *q, void *q1, int nsteps);
+
+/* Per-kernel device timing with CUDA events on the context's stream.  While
+ * enabled, steps run without the graph and every kernel launch is bracketed
+ * by an event pair.  hermes_profile_read synchronises, returns accumulated
+ * milliseconds and launch counts per kernel kind and resets them.  Kinds:
+ * 0 CFL reduction, 1 limiter, 2 x faces, 3 y faces, 4 z faces, 5 cell update. */
+int hermes_profile_enable(hermes_ctx *ctx, int enable);
+int hermes_profile_read(hermes_ctx *ctx, double *ms /* [6] */, int64_t *launches /* [6] */);
+
 /* Per-box time and last time step of an ensemble (nbox entries each). */
 int hermes_box_times(hermes_ctx *ctx, double *t, double *dt);
 /* Set the time of every box (device) */

@@ -109,3 +109,21 @@ def test_wall_sod_symmetry():
     o.advance(Q, 40)
     rho = Q[:, 0, 0, 0, 0]
     assert np.allclose(rho, rho[::-1], rtol=1e-12, atol=1e-14)
+
+
+def test_tgv_symmetry_planes_sit_on_hllc_discontinuity():
+    """The reference's HLLC receives the stress-augmented point flux
+    (flux.f90:87-89); its star fluxes then differ by P_xx,L - P_xx,R at
+    S_M = 0, and the exact Taylor-Green field has S_M = 0 on its symmetry
+    planes.  A 1e-14 nudge of one value therefore moves the oracle's own
+    trajectory by ~1e-6 in 50 steps, while a symmetry-broken field stays
+    conditioned at rounding level."""
+    cfg = config.taylor_green_3d(n=8, precision="fp64")
+    for perturb, lo, hi in ((0.0, 1e-8, 1.0), (1e-3, 0.0, 1e-12)):
+        Q = ic.taylor_green(cfg, perturb=perturb, seed=1)
+        Qp = Q.copy(order="F")
+        Qp[3, 3, 3, 1, 0] *= 1 + 1e-14
+        O.Oracle(cfg).advance(Q, 50)
+        O.Oracle(cfg).advance(Qp, 50)
+        sens = np.linalg.norm(Q - Qp) / np.linalg.norm(Q)
+        assert lo <= sens < hi, (perturb, sens)

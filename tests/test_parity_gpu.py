@@ -49,6 +49,8 @@ RHS_CASES = {
 def test_rhs_parity(name):
     cfg, stress = RHS_CASES[name]
     Q = ic.random_smooth(cfg, seed=7, amp=0.1, stress_amp=0.05 * stress)
+    if cfg.ivis == 2:
+        Q = ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.01)
     o = _oracle(cfg)
     Qo = Q.copy(order="F")
     r_o = o.rhs(Qo, limit=True)
@@ -95,7 +97,10 @@ def test_min_dt_parity():
 STEP_CASES = {
     "sod_256_rk2_nb4": (lambda: config.sod_1d(nx=256), lambda c: ic.sod(c)),
     "vortex_16_rk3_nb10": (lambda: config.isentropic_vortex_2d(n=16), lambda c: ic.isentropic_vortex(c)),
-    "tgv_8_rk3_nb4_ivis1": (lambda: config.taylor_green_3d(n=8, precision="fp64"), lambda c: ic.taylor_green(c)),
+    # symmetry broken by 1e-3: the exact field sits on the reference HLLC's
+    # discontinuity (see ic.taylor_green and test_oracle_kat)
+    "tgv_8_rk3_nb4_ivis1": (lambda: config.taylor_green_3d(n=8, precision="fp64"),
+                            lambda c: ic.taylor_green(c, perturb=1e-3, seed=1)),
     "random_nb8_walls_rk2": (lambda: config.Config(nx=10, ny=6, nz=3, nbasis=8, iquad=2, ivis=1, coll=2.0, colvis=0.5,
                                                    xlobc="wall", xhibc="noslip", zlobc="outflow", zhibc="wall"),
                              lambda c: ic.random_smooth(c, seed=5, amp=0.05, stress_amp=0.01)),
