@@ -207,6 +207,7 @@ def run_ours(args, rank, ws):
         times = time_steps(s, q, q1, K, flush)
     elapsed = max_over_ranks(sum(times), ws)
     clocks = clk.summary()
+    qg64 = q.clone()          # FP64 state after W + K steps, the reference for the FP32 error
     dof_stage = cfg.dof * cfg.stages
     value = ws * dof_stage * K / elapsed
     ms_per_step = 1e3 * elapsed / K
@@ -267,7 +268,6 @@ def run_ours(args, rank, ws):
     out["alu"] = {"bound_by": "fp64 pipe", "flops_per_cell_stage": fl, "achieved_tflops": step_flops / (ms_per_step * 1e-3) / 1e12,
                   "peak": ap, "frac_fp64": (step_flops / (ms_per_step * 1e-3) / 1e12) / ap["fp64_tflops"] if "fp64_tflops" in ap else None,
                   "flop_model": "algorithmic: nonzero table products (FMA = 2), division/sqrt = 1"}
-    qg64 = q.clone()
     s.close()
 
     # ---- variants -------------------------------------------------------
