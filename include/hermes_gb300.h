@@ -168,6 +168,27 @@ int hermes_set_noise_step(hermes_ctx *ctx, uint64_t step);
  * NaN cell average was produced), cleared on read.  Synchronises. */
 int hermes_check(hermes_ctx *ctx);
 
+/* The right-hand side of hermes_rhs for one grid, computed without a
+ * context and without allocating any device memory.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory when they need
+ * a right-hand side: a host code whose device memory belongs to its own
+ * framework or pool (for example a Fortran/MPI driver calling through its FFI
+ * under a fixed memory budget), or a time loop that must not pay
+ * cudaMalloc's device-wide synchronisation.
+ *
+ * q, rhs: device arrays of cfg's grid (q limited in place when apply_limiter);
+ * stream: the cudaStream_t to run on (NULL = legacy default stream); the call
+ * returns without synchronising.  The face-flux scratch lives in a static
+ * device array of HERMES_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library holds until exit; a grid whose face fluxes do not fit returns
+ * HERMES_ERR_SHAPE.  All calls share that array: calls that overlap on the GPU
+ * race.  The first call on a device looks up the array's device address and
+ * should come before any stream capture.  err (errlen bytes, may be NULL)
+ * receives a message on failure. */
+#define HERMES_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int hermes_rhs_noalloc(const hermes_config *cfg, void *q, void *rhs, int apply_limiter, void *stream, char *err,
+                       size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif
