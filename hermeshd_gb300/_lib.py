@@ -56,7 +56,7 @@ def to_c(cfg: Config) -> HermesConfig:
     c = HermesConfig()
     c.nx, c.ny, c.nz = cfg.nx, cfg.ny, cfg.nz
     c.nbasis, c.iquad, c.iorder = cfg.nbasis, cfg.iquad, cfg.iorder
-    c.ivis, c.ieos, c.ihllc = cfg.ivis, cfg.ieos, int(bool(cfg.ihllc))
+    c.ivis, c.ieos, c.ihllc = cfg.ivis, cfg.ieos, int(cfg.ihllc)
     for i, b in enumerate(cfg.bc):
         c.bc[i] = b
     c.precision = 64 if cfg.precision == "fp64" else 32

@@ -90,9 +90,9 @@ class Config:
     iquad: int = 2
     iorder: int = 2                  # 2 'heun', 3 'shu-osher' (integrator.f90:39-55)
     # physics switches
-    ivis: int = 0                    # 0 explicit, 1 semi-implicit stress, 2 10-moment
+    ivis: int = 0                    # 0 explicit, 1 semi-implicit stress, 2 10-moment, 3 Grad closure (E_ij)
     ieos: int = 1                    # 1 ideal gas, 2 Murnaghan-Tait
-    ihllc: bool = True
+    ihllc: int = 1                   # 0 central/LLF, 1 HLLC, 2 Roe (the monolithic code's iroe)
     aindex: float = 5.0 / 3.0        # gamma
     rh_floor: float = 5.0e-6         # params.f90:93
     T_floor: float = field(default_factory=lambda: Units().T_floor)
@@ -162,8 +162,10 @@ class Config:
             raise ValueError(f"(nbasis, iquad) = ({self.nbasis}, {self.iquad}) not in {allowed}")
         if min(self.nx, self.ny, self.nz) < 1:
             raise ValueError("grid dimensions must be >= 1")
-        if self.ivis not in (0, 1, 2) or self.ieos not in (1, 2) or self.iorder not in (2, 3):
-            raise ValueError("ivis in {0,1,2}, ieos in {1,2}, iorder in {2,3}")
+        if self.ivis not in (0, 1, 2, 3) or self.ieos not in (1, 2) or self.iorder not in (2, 3):
+            raise ValueError("ivis in {0,1,2,3}, ieos in {1,2}, iorder in {2,3}")
+        if int(self.ihllc) not in (0, 1, 2):
+            raise ValueError("ihllc in {0 central/LLF, 1 HLLC, 2 Roe}")
         if self.precision not in ("fp64", "fp32"):
             raise ValueError("precision must be 'fp64' or 'fp32'")
 
@@ -183,7 +185,7 @@ def sod_1d(nx: int = 256, **kw) -> Config:
     with velocity and time rescaled by sqrt(P_base)."""
     u = Units(TK=300.0, mu=18.0)
     c = Config(nx=nx, ny=1, nz=1, lx=1.0, ly=1.0 / 12.0, lz=1.0 / 120.0, nbasis=4, iquad=2, iorder=2,
-               ivis=0, ieos=1, ihllc=True, aindex=5.0 / 3.0, T_floor=u.T_floor / u.P_base,
+               ivis=0, ieos=1, ihllc=1, aindex=5.0 / 3.0, T_floor=u.T_floor / u.P_base,
                P_1=u.P_1 / u.P_base, P_base=1.0, cflm=0.3, xlobc="wall", xhibc="wall", tf=0.2)
     return c.replace(**kw)
 
@@ -195,7 +197,7 @@ def isentropic_vortex_2d(n: int = 128, precision: str = "fp64", **kw) -> Config:
     tests/2D_isentropic_vortex/{input,params}_isentr.f90."""
     u = units_isentropic_vortex()
     c = Config(nx=n, ny=n, nz=1, lx=10.0, ly=10.0, lz=10.0 / 120.0, nbasis=10, iquad=3, iorder=3,
-               ivis=0, ieos=1, ihllc=True, aindex=7.0 / 5.0, T_floor=u.T_floor, P_1=u.P_1, P_base=u.P_base,
+               ivis=0, ieos=1, ihllc=1, aindex=7.0 / 5.0, T_floor=u.T_floor, P_1=u.P_1, P_base=u.P_base,
                tf=10.0, precision=precision)
     return c.replace(**kw)
 
@@ -210,7 +212,7 @@ def taylor_green_3d(n: int = 64, precision: str = "fp32", mach: float = 0.1, rey
     p = cs * cs / gamma
     mu = 1.0 / reynolds
     L = 2.0 * math.pi
-    c = Config(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, nbasis=4, iquad=2, iorder=3, ivis=1, ieos=1, ihllc=True,
+    c = Config(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, nbasis=4, iquad=2, iorder=3, ivis=1, ieos=1, ihllc=1,
                aindex=gamma, coll=p / mu, colvis=p, precision=precision)
     return c.replace(**kw)
 
@@ -229,7 +231,7 @@ def fh_box(n: int, eta: float = 1.0, kT_over_rho_dV: float = 1.0e-3, seed: int =
     L = n * dx
     p = 1.0
     eta_sd = math.sqrt(2.0 * eta * 1.0 / (dV * dt_noise))
-    c = Config(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, nbasis=4, iquad=2, iorder=2, ivis=1, ieos=1, ihllc=True,
+    c = Config(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, nbasis=4, iquad=2, iorder=2, ivis=1, ieos=1, ihllc=1,
                aindex=gamma, coll=p / eta, colvis=p, llns=True, eta_sd=eta_sd, zeta_sd=0.0, seed=seed,
                precision=precision)
     return c.replace(**kw)
@@ -241,6 +243,6 @@ def poiseuille_2d(nx: int = 64, ny: int = 128, viscosity: float = 0.05, body_for
     driven by a uniform body force in x.  rho = 1, p = 1."""
     p = 1.0
     c = Config(nx=nx, ny=ny, nz=1, lx=2.0, ly=1.0, lz=1.0 / 120.0, nbasis=4, iquad=2, iorder=2, ivis=1, ieos=1,
-               ihllc=True, aindex=5.0 / 3.0, coll=p / viscosity, colvis=p, ylobc="noslip", yhibc="noslip",
+               ihllc=1, aindex=5.0 / 3.0, coll=p / viscosity, colvis=p, ylobc="noslip", yhibc="noslip",
                body_force=body_force)
     return c.replace(**kw)

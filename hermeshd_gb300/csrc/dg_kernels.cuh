@@ -342,7 +342,7 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
         point_flux<T, DIR>(ph, qR, wR, SR, fR);
     }
     // flux.f90:243-262: central flux, LLF with the freezing speed for ivis 2
-    if (ph.ivis == 2) {
+    if (ph.ivis >= 2) {   // ivis 3: the Grad-closure code always applies LLF (ten_moment.f90:1131-1147)
         const T cfr = fmax(cfcal<T, DIR>(ph, qL), cfcal<T, DIR>(ph, qR));
 #pragma unroll
         for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]) - T(0.5) * cfr * (qR[v] - qL[v]);
@@ -350,7 +350,12 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
 #pragma unroll
         for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]);
     }
-    if (ph.ihllc) {
+    if (ph.ihllc == 2) {
+        T FR[NQ];
+        if (roe<T, DIR>(ph, qL, qR, fL, fR, FR)) {
+            F[RH] = FR[RH]; F[MX] = FR[MX]; F[MY] = FR[MY]; F[MZ] = FR[MZ]; F[EN] = FR[EN];
+        }
+    } else if (ph.ihllc == 1) {
         T rho_i_last = T(0);
         if (ph.ieos == 2) {
             // 1/rho of the last point of the reference's call: the right state at point NF-1
@@ -394,6 +399,7 @@ struct CellArgs {
     int* flags;
     unsigned stage;
     int mode, comb;
+    int split_source;   // Grad closure with RK2: the implicit source step after the update
 };
 
 template <class T, class TB>
@@ -530,7 +536,11 @@ __global__ void __launch_bounds__(CELL_TPB) k_cell(const T* Qin, const T* Q0, T*
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
             T e = QS(b, v) - dt * r[b];                    // integrator.f90:147-149,171-173
-            if (ph.ivis != 0 && v >= PXX) e = faci * e;    // integrator.f90:174,220-224
+            if ((ph.ivis == 1 || ph.ivis == 2) && v >= PXX) e = faci * e;   // integrator.f90:174,220-224
+            if (a.split_source) {                          // combined after the source step below
+                QS(b, v) = e;
+                continue;
+            }
             T o = e;
             if (a.comb != COMB_NONE) {
                 const T q0 = q0b[(long long)(b * NQ + v) * nc + le];
@@ -601,6 +611,75 @@ __global__ void __launch_bounds__(CELL_TPB) k_cell(const T* Qin, const T* Q0, T*
             finish(v, r);
         }
     });
+    if (a.split_source) {
+        // Grad closure: implicit relaxation of E_ij with the sources of the
+        // advected state (ten_moment.f90:719-793 source_calc, :839-892
+        // advance_time_level_source), then the RK combination and the store.
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int m = 0; m < 6; ++m) ACC(b, PXX + m) = T(0);
+        const T coll = T(ph.coll), oth = T(1.0 / 3.0);
+        sfor<NPG>([&](auto gg) {
+            constexpr int g = decltype(gg)::value;
+            T u[4];
+            sfor<4>([&](auto vv) {
+                constexpr int v = decltype(vv)::value;
+                T s = T(0);
+                sfor<NB>([&](auto bb) {
+                    constexpr int b = decltype(bb)::value;
+                    constexpr double c = TB::INT(g, b);
+                    if constexpr (c != 0.0) s = fma(T(c), QS(b, v), s);
+                });
+                u[v] = s;
+            });
+            const T dni = T(1) / u[RH];
+            const T vx = u[MX] * dni, vy = u[MY] * dni, vz = u[MZ] * dni, cd = coll * u[RH];
+            T S[6];
+            S[0] = cd * (T(2) * vx * vx - vy * vy - vz * vz) * oth;
+            S[1] = cd * (T(2) * vy * vy - vz * vz - vx * vx) * oth;
+            S[2] = cd * (T(2) * vz * vz - vx * vx - vy * vy) * oth;
+            S[3] = cd * vx * vy;
+            S[4] = cd * vx * vz;
+            S[5] = cd * vy * vz;
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr double c = TB::SRC(g, b);
+                if constexpr (c != 0.0) {
+#pragma unroll
+                    for (int m = 0; m < 6; ++m) ACC(b, PXX + m) = fma(T(c), S[m], ACC(b, PXX + m));
+                }
+            });
+        });
+        const T den = T(1) + dt * coll;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            T E[6];
+#pragma unroll
+            for (int m = 0; m < 6; ++m) E[m] = QS(b, PXX + m);
+            const T Esum = coll * dt * (E[0] + E[1] + E[2]) * oth;
+            const T Ssum = coll * (dt * dt) * (ACC(b, PXX) + ACC(b, PYY) + ACC(b, PZZ)) * oth;
+#pragma unroll
+            for (int m = 0; m < 3; ++m) QS(b, PXX + m) = (E[m] + dt * ACC(b, PXX + m) + Esum + Ssum) / den;
+#pragma unroll
+            for (int m = 3; m < 6; ++m) QS(b, PXX + m) = (E[m] + dt * ACC(b, PXX + m)) / den;
+        }
+#pragma unroll
+        for (int v = 0; v < NQ; ++v)
+#pragma unroll
+            for (int b = 0; b < NB; ++b) {
+                const T e = QS(b, v);
+                T o = e;
+                if (a.comb != COMB_NONE) {
+                    const T q0 = q0b[(long long)(b * NQ + v) * nc + le];
+                    if (a.comb == COMB_HALF) o = T(0.5) * (q0 + e);
+                    else if (a.comb == COMB_34) o = T(0.75) * q0 + T(0.25) * e;
+                    else o = T(1.0 / 3.0) * q0 + T(2.0 / 3.0) * e;
+                }
+                if (b == 0 && o != o) bad = true;
+                ob[(long long)(b * NQ + v) * nc + le] = o;
+            }
+    }
     if (bad) a.flags[0] |= FLAG_NONFINITE;   // integrator.f90:234-250 (the reference exits)
 #undef QS
 #undef ACC

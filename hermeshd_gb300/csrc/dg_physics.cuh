@@ -123,7 +123,7 @@ __device__ __forceinline__ void point_flux(const Phys& ph, const T q[NQ], const 
     const T P_xx = q[PXX], P_yy = q[PYY], P_zz = q[PZZ], P_xy = q[PXY], P_xz = q[PXZ], P_yz = q[PYZ];
     const T vx = w.vx, vy = w.vy, vz = w.vz, P = w.P, P_10 = w.P_10, P_5 = w.P;
     const T Sxx = S[0], Syy = S[1], Szz = S[2], Sxy = S[3], Sxz = S[4], Syz = S[5];
-    const bool tenm = (ph.ivis == 2);
+    const bool tenm = (ph.ivis >= 2);   // ivis 2 and the Grad closure (ivis 3)
     if constexpr (DIR == 0) {
         f[RH] = M_x;
         if (!tenm) {
@@ -136,6 +136,7 @@ __device__ __forceinline__ void point_flux(const Phys& ph, const T q[NQ], const 
             f[MZ] = P_xz;
         }
         f[EN] = (Ener + P) * vx + (P_xx - Sxx) * vx + (P_xy - Sxy) * vy + (P_xz - Sxz) * vz;
+        if (ph.ivis == 3) f[EN] = (Ener + P) * vx;   // Grad closure: ten_moment.f90:969
         if (!tenm) {
             f[PXX] = c4d3cv * vx; f[PYY] = -c2d3cv * vx; f[PZZ] = -c2d3cv * vx;
             f[PXY] = colvis * vy; f[PXZ] = colvis * vz; f[PYZ] = T(0);
@@ -159,6 +160,7 @@ __device__ __forceinline__ void point_flux(const Phys& ph, const T q[NQ], const 
             f[MZ] = P_yz;
         }
         f[EN] = (Ener + P) * vy + (P_yy - Syy) * vy + (P_xy - Sxy) * vx + (P_yz - Syz) * vz;
+        if (ph.ivis == 3) f[EN] = (Ener + P) * vy;   // Grad closure: ten_moment.f90:969
         if (!tenm) {
             f[PXX] = -c2d3cv * vy; f[PYY] = c4d3cv * vy; f[PZZ] = -c2d3cv * vy;
             f[PXY] = colvis * vx; f[PXZ] = T(0); f[PYZ] = colvis * vz;
@@ -182,6 +184,7 @@ __device__ __forceinline__ void point_flux(const Phys& ph, const T q[NQ], const 
             f[MZ] = P_zz - P_10 + P_5;
         }
         f[EN] = (Ener + P) * vz + (P_zz - Szz) * vz + (P_xz - Sxz) * vx + (P_yz - Syz) * vy;
+        if (ph.ivis == 3) f[EN] = (Ener + P) * vz;   // Grad closure: ten_moment.f90:969
         if (!tenm) {
             f[PXX] = -c2d3cv * vz; f[PYY] = -c2d3cv * vz; f[PZZ] = c4d3cv * vz;
             f[PXY] = T(0); f[PXZ] = colvis * vx; f[PYZ] = colvis * vy;
@@ -284,6 +287,69 @@ __device__ __forceinline__ void hllc(const Phys& ph, const T qL[NQ], const T qR[
         out[0] = out[1] = out[2] = out[3] = out[4] = nan;
     }
     F[RH] = out[0]; F[IPAR] = out[1]; F[IP1] = out[2]; F[IP2] = out[3]; F[EN] = out[4];
+}
+
+
+// ---------------------------------------------------------------------------
+// Roe solver of the monolithic 10-moment code
+// (src/ces/10_moment/dg_3D_hydro_lqc_SEAN.f90:1614-1789) at one face point.
+// Returns false (kroe = 0: keep the central/LLF flux) when the Roe sound
+// speed squared is <= 0; otherwise writes rh..en of F.  The Roe enthalpy
+// keeps the reference's factor 1/2 on its pressure term (:1676).
+// ---------------------------------------------------------------------------
+template <class T, int DIR>
+__device__ __forceinline__ bool roe(const Phys& ph, const T qL[NQ], const T qR[NQ], const T fL[NQ], const T fR[NQ],
+                                    T F[NQ]) {
+    constexpr int IP = DIR == 0 ? MX : DIR == 1 ? MY : MZ;
+    constexpr int I1 = DIR == 0 ? MY : DIR == 1 ? MZ : MX;
+    constexpr int I2 = DIR == 0 ? MZ : DIR == 1 ? MX : MY;
+    const T aindm1 = T(ph.aindm1), cp = T(ph.aindex / ph.aindm1);
+    T skr[2], swr[2][4];
+#pragma unroll
+    for (int j9 = 0; j9 < 2; ++j9) {
+        const T* q = j9 == 0 ? qL : qR;
+        const T dnii = T(1) / q[RH];
+        const T v0 = q[IP] * dnii, v1 = q[I1] * dnii, v2 = q[I2] * dnii;
+        const T vsq = v0 * v0 + v1 * v1 + v2 * v2;
+        const T Pri = aindm1 * (q[EN] - T(0.5) * q[RH] * vsq);
+        skr[j9] = sqrt(q[RH]);
+        swr[j9][0] = skr[j9] * v0;
+        swr[j9][1] = skr[j9] * v1;
+        swr[j9][2] = skr[j9] * v2;
+        swr[j9][3] = T(0.5) * skr[j9] * (vsq + cp * Pri / q[RH]);
+    }
+    const T Qri = T(1) / qL[RH];
+    const T delrho = qR[RH] * Qri - T(1);
+    const T dele = (qR[EN] - qL[EN]) * Qri;
+    const T dm1 = (qR[IP] - qL[IP]) * Qri, dm2 = (qR[I1] - qL[I1]) * Qri, dm3 = (qR[I2] - qL[I2]) * Qri;
+    const T dsk = T(0.5) * (skr[1] + skr[0]);
+    const T vc0 = T(0.5) * (swr[1][0] + swr[0][0]) / dsk;
+    const T vc1 = T(0.5) * (swr[1][1] + swr[0][1]) / dsk;
+    const T vc2 = T(0.5) * (swr[1][2] + swr[0][2]) / dsk;
+    const T hc = T(0.5) * (swr[1][3] + swr[0][3]) / dsk;
+    const T vcsq = vc0 * vc0 + vc1 * vc1 + vc2 * vc2;
+    const T asq = aindm1 * (hc - T(0.5) * vcsq);
+    if (!(asq > T(0))) return false;
+    const T sc9 = sqrt(asq);
+    const T l0 = fabs(vc0 - sc9), l1 = fabs(vc0 + sc9), l2 = fabs(vc0);
+    const T ea2i = aindm1 / asq;
+    const T vcdel = vc0 * dm1 + vc1 * dm2 + vc2 * dm3 - dele;
+    const T a9e = T(0.5) * ea2i * (T(0.5) * vcsq * delrho - vcdel);
+    const T sk9 = T(0.5) * (dm1 - vc0 * delrho) / sc9;
+    const T w0 = (a9e - sk9) * l0, w1 = (a9e + sk9) * l1, w2 = ea2i * ((hc - vcsq) * delrho + vcdel) * l2;
+    const T w3 = (dm2 - vc1 * delrho) * l2, w4 = (dm3 - vc2 * delrho) * l2;
+    // dF = sum_j w_j evec(:, j), scaled by rho_L
+    const T d0 = (w0 + w1 + w2) * qL[RH];
+    const T d1 = (w0 * (hc - sc9 * vc0) + w1 * (hc + sc9 * vc0) + w2 * (T(0.5) * vcsq) + w3 * vc1 + w4 * vc2) * qL[RH];
+    const T d2 = (w0 * (vc0 - sc9) + w1 * (vc0 + sc9) + w2 * vc0) * qL[RH];
+    const T d3 = ((w0 + w1 + w2) * vc1 + w3) * qL[RH];
+    const T d4 = ((w0 + w1 + w2) * vc2 + w4) * qL[RH];
+    F[RH] = T(0.5) * (fL[RH] + fR[RH] - d0);
+    F[EN] = T(0.5) * (fL[EN] + fR[EN] - d1);
+    F[IP] = T(0.5) * (fL[IP] + fR[IP] - d2);
+    F[I1] = T(0.5) * (fL[I1] + fR[I1] - d3);
+    F[I2] = T(0.5) * (fL[I2] + fR[I2] - d4);
+    return true;
 }
 
 }  // namespace hermes

@@ -129,7 +129,8 @@ std::string check_config(const hermes_config& c) {
         return "unsupported (nbasis, iquad): supported are (4,2), (8,2), (10,3)";
     if (c.precision != 64 && c.precision != 32) return "precision must be 64 or 32";
     if (c.nx < 1 || c.ny < 1 || c.nz < 1) return "grid dimensions must be >= 1";
-    if (c.ivis < 0 || c.ivis > 2) return "ivis must be 0, 1 or 2";
+    if (c.ivis < 0 || c.ivis > 3) return "ivis must be 0, 1, 2 or 3 (Grad closure)";
+    if (c.ihllc < 0 || c.ihllc > 2) return "ihllc must be 0 (central/LLF), 1 (HLLC) or 2 (Roe)";
     if (c.ieos != 1 && c.ieos != 2) return "ieos must be 1 or 2";
     if (c.iorder != 2 && c.iorder != 3) return "iorder must be 2 or 3";
     for (int i = 0; i < 6; ++i)
@@ -159,7 +160,7 @@ Phys make_phys(const hermes_config& c) {
     p.body_force = c.body_force;
     p.ivis = c.ivis;
     p.ieos = c.ieos;
-    p.ihllc = c.ihllc ? 1 : 0;
+    p.ihllc = c.ihllc;
     p.llns = c.llns ? 1 : 0;
     return p;
 }
@@ -248,7 +249,8 @@ void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
     }
 }
 void enq_cell(hermes_ctx* c, const void* qin, const void* q0, void* out, int mode, int comb, unsigned stage) {
-    CellArgs a{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb};
+    const int split = (mode == MODE_STAGE && c->cfg.ivis == 3 && c->cfg.iorder == 2) ? 1 : 0;
+    CellArgs a{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb, split};
     ProfScope ps(c, 5);
     c->K.cell(qin, q0, out, c->d_flux, a, c->stream);
 }

@@ -91,7 +91,7 @@ int device_addrs(int dev, DevAddrs** out, char* err, size_t errlen) {
 bool supported(const hermes_config& c) {
     const bool basis = (c.nbasis == 4 && c.iquad == 2) || (c.nbasis == 8 && c.iquad == 2) || (c.nbasis == 10 && c.iquad == 3);
     bool ok = basis && (c.precision == 64 || c.precision == 32) && c.nx >= 1 && c.ny >= 1 && c.nz >= 1 &&
-              c.ivis >= 0 && c.ivis <= 2 && (c.ieos == 1 || c.ieos == 2) && c.lx > 0 && c.ly > 0 && c.lz > 0;
+              c.ivis >= 0 && c.ivis <= 3 && c.ihllc >= 0 && c.ihllc <= 2 && (c.ieos == 1 || c.ieos == 2) && c.lx > 0 && c.ly > 0 && c.lz > 0;
     for (int i = 0; i < 6; ++i) ok = ok && c.bc[i] >= 0 && c.bc[i] <= 3;
     return ok;
 }
@@ -175,7 +175,7 @@ extern "C" int hermes_rhs_noalloc(const hermes_config* cfg, void* q, void* rhs, 
     ph.aindex = c.aindex; ph.aindm1 = c.aindex - 1.0; ph.rh_floor = c.rh_floor; ph.T_floor = c.T_floor;
     ph.P_floor = c.T_floor * c.rh_floor; ph.rh_mult = c.rh_mult; ph.coll = c.coll; ph.colvis = c.colvis;
     ph.P_1 = c.P_1; ph.P_base = c.P_base; ph.eta_sd = c.eta_sd; ph.zeta_sd = c.zeta_sd;
-    ph.body_force = c.body_force; ph.ivis = c.ivis; ph.ieos = c.ieos; ph.ihllc = c.ihllc ? 1 : 0;
+    ph.body_force = c.body_force; ph.ivis = c.ivis; ph.ieos = c.ieos; ph.ihllc = c.ihllc;
     ph.llns = c.llns ? 1 : 0;
     Geom G{};
     G.boxes = A->box;
@@ -186,7 +186,7 @@ extern "C" int hermes_rhs_noalloc(const hermes_config* cfg, void* q, void* rhs, 
     if (apply_limiter && (c.ieos == 1 || c.ieos == 2)) K.limit(q, G, ph, s);
     FaceArgs fa{G, ph, A->step, 0u};
     for (int d = 0; d < 3; ++d) K.face(d, q, A->scratch, fa, s);
-    CellArgs ca{G, ph, A->state, A->step, A->flags, 0u, MODE_RHS, COMB_NONE};
+    CellArgs ca{G, ph, A->state, A->step, A->flags, 0u, MODE_RHS, COMB_NONE, 0};
     K.cell(q, nullptr, rhs, A->scratch, ca, s);
     e = cudaGetLastError();
     if (e != cudaSuccess) { set_err(err, errlen, cudaGetErrorString(e)); return HERMES_ERR_CUDA; }

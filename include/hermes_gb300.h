@@ -54,9 +54,12 @@ typedef struct hermes_config {
     int32_t nx, ny, nz;        /* cells; input.f90 nx, ny, nz with one MPI domain */
     int32_t nbasis, iquad;     /* (4,2), (8,2) or (10,3): input.f90 nbasis, iquad */
     int32_t iorder;            /* 2 'heun' or 3 'shu-osher': integrator.f90:39-55 */
-    int32_t ivis;              /* 0, 1, 2: input.f90 ivis */
+    int32_t ivis;              /* 0, 1, 2: input.f90 ivis; 3: Grad closure (E_ij form with an implicit
+                                  source step after each RK2 stage) of src/ces/10_moment/
+                                  dg_3D_hydro_bitri_ten_moment.f90 (its ivis 0) */
     int32_t ieos;              /* 1 ideal gas, 2 Murnaghan-Tait */
-    int32_t ihllc;             /* nonzero: HLLC for rh..en (flux.f90:264-271) */
+    int32_t ihllc;             /* Riemann solver for rh..en: 0 central/LLF only, 1 HLLC (flux.f90:264-271),
+                                  2 Roe (src/ces/10_moment/dg_3D_hydro_lqc_SEAN.f90:1614-1789) */
     int32_t bc[6];             /* xlo, xhi, ylo, yhi, zlo, zhi: HERMES_BC_* */
     int32_t precision;         /* 64 (FP64) or 32 (FP32 bulk, FP64 CFL and limiter fixes) */
     int32_t llns;              /* nonzero: stochastic stress (random.f90:106-145) */

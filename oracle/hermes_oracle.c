@@ -482,6 +482,8 @@ static void flux_calc_pnts_r(const orc_ctx *c, const double *Qp, double *fp, int
                 FP(MZ) = P_xz;
             }
             FP(EN) = (Ener + P) * vx + (P_xx - Sxx) * vx + (P_xy - Sxy) * vy + (P_xz - Sxz) * vz;
+            /* Grad closure (ivis 3): dg_3D_hydro_bitri_ten_moment.f90:969 */
+            if (ivis == 3) FP(EN) = (Ener + P) * vx;
             if (ivis == 0 || ivis == 1) {
                 FP(PXX) = c4d3cv * vx; FP(PYY) = -c2d3cv * vx; FP(PZZ) = -c2d3cv * vx;
                 FP(PXY) = colvis * vy; FP(PXZ) = colvis * vz; FP(PYZ) = 0;
@@ -506,6 +508,8 @@ static void flux_calc_pnts_r(const orc_ctx *c, const double *Qp, double *fp, int
                 FP(MZ) = P_yz;
             }
             FP(EN) = (Ener + P) * vy + (P_yy - Syy) * vy + (P_xy - Sxy) * vx + (P_yz - Syz) * vz;
+            /* Grad closure (ivis 3): dg_3D_hydro_bitri_ten_moment.f90:969 */
+            if (ivis == 3) FP(EN) = (Ener + P) * vy;
             if (ivis == 0 || ivis == 1) {
                 FP(PXX) = -c2d3cv * vy; FP(PYY) = c4d3cv * vy; FP(PZZ) = -c2d3cv * vy;
                 FP(PXY) = colvis * vx; FP(PXZ) = 0; FP(PYZ) = colvis * vz;
@@ -530,6 +534,8 @@ static void flux_calc_pnts_r(const orc_ctx *c, const double *Qp, double *fp, int
                 FP(MZ) = P_zz - P_10 + P_5;
             }
             FP(EN) = (Ener + P) * vz + (P_zz - Szz) * vz + (P_xz - Sxz) * vx + (P_yz - Syz) * vy;
+            /* Grad closure (ivis 3): dg_3D_hydro_bitri_ten_moment.f90:969 */
+            if (ivis == 3) FP(EN) = (Ener + P) * vz;
             if (ivis == 0 || ivis == 1) {
                 FP(PXX) = -c2d3cv * vz; FP(PYY) = -c2d3cv * vz; FP(PZZ) = c4d3cv * vz;
                 FP(PXY) = 0; FP(PXZ) = colvis * vx; FP(PYZ) = colvis * vy;
@@ -651,6 +657,78 @@ static void flux_hllc(const orc_ctx *c, const double *Qlr, const double *flr, do
             for (int e = 0; e < 5; ++e) out[e] = FL(i4 + nf, ivar[e]);
         /* fhllc(i4, ivar(e)) = out(e) */
         for (int e = 0; e < 5; ++e) fhllc[(size_t)ivar[e] * nf + i4] = out[e];
+    }
+#undef QL
+#undef FL
+}
+
+/* Roe solver of the monolithic 10-moment code
+ * (src/ces/10_moment/dg_3D_hydro_lqc_SEAN.f90:1614-1789, Eulderink-Mellema):
+ * F = (F_L + F_R - dF)/2 for rh..en with dF from the Roe-averaged
+ * eigensystem; kroe = 0 (keep the central/LLF flux) where the Roe sound speed
+ * squared is <= 0.  Reproduces the reference's Roe enthalpy, whose pressure
+ * term carries a factor 1/2 (:1676). */
+static void flux_roe(const orc_ctx *c, const double *Qlr, const double *flr, double *froe, int *kroe, int ixyz) {
+    const int nf = c->nface, nfe = c->nfe;
+    int ip, i1, i2;
+    if (ixyz == 1) { ip = MX; i1 = MY; i2 = MZ; }
+    else if (ixyz == 2) { ip = MY; i1 = MZ; i2 = MX; }
+    else { ip = MZ; i1 = MX; i2 = MY; }
+    const double aindm1 = c->aindm1, cp = c->p.aindex / c->aindm1;
+#define QL(k, v) Qlr[(size_t)(v) * nfe + (k)]
+#define FL(k, v) flr[(size_t)(v) * nfe + (k)]
+    for (int i9 = 0; i9 < nf; ++i9) {
+        double skr[2], swr[2][4];
+        kroe[i9] = 1;
+        for (int j9 = 0; j9 < 2; ++j9) {
+            int ilr = i9 + j9 * nf;
+            double dnii = 1. / QL(ilr, RH);
+            double v0 = QL(ilr, ip) * dnii, v1 = QL(ilr, i1) * dnii, v2 = QL(ilr, i2) * dnii;
+            double vsq = v0 * v0 + v1 * v1 + v2 * v2;
+            double Pri = aindm1 * (QL(ilr, EN) - 0.5 * QL(ilr, RH) * vsq);
+            skr[j9] = sqrt(QL(ilr, RH));
+            swr[j9][0] = skr[j9] * v0;
+            swr[j9][1] = skr[j9] * v1;
+            swr[j9][2] = skr[j9] * v2;
+            swr[j9][3] = 0.5 * skr[j9] * (vsq + cp * Pri / QL(ilr, RH));
+        }
+        double Qri = 1. / QL(i9, RH);
+        double delrho = QL(i9 + nf, RH) * Qri - 1.;
+        double dele = (QL(i9 + nf, EN) - QL(i9, EN)) * Qri;
+        double dm1 = (QL(i9 + nf, ip) - QL(i9, ip)) * Qri;
+        double dm2 = (QL(i9 + nf, i1) - QL(i9, i1)) * Qri;
+        double dm3 = (QL(i9 + nf, i2) - QL(i9, i2)) * Qri;
+        double dwr[4];
+        for (int j = 0; j < 4; ++j) dwr[j] = 0.5 * (swr[1][j] + swr[0][j]);
+        double dsk = 0.5 * (skr[1] + skr[0]);
+        double vc0 = dwr[0] / dsk, vc1 = dwr[1] / dsk, vc2 = dwr[2] / dsk, hc = dwr[3] / dsk;
+        double vcsq = vc0 * vc0 + vc1 * vc1 + vc2 * vc2;
+        double asq = aindm1 * (hc - 0.5 * vcsq);
+        if (asq <= 0.0) kroe[i9] = 0;
+        double sc9 = sqrt(asq);
+        double lam[5] = {fabs(vc0 - sc9), fabs(vc0 + sc9), fabs(vc0), fabs(vc0), fabs(vc0)};
+        /* evec[row][col]: rows density, energy, parallel, perp1, perp2 */
+        double ev[5][5] = {{1., 1., 1., 0., 0.},
+                           {hc - sc9 * vc0, hc + sc9 * vc0, 0.5 * vcsq, vc1, vc2},
+                           {vc0 - sc9, vc0 + sc9, vc0, 0., 0.},
+                           {vc1, vc1, vc1, 1., 0.},
+                           {vc2, vc2, vc2, 0., 1.}};
+        double ea2i = aindm1 / asq;
+        double vcdel = vc0 * dm1 + vc1 * dm2 + vc2 * dm3 - dele;
+        double a9e = 0.5 * ea2i * (0.5 * vcsq * delrho - vcdel);
+        double sk9 = 0.5 * (dm1 - vc0 * delrho) / sc9;
+        double a9[5] = {a9e - sk9, a9e + sk9, ea2i * ((hc - vcsq) * delrho + vcdel), dm2 - vc1 * delrho, dm3 - vc2 * delrho};
+        double df[5];
+        for (int r = 0; r < 5; ++r) {
+            df[r] = 0.;
+            for (int j = 0; j < 5; ++j) df[r] = df[r] + a9[j] * lam[j] * ev[r][j];
+            df[r] = df[r] * QL(i9, RH);
+        }
+        froe[(size_t)RH * nf + i9] = 0.5 * (FL(i9, RH) + FL(i9 + nf, RH) - df[0]);
+        froe[(size_t)EN * nf + i9] = 0.5 * (FL(i9, EN) + FL(i9 + nf, EN) - df[1]);
+        froe[(size_t)ip * nf + i9] = 0.5 * (FL(i9, ip) + FL(i9 + nf, ip) - df[2]);
+        froe[(size_t)i1 * nf + i9] = 0.5 * (FL(i9, i1) + FL(i9 + nf, i1) - df[3]);
+        froe[(size_t)i2 * nf + i9] = 0.5 * (FL(i9, i2) + FL(i9 + nf, i2) - df[4]);
     }
 #undef QL
 #undef FL
@@ -800,7 +878,7 @@ static void calc_flux_dir(orc_ctx *c, const double *Q, int d) {
                 }
                 flux_calc_pnts_r(c, Qf, ff, d, nfe, noise, site);
                 for (int p = 0; p < nf; ++p) cfr[p] = 0.0;
-                if (c->p.ivis == 2) {
+                if (c->p.ivis >= 2) {   /* ivis 3: the monolith always applies LLF (ten_moment.f90:1131-1147) */
                     for (int p = 0; p < nfe; ++p) {
                         double qv[NQ];
                         for (int v = 0; v < NQ; ++v) qv[v] = Qf[v * nfe + p];
@@ -814,13 +892,22 @@ static void calc_flux_dir(orc_ctx *c, const double *Q, int d) {
                         flux[o] = 0.5 * (ff[v * nfe + p] + ff[v * nfe + p + nf]) -
                                   0.5 * cfr[p] * (Qf[v * nfe + p + nf] - Qf[v * nfe + p]);
                     }
-                if (c->p.ihllc) {
+                if (c->p.ihllc == 1) {
                     flux_hllc(c, Qf, ff, fh, d);
                     for (int v = 0; v < 5; ++v)
                         for (int p = 0; p < nf; ++p) {
                             size_t o = (size_t)p + nf * (i + (size_t)fx * (j + (size_t)fy * (k + (size_t)fz * v)));
                             flux[o] = fh[v * nf + p];
                         }
+                } else if (c->p.ihllc == 2) {
+                    int kroe[16];
+                    flux_roe(c, Qf, ff, fh, kroe, d);
+                    for (int v = 0; v < 5; ++v)
+                        for (int p = 0; p < nf; ++p)
+                            if (kroe[p] > 0) {
+                                size_t o = (size_t)p + nf * (i + (size_t)fx * (j + (size_t)fy * (k + (size_t)fz * v)));
+                                flux[o] = fh[v * nf + p];
+                            }
                 }
             }
         }
@@ -990,7 +1077,7 @@ static void glflux_assemble(orc_ctx *c) {
 static void source_calc(orc_ctx *c, const double *Q) {
     const int nx = c->nx, ny = c->ny, nz = c->nz, npg = c->npg, nb = c->nb;
     size_t n = (size_t)nx * ny * nz * NQ * nb;
-    if (c->p.ivis == 1 && c->p.body_force == 0.0) {  /* every point source is 0 in this mode */
+    if ((c->p.ivis == 1 || c->p.ivis == 3) && c->p.body_force == 0.0) {  /* every point source is 0 in this mode */
         memset(c->source_r, 0, n * sizeof(double));
         return;
     }
@@ -1010,7 +1097,7 @@ static void source_calc(orc_ctx *c, const double *Q) {
                         src[MX * npg + g] = Qin[RH] * gforce;
                         src[EN * npg + g] = Qin[MX] * gforce;
                     }
-                    if (c->p.ivis == 1) {
+                    if (c->p.ivis == 1 || c->p.ivis == 3) {
                         for (int v = PXX; v <= PYZ; ++v) src[v * npg + g] = 0;
                     } else if (c->p.ivis == 0) {
                         for (int v = PXX; v <= PYZ; ++v) src[v * npg + g] = -coll * Qin[v];
@@ -1134,7 +1221,8 @@ static void advance_time_level(orc_ctx *c, const double *Qin, double *Qout, doub
     const double *gl = c->glflux_r, *sr = c->source_r;
     double t0 = wtime();
 #define IX(v, b, e) ((e) + nc * ((v) + (size_t)NQ * (b)))
-    if (c->p.ivis == 0) {
+    if (c->p.ivis == 0 || c->p.ivis == 3) {
+        /* ivis 3: advance_time_level_gl (ten_moment.f90:795-837) with fac = 1 */
 #pragma omp parallel for
         for (long e = 0; e < (long)(nc * NQ * nb); ++e) Qout[e] = Qin[e] - dt * (gl[e] - sr[e]);
     } else if (c->p.ivis == 1) {
@@ -1176,11 +1264,57 @@ static void advance_time_level(orc_ctx *c, const double *Qin, double *Qout, doub
     c->timers[5] += wtime() - t0;
 }
 
+/* Grad closure (ivis 3), the operator-split implicit relaxation step of
+ * dg_3D_hydro_bitri_ten_moment.f90:719-793 (source_calc) and :839-892
+ * (advance_time_level_source), in place on Q.  The reference calls it with
+ * the same array as input and output (non-conforming aliasing whose result
+ * depends on the compiler); here every update reads the values before the
+ * step. */
+static void source_split(orc_ctx *c, double *Q, double dt) {
+    const int nx = c->nx, ny = c->ny, nz = c->nz, npg = c->npg, nb = c->nb;
+    const double coll = c->p.coll, oth = 1. / 3.;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                double S[6][64];
+                for (int g = 0; g < npg; ++g) {
+                    double dn = trace(c, c->bfvals_int, g, Q, i, j, k, RH), dni = 1. / dn;
+                    double vx = trace(c, c->bfvals_int, g, Q, i, j, k, MX) * dni;
+                    double vy = trace(c, c->bfvals_int, g, Q, i, j, k, MY) * dni;
+                    double vz = trace(c, c->bfvals_int, g, Q, i, j, k, MZ) * dni;
+                    double cd = coll * dn;
+                    S[0][g] = cd * (2 * vx * vx - vy * vy - vz * vz) * oth;
+                    S[1][g] = cd * (2 * vy * vy - vz * vz - vx * vx) * oth;
+                    S[2][g] = cd * (2 * vz * vz - vx * vx - vy * vy) * oth;
+                    S[3][g] = cd * vx * vy;
+                    S[4][g] = cd * vx * vz;
+                    S[5][g] = cd * vy * vz;
+                }
+                for (int b = 1; b <= nb; ++b) {
+                    double sr[6], E[6];
+                    for (int m = 0; m < 6; ++m) {
+                        double s = 0.;
+                        for (int g = 0; g < npg; ++g) s += TB(c->bval_int_wgt, g, b) * S[m][g];
+                        sr[m] = 0.125 * c->cbasis[b] * s;
+                        E[m] = Q[QI(c, i, j, k, PXX + m, b - 1)];
+                    }
+                    double den = 1. + dt * coll;
+                    double Esum = coll * dt * (E[0] + E[1] + E[2]) * oth;
+                    double Ssum = coll * (dt * dt) * (sr[0] + sr[1] + sr[2]) * oth;
+                    for (int m = 0; m < 3; ++m) Q[QI(c, i, j, k, PXX + m, b - 1)] = (E[m] + dt * sr[m] + Esum + Ssum) / den;
+                    for (int m = 3; m < 6; ++m) Q[QI(c, i, j, k, PXX + m, b - 1)] = (E[m] + dt * sr[m]) / den;
+                }
+            }
+}
+
 /* integrator.f90:93-122 euler_step */
 void orc_euler_step(orc_ctx *c, double *Qin, double *Qout, double dt) {
     if (c->p.ieos == 1 || c->p.ieos == 2) orc_limiter(c, Qin);
     calc_rhs(c, Qin);
     advance_time_level(c, Qin, Qout, dt);
+    /* ten_moment.f90:342-361: RK2 follows each advection stage by the source step */
+    if (c->p.ivis == 3 && c->p.iorder == 2) source_split(c, Qout, dt);
     c->noise_stage++;
 }
 

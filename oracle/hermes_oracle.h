@@ -32,9 +32,9 @@ enum { ORC_BC_PERIODIC = 0, ORC_BC_OUTFLOW = 1, ORC_BC_WALL = 2, ORC_BC_NOSLIP =
 typedef struct orc_params {
     int nx, ny, nz;          /* cells (input.f90 nx,ny,nz with mpi_n* = 1) */
     int nbasis, iquad;       /* (4,2) (8,2) (10,3) (27,3) */
-    int ivis;                /* 0 explicit, 1 semi-implicit stress, 2 10-moment */
+    int ivis;                /* 0 explicit, 1 semi-implicit stress, 2 10-moment, 3 Grad closure */
     int ieos;                /* 1 ideal gas, 2 Murnaghan-Tait */
-    int ihllc;               /* 1: HLLC overwrites rh..en face fluxes */
+    int ihllc;               /* 0 central/LLF, 1 HLLC (flux.f90:264-271), 2 Roe (SEAN monolith) */
     int iorder;              /* 2 Heun (RK2), 3 Shu-Osher (RK3) */
     int bc[6];               /* xlo, xhi, ylo, yhi, zlo, zhi */
     double lx, ly, lz;       /* domain lengths, domain centred at 0 */

@@ -54,10 +54,11 @@ def test_generated_tables_bit_identical(nb, nq):
     assert np.array_equal(o.table("wgt3d"), np.array(T["W3"]))
 
 
-def test_sod_converges_to_exact():
+@pytest.mark.parametrize("solver", [1, 2], ids=["hllc", "roe"])
+def test_sod_converges_to_exact(solver):
     errs = []
     for nx in (64, 128, 256):
-        cfg = config.sod_1d(nx=nx)
+        cfg = config.sod_1d(nx=nx, ihllc=solver)
         o = O.Oracle(cfg)
         Q = ic.sod(cfg)
         t = 0.0

@@ -42,6 +42,14 @@ RHS_CASES = {
     "nb4_2d_bodyforce_noslip": (config.Config(nx=6, ny=8, nz=1, nbasis=4, iquad=2, ivis=1, coll=5.0, colvis=1.0,
                                               ylobc="noslip", yhibc="noslip", body_force=0.1), 0.0),
     "nb4_x_periodic_hi_only": (config.Config(nx=6, ny=3, nz=2, nbasis=4, iquad=2, xlobc="wall", xhibc="periodic"), 0.0),
+    # Roe solver of the monolithic code (ihllc = 2)
+    "nb4_3d_roe": (config.Config(nx=5, ny=4, nz=3, nbasis=4, iquad=2, ihllc=2), 0.0),
+    "nb10_2d_roe_walls_ivis1": (config.Config(nx=6, ny=5, nz=1, nbasis=10, iquad=3, ihllc=2, ivis=1, coll=2.0,
+                                              colvis=1.0, xlobc="wall", xhibc="wall"), 0.5),
+    "nb8_3d_central_only": (config.Config(nx=4, ny=4, nz=3, nbasis=8, iquad=2, ihllc=0), 0.0),
+    # Grad closure (ivis 3, E_ij form)
+    "nb4_3d_grad": (config.Config(nx=5, ny=4, nz=3, nbasis=4, iquad=2, ivis=3, coll=1.5), 1.0),
+    "nb10_2d_grad_roe": (config.Config(nx=5, ny=6, nz=1, nbasis=10, iquad=3, ivis=3, coll=0.5, ihllc=2), 1.0),
 }
 
 
@@ -49,7 +57,7 @@ RHS_CASES = {
 def test_rhs_parity(name):
     cfg, stress = RHS_CASES[name]
     Q = ic.random_smooth(cfg, seed=7, amp=0.1, stress_amp=0.05 * stress)
-    if cfg.ivis == 2:
+    if cfg.ivis >= 2:
         Q = ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.01)
     o = _oracle(cfg)
     Qo = Q.copy(order="F")
@@ -105,6 +113,11 @@ STEP_CASES = {
                                                    xlobc="wall", xhibc="noslip", zlobc="outflow", zhibc="wall"),
                              lambda c: ic.random_smooth(c, seed=5, amp=0.05, stress_amp=0.01)),
     "fh_noise_8_rk2_nb4": (lambda: config.fh_box(8, precision="fp64", seed=42), lambda c: ic.equilibrium(c)),
+    "sod_256_rk2_roe": (lambda: config.sod_1d(nx=256, ihllc=2), lambda c: ic.sod(c)),
+    "grad_rk2_split_source_nb4": (lambda: config.Config(nx=6, ny=5, nz=4, nbasis=4, iquad=2, ivis=3, coll=2.0, iorder=2),
+                                  lambda c: ic.ten_moment_stress(c, ic.random_smooth(c, seed=9, amp=0.05), p=1.0, amp=0.01)),
+    "grad_rk3_nb10": (lambda: config.Config(nx=8, ny=8, nz=1, nbasis=10, iquad=3, ivis=3, coll=1.0, iorder=3),
+                      lambda c: ic.ten_moment_stress(c, ic.random_smooth(c, seed=2, amp=0.05), p=1.0, amp=0.01)),
 }
 
 
