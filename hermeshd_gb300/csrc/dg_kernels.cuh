@@ -23,7 +23,7 @@ namespace hermes {
 
 constexpr int LIMIT_TPB = 128;
 constexpr int FACE_TPB = 128;
-constexpr int CELL_TPB = 64;
+constexpr int CELL_CPB = 32;   // cells per block of k_cell (two threads per cell)
 constexpr int DT_TPB = 256;
 
 // stage combination of integrator.f90:62-86
@@ -254,7 +254,7 @@ struct FaceArgs {
     unsigned stage;
 };
 
-template <class T, class TB, int DIR, int P>
+template <class T, class TB, int DIR, int P, bool NOISE>
 __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restrict__ flux, const FaceArgs& a, long long gf) {
     const Geom& G = a.G;
     const Phys& ph = a.ph;
@@ -329,18 +329,16 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
     }
     // point fluxes of both sides (flux.f90:240), stochastic stress per side
     T SL[6] = {T(0), T(0), T(0), T(0), T(0), T(0)}, SR[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-    if (ph.llns) {
+    if constexpr (NOISE) {
         NoiseCtr nc_{*a.step, a.stage};
         random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P, SL);
         random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P + TB::NF, SR);
     }
     T fL[NQ], fR[NQ], F[NQ];
-    {
-        Prim<T> wL = primitives(ph, qL);
-        point_flux<T, DIR>(ph, qL, wL, SL, fL);
-        Prim<T> wR = primitives(ph, qR);
-        point_flux<T, DIR>(ph, qR, wR, SR, fR);
-    }
+    const Prim<T> wL = primitives(ph, qL);
+    point_flux<T, DIR>(ph, qL, wL, SL, fL);
+    const Prim<T> wR = primitives(ph, qR);
+    point_flux<T, DIR>(ph, qR, wR, SR, fR);
     // flux.f90:243-262: central flux, LLF with the freezing speed for ivis 2
     if (ph.ivis >= 2) {   // ivis 3: the Grad-closure code always applies LLF (ten_moment.f90:1131-1147)
         const T cfr = fmax(cfcal<T, DIR>(ph, qL), cfcal<T, DIR>(ph, qR));
@@ -366,7 +364,7 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
             else rlast = trace_var<TB, DIR, 1, TB::NF - 1, RH>(Qb, nc, cell_at(n - 1));
             rho_i_last = T(1) / rlast;
         }
-        hllc<T, DIR>(ph, qL, qR, fL, fR, rho_i_last, F);
+        hllc<T, DIR>(ph, qL, qR, fL, fR, wL.dni, wR.dni, rho_i_last, F);
     }
     // store, scaled by the inverse spacing of this direction
     const T sc = T(B.di[DIR]);
@@ -376,20 +374,27 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
     for (int v = 0; v < NQ; ++v) fb[(long long)(v * TB::NF + P) * nfd + lf] = F[v] * sc;
 }
 
-template <class T, class TB, int DIR>
-__global__ void __launch_bounds__(FACE_TPB) k_face(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
+template <class T, class TB, int DIR, bool NOISE>
+__global__ void __launch_bounds__(FACE_TPB, 4) k_face(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
     long long gf = (long long)blockIdx.x * FACE_TPB + threadIdx.x;
     if (gf >= a.G.nface[DIR]) return;
     const int p = blockIdx.y;
     sfor<TB::NF>([&](auto pp) {
         constexpr int P = decltype(pp)::value;
-        if (p == P) face_point<T, TB, DIR, P>(Q, flux, a, gf);
+        if (p == P) face_point<T, TB, DIR, P, NOISE>(Q, flux, a, gf);
     });
 }
 
 // ===========================================================================
-// k_cell: one thread per cell; the cell's coefficients and volume
-// accumulators live in the thread's own column of shared memory.
+// k_cell: two threads per cell.  In a block of 2*CELL_CPB threads, thread
+// c < CELL_CPB owns the hydro variables rh..en of cell c and thread
+// CELL_CPB + c owns the six stress variables of the same cell.  The cell's
+// coefficients are shared through one shared-memory column per cell; each
+// thread keeps the volume-quadrature accumulators of its own variables in
+// registers.  The stress thread re-evaluates rho and the momenta at the
+// quadrature points (its fluxes need the velocity), a few per cent of the
+// cell's FP64 work, in exchange for twice the threads and no accumulator
+// traffic through shared memory.
 // ===========================================================================
 struct CellArgs {
     Geom G;
@@ -402,169 +407,160 @@ struct CellArgs {
     int split_source;   // Grad closure with RK2: the implicit source step after the update
 };
 
-template <class T, class TB>
-__global__ void __launch_bounds__(CELL_TPB) k_cell(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux, CellArgs a) {
-    // Qin, Q0 and out may alias (the RK stages write in place); each thread
-    // reads its own cell's elements before writing them.
-    constexpr int NB = TB::NB, NF = TB::NF, NPG = TB::NPG;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* qs = reinterpret_cast<T*>(smem_raw);           // [NB*NQ][CELL_TPB]
-    T* acc = qs + NB * NQ * CELL_TPB;                  // [NB*NQ][CELL_TPB]
-    const int tid = threadIdx.x;
-    const long long gc = (long long)blockIdx.x * CELL_TPB + tid;
-    if (gc >= a.G.ncell) return;
-    const Phys& ph = a.ph;
-    const int bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
-    const Box& B = a.G.boxes[bx];
-    const long long le = gc - B.cell0, nc = B.ncell;
-    const T* Qb = Qin + B.q0;
-#define QS(b, v) qs[((b) * NQ + (v)) * CELL_TPB + tid]
-#define ACC(b, v) acc[((b) * NQ + (v)) * CELL_TPB + tid]
-#pragma unroll
-    for (int bv = 0; bv < NB * NQ; ++bv) {
-        qs[bv * CELL_TPB + tid] = Qb[(long long)bv * nc + le];
-        acc[bv * CELL_TPB + tid] = T(0);
-    }
-    const T di[3] = {T(B.di[0]), T(B.di[1]), T(B.di[2])};
-    const bool noise = ph.llns != 0;
-    const NoiseCtr nctr{noise ? *a.step : 0ull, a.stage};
-    const bool src_lin = (ph.ivis == 0), src_tenm = (ph.ivis == 2), src_bf = (ph.body_force != 0.0);
+// RK combination of integrator.f90:62-86
+template <class T>
+__device__ __forceinline__ T rk_combine(int comb, T q0, T e) {
+    if (comb == COMB_HALF) return T(0.5) * (q0 + e);                         // integrator.f90:70
+    if (comb == COMB_34) return T(0.75) * q0 + T(0.25) * e;                  // integrator.f90:82
+    return T(1.0 / 3.0) * q0 + T(2.0 / 3.0) * e;                            // integrator.f90:85
+}
 
-    // ---- volume quadrature and point sources (flux.f90:751-928, sources.f90:28-78)
-    sfor<NPG>([&](auto gg) {
+// what the phases of one cell share
+template <class T>
+struct CellCtx {
+    const T* qs_base;
+    T* qs;            // shared column base of this block
+    int lc;           // cell slot in the block
+    bool act;
+    int bx;
+    long long le, nc;
+    const Box* B;
+    T di[3];
+    NoiseCtr nctr;
+    bool noise;
+    T dt, faci;
+    T* ob;
+    const T* q0b;
+    long long fm[3], fp[3], nfd[3];
+    bool bad;
+};
+
+// phase 1: volume quadrature and point sources of one group's variables
+// (flux.f90:751-928, sources.f90:28-78); acc collects volume + source
+template <class T, class TB, int GRP, bool NOISE>
+__device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T (&acc)[6][TB::NB]) {
+    constexpr int NB = TB::NB, NPG = TB::NPG;
+    constexpr int GV0 = GRP == 0 ? 0 : PXX;
+    constexpr int GNV = GRP == 0 ? 5 : 6;
+    const Phys& ph = a.ph;
+    // coefficients are re-read from shared memory at every point: held in
+    // registers across the point loop they would cost ~NB*NQ registers
+    const volatile T* qs = cx.qs;
+    const int lc = cx.lc;
+    // the stress thread needs the stress values at the points for the
+    // 10-moment fluxes (ivis 2, 3) and the ivis-0 source; ivis 1 needs only
+    // the velocity
+    const bool need_all = GRP == 0 || ph.ivis != 1;
+    sfor_seq<NPG>([&](auto gg) {
         constexpr int g = decltype(gg)::value;
         T u[NQ];
         sfor<NQ>([&](auto vv) {
             constexpr int v = decltype(vv)::value;
-            T s = T(0);
-            sfor<NB>([&](auto bb) {
-                constexpr int b = decltype(bb)::value;
-                constexpr double c = TB::INT(g, b);
-                if constexpr (c != 0.0) s = fma(T(c), QS(b, v), s);
-            });
-            u[v] = s;
+            if (v <= MZ || need_all) {
+                T s = T(0);
+                sfor<NB>([&](auto bb) {
+                    constexpr int b = decltype(bb)::value;
+                    constexpr double c = TB::INT(g, b);
+                    if constexpr (c != 0.0) s = fma(T(c), qs[(b * NQ + v) * CELL_CPB + lc], s);
+                });
+                u[v] = s;
+            } else {
+                u[v] = T(0);
+            }
         });
         const Prim<T> w = primitives(ph, u);
         sfor<3>([&](auto dd) {
             constexpr int d = decltype(dd)::value;
             T S[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-            if (noise) random_stress<T>(ph, B.seed, nctr, 3 + d, (unsigned long long)le, g, S);
+            if constexpr (GRP == 0 && NOISE) random_stress<T>(ph, cx.B->seed, cx.nctr, 3 + d, (unsigned long long)cx.le, g, S);
             T f[NQ];
             point_flux<T, d>(ph, u, w, S, f);
-#pragma unroll
-            for (int v = 0; v < NQ; ++v) f[v] *= di[d];
+            T fs[GNV];
+            sfor<GNV>([&](auto mm) { fs[decltype(mm)::value] = f[GV0 + decltype(mm)::value] * cx.di[d]; });
             sfor<NB>([&](auto bb) {
                 constexpr int b = decltype(bb)::value;
                 constexpr double c = vtab<TB, d>(g, b);
                 if constexpr (c != 0.0) {
-#pragma unroll
-                    for (int v = 0; v < NQ; ++v) ACC(b, v) = fma(T(c), f[v], ACC(b, v));
+                    sfor<GNV>([&](auto mm) {
+                        constexpr int m = decltype(mm)::value;
+                        acc[m][b] = fma(T(c), fs[m], acc[m][b]);
+                    });
                 }
             });
         });
-        if (src_lin || src_tenm || src_bf) {
-            T s[NQ];
-#pragma unroll
-            for (int v = 0; v < NQ; ++v) s[v] = T(0);
-            if (src_bf) {   // body force (no reference counterpart)
+        T s[GNV];
+        bool any = false;
+        sfor<GNV>([&](auto mm) { s[decltype(mm)::value] = T(0); });
+        if (GRP == 0) {
+            if (ph.body_force != 0.0) {   // body force (no reference counterpart)
                 s[MX] = u[RH] * T(ph.body_force);
                 s[EN] = u[MX] * T(ph.body_force);
+                any = true;
             }
-            if (src_lin) {  // sources.f90:37-43
-                const T coll = T(ph.coll);
-#pragma unroll
-                for (int v = PXX; v <= PYZ; ++v) s[v] = -coll * u[v];
-            } else if (src_tenm) {  // sources.f90:51-69
-                const T vx2 = w.vx * w.vx, vy2 = w.vy * w.vy, vz2 = w.vz * w.vz;
-                const T colldn = T(ph.coll) * w.dn, c1d3 = T(1.0 / 3.0);
-                s[PXX] = colldn * (T(2) * vx2 - vy2 - vz2) * c1d3;
-                s[PYY] = colldn * (T(2) * vy2 - vz2 - vx2) * c1d3;
-                s[PZZ] = colldn * (T(2) * vz2 - vx2 - vy2) * c1d3;
-                s[PXY] = colldn * w.vx * w.vy;
-                s[PXZ] = colldn * w.vx * w.vz;
-                s[PYZ] = colldn * w.vy * w.vz;
-            }
+        } else if (ph.ivis == 0) {        // sources.f90:37-43
+            sfor<6>([&](auto mm) { s[decltype(mm)::value] = -T(ph.coll) * u[PXX + decltype(mm)::value]; });
+            any = true;
+        } else if (ph.ivis == 2) {        // sources.f90:51-69
+            const T vx2 = w.vx * w.vx, vy2 = w.vy * w.vy, vz2 = w.vz * w.vz;
+            const T colldn = T(ph.coll) * w.dn, c1d3 = T(1.0 / 3.0);
+            s[0] = colldn * (T(2) * vx2 - vy2 - vz2) * c1d3;
+            s[1] = colldn * (T(2) * vy2 - vz2 - vx2) * c1d3;
+            s[2] = colldn * (T(2) * vz2 - vx2 - vy2) * c1d3;
+            s[3] = colldn * w.vx * w.vy;
+            s[4] = colldn * w.vx * w.vz;
+            s[5] = colldn * w.vy * w.vz;
+            any = true;
+        }
+        if (any) {
             sfor<NB>([&](auto bb) {
                 constexpr int b = decltype(bb)::value;
                 constexpr double c = TB::SRC(g, b);
                 if constexpr (c != 0.0) {
-                    if (src_bf) {
-                        ACC(b, MX) = fma(T(c), s[MX], ACC(b, MX));
-                        ACC(b, EN) = fma(T(c), s[EN], ACC(b, EN));
-                    }
-                    if (src_lin || src_tenm) {
-#pragma unroll
-                        for (int v = PXX; v <= PYZ; ++v) ACC(b, v) = fma(T(c), s[v], ACC(b, v));
-                    }
+                    sfor<GNV>([&](auto mm) {
+                        constexpr int m = decltype(mm)::value;
+                        acc[m][b] = fma(T(c), s[m], acc[m][b]);
+                    });
                 }
             });
         }
     });
+}
 
-    // ---- surface assembly, update and RK combination, one variable at a time
-    const int n0 = B.n[0], n1 = B.n[1];
-    const int ci = (int)(le % n0), cj = (int)((le / n0) % n1), ck = (int)(le / ((long long)n0 * n1));
-    long long fm[3], fp[3], nfd[3];
-    {
-        const int c[3] = {ci, cj, ck};
-        for (int d = 0; d < 3; ++d) {
-            int e0 = d == 0 ? B.nfp[0] : B.n[0], e1 = d == 1 ? B.nfp[1] : B.n[1], e2 = d == 2 ? B.nfp[2] : B.n[2];
-            nfd[d] = (long long)e0 * e1 * e2;
-            int hi = c[d] + 1;
-            if (B.nfp[d] == B.n[d] && hi == B.n[d]) hi = 0;
-            int lo = c[d];
-            int a0 = d == 0 ? lo : ci, a1 = d == 1 ? lo : cj, a2 = d == 2 ? lo : ck;
-            fm[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
-            a0 = d == 0 ? hi : ci; a1 = d == 1 ? hi : cj; a2 = d == 2 ? hi : ck;
-            fp[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
-        }
-    }
-    const T dt = T(a.st[bx].dt);
-    const T faci = T(1) / (T(1) + dt * T(ph.coll));
-    T* ob = out + B.q0;
-    const T* q0b = Q0 ? Q0 + B.q0 : nullptr;
-    bool bad = false;
-    T rs[3][NB];   // rhs of pxx, pyy, pzz, kept for the coupled ivis-2 update
+template <class T>
+__device__ __forceinline__ void cell_store(const CellArgs& a, CellCtx<T>& cx, int grp, int v, int b, T e) {
+    const bool stash = a.split_source != 0;
+    if (stash) cx.qs[(b * NQ + v) * CELL_CPB + cx.lc] = e;   // the split source step reads them
+    if (grp == 1 && stash) return;                          // stress: stored after the source step
+    T o = e;
+    if (a.comb != COMB_NONE) o = rk_combine(a.comb, cx.q0b[(long long)(b * NQ + v) * cx.nc + cx.le], o);
+    if (b == 0 && o != o) cx.bad = true;
+    cx.ob[(long long)(b * NQ + v) * cx.nc + cx.le] = o;
+}
 
-    auto finish = [&](int v, const T* r) {
-        // r[b] = glflux - source of variable v
-        if (a.mode == MODE_RHS) {
-#pragma unroll
-            for (int b = 0; b < NB; ++b) ob[(long long)(b * NQ + v) * nc + le] = r[b];
-            return;
-        }
-#pragma unroll
-        for (int b = 0; b < NB; ++b) {
-            T e = QS(b, v) - dt * r[b];                    // integrator.f90:147-149,171-173
-            if ((ph.ivis == 1 || ph.ivis == 2) && v >= PXX) e = faci * e;   // integrator.f90:174,220-224
-            if (a.split_source) {                          // combined after the source step below
-                QS(b, v) = e;
-                continue;
-            }
-            T o = e;
-            if (a.comb != COMB_NONE) {
-                const T q0 = q0b[(long long)(b * NQ + v) * nc + le];
-                if (a.comb == COMB_HALF) o = T(0.5) * (q0 + e);                           // integrator.f90:70
-                else if (a.comb == COMB_34) o = T(0.75) * q0 + T(0.25) * e;               // integrator.f90:82
-                else o = T(1.0 / 3.0) * q0 + T(2.0 / 3.0) * e;                            // integrator.f90:85
-            }
-            if (b == 0 && o != o) bad = true;
-            ob[(long long)(b * NQ + v) * nc + le] = o;
-        }
-    };
-
-    sfor<NQ>([&](auto vv) {
-        constexpr int v = decltype(vv)::value;
+// phase 2: surface assembly (flux.f90:958-978), update and RK combination,
+// one variable at a time
+template <class T, class TB, int GRP>
+__device__ __forceinline__ void cell_surface_update(const CellArgs& a, CellCtx<T>& cx, const T* __restrict__ flux,
+                                                    T (&acc)[6][TB::NB]) {
+    constexpr int NB = TB::NB, NF = TB::NF;
+    constexpr int GV0 = GRP == 0 ? 0 : PXX;
+    constexpr int GNV = GRP == 0 ? 5 : 6;
+    const Phys& ph = a.ph;
+    T* qs = cx.qs;
+    const int lc = cx.lc;
+    const T dt = cx.dt, faci = cx.faci;
+    sfor_seq<GNV>([&](auto mm) {
+        constexpr int m = decltype(mm)::value;
+        constexpr int v = GV0 + m;
         T r[NB];
-#pragma unroll
-        for (int b = 0; b < NB; ++b) r[b] = -ACC(b, v);
+        sfor<NB>([&](auto bb) { r[decltype(bb)::value] = -acc[m][decltype(bb)::value]; });
         sfor<3>([&](auto dd) {
             constexpr int d = decltype(dd)::value;
-            const T* fb = flux + a.G.boxes[bx].fbase[d] + (long long)v * NF * nfd[d];
+            const T* fb = flux + cx.B->fbase[d] + (long long)v * NF * cx.nfd[d];
             sfor<NF>([&](auto pp) {
                 constexpr int p = decltype(pp)::value;
-                const T Fp = __ldg(fb + (long long)p * nfd[d] + fp[d]);
-                const T Fm = __ldg(fb + (long long)p * nfd[d] + fm[d]);
+                const T Fp = __ldg(fb + (long long)p * cx.nfd[d] + cx.fp[d]);
+                const T Fm = __ldg(fb + (long long)p * cx.nfd[d] + cx.fm[d]);
                 sfor<NB>([&](auto bb) {
                     constexpr int b = decltype(bb)::value;
                     constexpr double cp = stab<TB, d, 1>(p, b);
@@ -574,115 +570,194 @@ __global__ void __launch_bounds__(CELL_TPB) k_cell(const T* Qin, const T* Q0, T*
                 });
             });
         });
-        if constexpr (v >= PXX && v <= PZZ) {
-#pragma unroll
-            for (int b = 0; b < NB; ++b) rs[v - PXX][b] = r[b];
-            if constexpr (v == PZZ) {
-                if (ph.ivis == 2 && a.mode == MODE_STAGE) {
-                    // integrator.f90:207-218: trace-coupled semi-implicit update
-                    const T coll = T(ph.coll), c1d3 = T(1.0 / 3.0);
-#pragma unroll
-                    for (int b = 0; b < NB; ++b) {
-                        const T Q_sum = coll * dt * (QS(b, PXX) + QS(b, PYY) + QS(b, PZZ)) * c1d3;
-                        const T R_sum = coll * (dt * dt) * (rs[0][b] + rs[1][b] + rs[2][b]) * c1d3;
-                        T e3[3];
-#pragma unroll
-                        for (int m = 0; m < 3; ++m) e3[m] = faci * (QS(b, PXX + m) - dt * rs[m][b] + Q_sum - R_sum);
-#pragma unroll
-                        for (int m = 0; m < 3; ++m) {
-                            T o = e3[m];
-                            if (a.comb != COMB_NONE) {
-                                const T q0 = q0b[(long long)(b * NQ + PXX + m) * nc + le];
-                                if (a.comb == COMB_HALF) o = T(0.5) * (q0 + e3[m]);
-                                else if (a.comb == COMB_34) o = T(0.75) * q0 + T(0.25) * e3[m];
-                                else o = T(1.0 / 3.0) * q0 + T(2.0 / 3.0) * e3[m];
-                            }
-                            if (b == 0 && o != o) bad = true;
-                            ob[(long long)(b * NQ + PXX + m) * nc + le] = o;
-                        }
-                    }
-                } else {
-                    finish(PXX, rs[0]);
-                    finish(PYY, rs[1]);
-                    finish(PZZ, rs[2]);
-                }
-            }
-        } else {
-            finish(v, r);
-        }
-    });
-    if (a.split_source) {
-        // Grad closure: implicit relaxation of E_ij with the sources of the
-        // advected state (ten_moment.f90:719-793 source_calc, :839-892
-        // advance_time_level_source), then the RK combination and the store.
-#pragma unroll
-        for (int b = 0; b < NB; ++b)
-#pragma unroll
-            for (int m = 0; m < 6; ++m) ACC(b, PXX + m) = T(0);
-        const T coll = T(ph.coll), oth = T(1.0 / 3.0);
-        sfor<NPG>([&](auto gg) {
-            constexpr int g = decltype(gg)::value;
-            T u[4];
-            sfor<4>([&](auto vv) {
-                constexpr int v = decltype(vv)::value;
-                T s = T(0);
-                sfor<NB>([&](auto bb) {
-                    constexpr int b = decltype(bb)::value;
-                    constexpr double c = TB::INT(g, b);
-                    if constexpr (c != 0.0) s = fma(T(c), QS(b, v), s);
-                });
-                u[v] = s;
-            });
-            const T dni = T(1) / u[RH];
-            const T vx = u[MX] * dni, vy = u[MY] * dni, vz = u[MZ] * dni, cd = coll * u[RH];
-            T S[6];
-            S[0] = cd * (T(2) * vx * vx - vy * vy - vz * vz) * oth;
-            S[1] = cd * (T(2) * vy * vy - vz * vz - vx * vx) * oth;
-            S[2] = cd * (T(2) * vz * vz - vx * vx - vy * vy) * oth;
-            S[3] = cd * vx * vy;
-            S[4] = cd * vx * vz;
-            S[5] = cd * vy * vz;
+        // r[b] = glflux - source of variable v
+        if (a.mode == MODE_RHS) {
             sfor<NB>([&](auto bb) {
                 constexpr int b = decltype(bb)::value;
-                constexpr double c = TB::SRC(g, b);
-                if constexpr (c != 0.0) {
-#pragma unroll
-                    for (int m = 0; m < 6; ++m) ACC(b, PXX + m) = fma(T(c), S[m], ACC(b, PXX + m));
-                }
+                cx.ob[(long long)(b * NQ + v) * cx.nc + cx.le] = r[b];
             });
-        });
-        const T den = T(1) + dt * coll;
-#pragma unroll
-        for (int b = 0; b < NB; ++b) {
-            T E[6];
-#pragma unroll
-            for (int m = 0; m < 6; ++m) E[m] = QS(b, PXX + m);
-            const T Esum = coll * dt * (E[0] + E[1] + E[2]) * oth;
-            const T Ssum = coll * (dt * dt) * (ACC(b, PXX) + ACC(b, PYY) + ACC(b, PZZ)) * oth;
-#pragma unroll
-            for (int m = 0; m < 3; ++m) QS(b, PXX + m) = (E[m] + dt * ACC(b, PXX + m) + Esum + Ssum) / den;
-#pragma unroll
-            for (int m = 3; m < 6; ++m) QS(b, PXX + m) = (E[m] + dt * ACC(b, PXX + m)) / den;
+            return;
         }
-#pragma unroll
-        for (int v = 0; v < NQ; ++v)
-#pragma unroll
-            for (int b = 0; b < NB; ++b) {
-                const T e = QS(b, v);
-                T o = e;
-                if (a.comb != COMB_NONE) {
-                    const T q0 = q0b[(long long)(b * NQ + v) * nc + le];
-                    if (a.comb == COMB_HALF) o = T(0.5) * (q0 + e);
-                    else if (a.comb == COMB_34) o = T(0.75) * q0 + T(0.25) * e;
-                    else o = T(1.0 / 3.0) * q0 + T(2.0 / 3.0) * e;
+        if constexpr (GRP == 1 && m < 3) {
+            if (ph.ivis == 2) {
+                // keep R of pxx, pyy, pzz in the accumulator rows (no longer needed)
+                sfor<NB>([&](auto bb) { acc[m][decltype(bb)::value] = r[decltype(bb)::value]; });
+                if constexpr (m == 2) {
+                    // integrator.f90:207-218: trace-coupled semi-implicit update
+                    const T coll = T(ph.coll), c1d3 = T(1.0 / 3.0);
+                    sfor<NB>([&](auto bb) {
+                        constexpr int b = decltype(bb)::value;
+                        const T q0 = qs[(b * NQ + PXX) * CELL_CPB + lc], q1 = qs[(b * NQ + PYY) * CELL_CPB + lc];
+                        const T q2 = qs[(b * NQ + PZZ) * CELL_CPB + lc];
+                        const T Q_sum = coll * dt * (q0 + q1 + q2) * c1d3;
+                        const T R_sum = coll * (dt * dt) * (acc[0][b] + acc[1][b] + acc[2][b]) * c1d3;
+                        const T e0 = faci * (q0 - dt * acc[0][b] + Q_sum - R_sum);
+                        const T e1 = faci * (q1 - dt * acc[1][b] + Q_sum - R_sum);
+                        const T e2 = faci * (q2 - dt * acc[2][b] + Q_sum - R_sum);
+                        cell_store(a, cx, GRP, PXX, b, e0);
+                        cell_store(a, cx, GRP, PYY, b, e1);
+                        cell_store(a, cx, GRP, PZZ, b, e2);
+                    });
                 }
-                if (b == 0 && o != o) bad = true;
-                ob[(long long)(b * NQ + v) * nc + le] = o;
+                return;
             }
+        }
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            T e = qs[(b * NQ + v) * CELL_CPB + lc] - dt * r[b];     // integrator.f90:147-149,171-173
+            if (GRP == 1 && (ph.ivis == 1 || ph.ivis == 2)) e = faci * e;   // :174,220-224
+            cell_store(a, cx, GRP, v, b, e);
+        });
+    });
+}
+
+// phase 3 (Grad closure with RK2): implicit relaxation of E_ij with the
+// sources of the advected state (ten_moment.f90:719-793 source_calc,
+// :839-892 advance_time_level_source), then the RK combination and the store
+template <class T, class TB>
+__device__ __forceinline__ void cell_split_source(const CellArgs& a, CellCtx<T>& cx) {
+    constexpr int NB = TB::NB, NPG = TB::NPG;
+    const Phys& ph = a.ph;
+    const volatile T* qs = cx.qs;
+    const int lc = cx.lc;
+    const T dt = cx.dt;
+    T src[6][NB];
+    sfor<6>([&](auto mm) { sfor<NB>([&](auto bb) { src[decltype(mm)::value][decltype(bb)::value] = T(0); }); });
+    const T coll = T(ph.coll), oth = T(1.0 / 3.0);
+    sfor_seq<NPG>([&](auto gg) {
+        constexpr int g = decltype(gg)::value;
+        T u[4];
+        sfor<4>([&](auto vv) {
+            constexpr int v = decltype(vv)::value;
+            T s = T(0);
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr double c = TB::INT(g, b);
+                if constexpr (c != 0.0) s = fma(T(c), qs[(b * NQ + v) * CELL_CPB + lc], s);
+            });
+            u[v] = s;
+        });
+        const T dni = T(1) / u[RH];
+        const T vx = u[MX] * dni, vy = u[MY] * dni, vz = u[MZ] * dni, cd = coll * u[RH];
+        T S[6];
+        S[0] = cd * (T(2) * vx * vx - vy * vy - vz * vz) * oth;
+        S[1] = cd * (T(2) * vy * vy - vz * vz - vx * vx) * oth;
+        S[2] = cd * (T(2) * vz * vz - vx * vx - vy * vy) * oth;
+        S[3] = cd * vx * vy;
+        S[4] = cd * vx * vz;
+        S[5] = cd * vy * vz;
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            constexpr double c = TB::SRC(g, b);
+            if constexpr (c != 0.0) {
+                sfor<6>([&](auto mm) {
+                    constexpr int m = decltype(mm)::value;
+                    src[m][b] = fma(T(c), S[m], src[m][b]);
+                });
+            }
+        });
+    });
+    const T den = T(1) + dt * coll;
+    sfor<NB>([&](auto bb) {
+        constexpr int b = decltype(bb)::value;
+        T E[6];
+        sfor<6>([&](auto mm) { E[decltype(mm)::value] = qs[(b * NQ + PXX + decltype(mm)::value) * CELL_CPB + lc]; });
+        const T Esum = coll * dt * (E[0] + E[1] + E[2]) * oth;
+        const T Ssum = coll * (dt * dt) * (src[0][b] + src[1][b] + src[2][b]) * oth;
+        sfor<6>([&](auto mm) {
+            constexpr int m = decltype(mm)::value;
+            const int v = PXX + m;
+            T o = m < 3 ? (E[m] + dt * src[m][b] + Esum + Ssum) / den : (E[m] + dt * src[m][b]) / den;
+            if (a.comb != COMB_NONE) o = rk_combine(a.comb, cx.q0b[(long long)(b * NQ + v) * cx.nc + cx.le], o);
+            if (b == 0 && o != o) cx.bad = true;
+            cx.ob[(long long)(b * NQ + v) * cx.nc + cx.le] = o;
+        });
+    });
+}
+
+// resident blocks per SM the register allocation must allow: FP32 fits 16
+// warps per SM in 128 registers; FP64 trades occupancy for the accumulator
+// rows of the larger bases
+template <class T, int NB>
+struct CellMinBlocks {
+    static constexpr int value = std::is_same<T, float>::value ? (NB <= 4 ? 8 : NB <= 8 ? 6 : 5)
+                                                               : (NB <= 4 ? 6 : NB <= 8 ? 5 : 4);
+};
+
+template <class T, class TB, bool NOISE>
+__global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value))
+    k_cell(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux, CellArgs a) {
+    // Qin, Q0 and out may alias (the RK stages write in place); every element
+    // is read before the thread that owns it writes it.
+    constexpr int NB = TB::NB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int tid = threadIdx.x;
+    const int grp = tid / CELL_CPB;                   // 0 hydro, 1 stress (warp-uniform)
+    CellCtx<T> cx;
+    cx.qs = reinterpret_cast<T*>(smem_raw);           // [NB*NQ][CELL_CPB]
+    cx.lc = tid % CELL_CPB;
+    const long long gc = (long long)blockIdx.x * CELL_CPB + cx.lc;
+    cx.act = gc < a.G.ncell;
+    cx.bx = 0; cx.le = 0; cx.nc = 1;
+    if (cx.act) {
+        cx.bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
+        cx.le = gc - a.G.boxes[cx.bx].cell0;
+        cx.nc = a.G.boxes[cx.bx].ncell;
     }
-    if (bad) a.flags[0] |= FLAG_NONFINITE;   // integrator.f90:234-250 (the reference exits)
-#undef QS
-#undef ACC
+    cx.B = &a.G.boxes[cx.bx];
+    const Box& B = *cx.B;
+    // ---- phase 0: each thread loads its own variables of its cell
+    if (cx.act) {
+        const T* Qb = Qin + B.q0;
+        const int v0 = grp == 0 ? 0 : PXX, v1 = grp == 0 ? PXX : NQ;
+        for (int v = v0; v < v1; ++v)
+#pragma unroll
+            for (int b = 0; b < NB; ++b) cx.qs[(b * NQ + v) * CELL_CPB + cx.lc] = Qb[(long long)(b * NQ + v) * cx.nc + cx.le];
+    }
+    for (int d = 0; d < 3; ++d) cx.di[d] = T(B.di[d]);
+    cx.noise = a.ph.llns != 0;
+    cx.nctr = NoiseCtr{cx.noise ? *a.step : 0ull, a.stage};
+    cx.dt = cx.act ? T(a.st[cx.bx].dt) : T(0);
+    cx.faci = T(1) / (T(1) + cx.dt * T(a.ph.coll));
+    cx.ob = out + B.q0;
+    cx.q0b = Q0 ? Q0 + B.q0 : nullptr;
+    cx.bad = false;
+    for (int d = 0; d < 3; ++d) { cx.fm[d] = 0; cx.fp[d] = 0; cx.nfd[d] = 1; }
+    if (cx.act) {
+        const int n0 = B.n[0], n1 = B.n[1];
+        const int c[3] = {(int)(cx.le % n0), (int)((cx.le / n0) % n1), (int)(cx.le / ((long long)n0 * n1))};
+        for (int d = 0; d < 3; ++d) {
+            const int e0 = d == 0 ? B.nfp[0] : B.n[0], e1 = d == 1 ? B.nfp[1] : B.n[1], e2 = d == 2 ? B.nfp[2] : B.n[2];
+            cx.nfd[d] = (long long)e0 * e1 * e2;
+            int hi = c[d] + 1;
+            if (B.nfp[d] == B.n[d] && hi == B.n[d]) hi = 0;
+            int a0 = d == 0 ? c[d] : c[0], a1 = d == 1 ? c[d] : c[1], a2 = d == 2 ? c[d] : c[2];
+            cx.fm[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
+            a0 = d == 0 ? hi : c[0]; a1 = d == 1 ? hi : c[1]; a2 = d == 2 ? hi : c[2];
+            cx.fp[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
+        }
+    }
+    __syncthreads();
+
+    T acc[6][NB];
+#pragma unroll
+    for (int m = 0; m < 6; ++m)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) acc[m][b] = T(0);
+    if (cx.act) {
+        if (grp == 0) cell_volume<T, TB, 0, NOISE>(a, cx, acc);
+        else cell_volume<T, TB, 1, NOISE>(a, cx, acc);
+    }
+    __syncthreads();   // every read of the other group's coefficients is done
+    if (cx.act) {
+        if (grp == 0) cell_surface_update<T, TB, 0>(a, cx, flux, acc);
+        else cell_surface_update<T, TB, 1>(a, cx, flux, acc);
+    }
+    if (a.split_source) {
+        __syncthreads();   // the hydro thread's updated rho and momenta are in the column
+        if (grp == 1 && cx.act) cell_split_source<T, TB>(a, cx);
+    }
+    if (cx.bad) a.flags[0] |= FLAG_NONFINITE;   // integrator.f90:234-250 (the reference exits)
 }
 
 // ===========================================================================

@@ -222,16 +222,15 @@ __device__ __forceinline__ T cfcal(const Phys& ph, const T q[NQ]) {
 // ---------------------------------------------------------------------------
 template <class T, int DIR>
 __device__ __forceinline__ void hllc(const Phys& ph, const T qL[NQ], const T qR[NQ], const T fL[NQ], const T fR[NQ],
-                                     T rho_i_last, T F[NQ]) {
+                                     T dniL, T dniR, T rho_i_last, T F[NQ]) {
+    // dniL, dniR: 1/rho of the two states, as computed by primitives()
     constexpr int IPAR = DIR == 0 ? MX : DIR == 1 ? MY : MZ;
     constexpr int IP1 = DIR == 0 ? MY : DIR == 1 ? MZ : MX;
     constexpr int IP2 = DIR == 0 ? MZ : DIR == 1 ? MX : MY;
     const T aindex = T(ph.aindex), aindm1 = T(ph.aindm1);
     const T rhoL = qL[RH], rhoR = qR[RH];
-    T ri = T(1) / rhoL;
-    const T uL = qL[IPAR] * ri, vL = qL[IP1] * ri, wL = qL[IP2] * ri;
-    ri = T(1) / rhoR;
-    const T uR = qR[IPAR] * ri, vR = qR[IP1] * ri, wR = qR[IP2] * ri;
+    const T uL = qL[IPAR] * dniL, vL = qL[IP1] * dniL, wL = qL[IP2] * dniL;
+    const T uR = qR[IPAR] * dniR, vR = qR[IP1] * dniR, wR = qR[IP2] * dniR;
     T pL = aindm1 * (qL[EN] - T(0.5) * rhoL * (uL * uL + vL * vL + wL * wL));
     T pR = aindm1 * (qR[EN] - T(0.5) * rhoR * (uR * uR + vR * vR + wR * wR));
     T cL, cR;
@@ -241,8 +240,10 @@ __device__ __forceinline__ void hllc(const Phys& ph, const T qL[NQ], const T qR[
         cL = sqrt(T(7.2) * T(ph.P_1) * pow(rhoL, T(6.2)) + pL * rho_i_last);
         cR = sqrt(T(7.2) * T(ph.P_1) * pow(rhoR, T(6.2)) + pR * rho_i_last);
     } else {
-        cL = sqrt(aindex * pL / rhoL);
-        cR = sqrt(aindex * pR / rhoR);
+        // sqrt(aindex*p/rho) of flux.f90:537-538, with the division taken as
+        // a product with 1/rho (one rounding apart; two divisions fewer)
+        cL = sqrt(aindex * pL * dniL);
+        cR = sqrt(aindex * pR * dniR);
     }
     // S_L = min(lambda_M(Q_l), lambda_M(Q_r)); S_R = max(lambda_P(Q_r), lambda_P(Q_l))
     const T sL = fmin(uL - cL, uR - cR);

@@ -112,16 +112,7 @@ int cuda_fail(hermes_ctx* c, const char* what, cudaError_t e) {
     } while (0)
 
 bool pick_kernels(const hermes_config& c, KernelSet& K) {
-    if (c.precision == 64) {
-        if (c.nbasis == 4 && c.iquad == 2) { K = kernels_f64_nb4(); return true; }
-        if (c.nbasis == 8 && c.iquad == 2) { K = kernels_f64_nb8(); return true; }
-        if (c.nbasis == 10 && c.iquad == 3) { K = kernels_f64_nb10(); return true; }
-    } else if (c.precision == 32) {
-        if (c.nbasis == 4 && c.iquad == 2) { K = kernels_f32_nb4(); return true; }
-        if (c.nbasis == 8 && c.iquad == 2) { K = kernels_f32_nb8(); return true; }
-        if (c.nbasis == 10 && c.iquad == 3) { K = kernels_f32_nb10(); return true; }
-    }
-    return false;
+    return kernel_set(c.precision, c.nbasis, c.llns != 0, &K);
 }
 
 std::string check_config(const hermes_config& c) {

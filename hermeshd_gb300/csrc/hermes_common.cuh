@@ -29,6 +29,19 @@ __device__ __forceinline__ void sfor(F&& f) {
     sfor_impl(f, std::make_integer_sequence<int, N>{});
 }
 
+// run-time loop over [0, N) whose body is still instantiated per index
+// (compile-time tables stay constant); iterations are not interleaved by the
+// scheduler, which bounds register pressure for large bodies
+template <int N, class F>
+__device__ __forceinline__ void sfor_seq(F&& f) {
+#pragma unroll 1
+    for (int i = 0; i < N; ++i) {
+        sfor<N>([&](auto I) {
+            if (i == decltype(I)::value) f(I);
+        });
+    }
+}
+
 // physics constants (params.f90 / input.f90), identical for every box
 struct Phys {
     double aindex, aindm1, rh_floor, T_floor, P_floor, rh_mult;

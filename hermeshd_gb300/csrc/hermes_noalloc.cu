@@ -97,14 +97,9 @@ bool supported(const hermes_config& c) {
 }
 
 KernelSet kernels_for(const hermes_config& c) {
-    if (c.precision == 64) {
-        if (c.nbasis == 4) return kernels_f64_nb4();
-        if (c.nbasis == 8) return kernels_f64_nb8();
-        return kernels_f64_nb10();
-    }
-    if (c.nbasis == 4) return kernels_f32_nb4();
-    if (c.nbasis == 8) return kernels_f32_nb8();
-    return kernels_f32_nb10();
+    KernelSet k{};
+    kernel_set(c.precision, c.nbasis, c.llns != 0, &k);
+    return k;
 }
 
 }  // namespace

@@ -1,10 +1,10 @@
-// Stage kernels except the face kernel: T = float, nbasis 10, iquad 3.
+// Generated launcher translation unit (one of four per instantiation, compiled in parallel).
 #include "dg_launch.cuh"
 
 namespace hermes {
-KernelSet kernels_f32_nb10() {
-    KernelSet k = Launch<float, 10, 3>::set();
-    k.face = &face_f32_nb10;
-    return k;
+// T = float, nbasis 10, iquad 3: cell kernel without noise
+void cell_f32_nb10(const void* Qin, const void* Q0, void* out, const void* flux, const CellArgs& a, cudaStream_t s) {
+    Launch<float, 10, 3>::cell<false>(Qin, Q0, out, flux, a, s);
 }
+cudaError_t prep_f32_nb10() { return Launch<float, 10, 3>::prepare_cell<false>(); }
 }  // namespace hermes

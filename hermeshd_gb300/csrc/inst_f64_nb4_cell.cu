@@ -1,10 +1,10 @@
-// Stage kernels except the face kernel: T = double, nbasis 4, iquad 2.
+// Generated launcher translation unit (one of four per instantiation, compiled in parallel).
 #include "dg_launch.cuh"
 
 namespace hermes {
-KernelSet kernels_f64_nb4() {
-    KernelSet k = Launch<double, 4, 2>::set();
-    k.face = &face_f64_nb4;
-    return k;
+// T = double, nbasis 4, iquad 2: cell kernel without noise
+void cell_f64_nb4(const void* Qin, const void* Q0, void* out, const void* flux, const CellArgs& a, cudaStream_t s) {
+    Launch<double, 4, 2>::cell<false>(Qin, Q0, out, flux, a, s);
 }
+cudaError_t prep_f64_nb4() { return Launch<double, 4, 2>::prepare_cell<false>(); }
 }  // namespace hermes

@@ -1,0 +1,119 @@
+// kernel_sets.cu -- the launchers of one configuration (precision, basis,
+// stochastic stress on/off), assembled from the instantiation units.
+#include "dg_launch.cuh"
+
+namespace hermes {
+void face_f64_nb4(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void facen_f64_nb4(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void limit_f64_nb4(void*, const Geom&, const Phys&, cudaStream_t);
+void mindt_f64_nb4(const void*, const DtArgs&, cudaStream_t);
+void cell_f64_nb4(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+void celln_f64_nb4(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+cudaError_t prep_f64_nb4();
+cudaError_t prepn_f64_nb4();
+void face_f64_nb8(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void facen_f64_nb8(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void limit_f64_nb8(void*, const Geom&, const Phys&, cudaStream_t);
+void mindt_f64_nb8(const void*, const DtArgs&, cudaStream_t);
+void cell_f64_nb8(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+void celln_f64_nb8(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+cudaError_t prep_f64_nb8();
+cudaError_t prepn_f64_nb8();
+void face_f64_nb10(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void facen_f64_nb10(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void limit_f64_nb10(void*, const Geom&, const Phys&, cudaStream_t);
+void mindt_f64_nb10(const void*, const DtArgs&, cudaStream_t);
+void cell_f64_nb10(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+void celln_f64_nb10(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+cudaError_t prep_f64_nb10();
+cudaError_t prepn_f64_nb10();
+void face_f32_nb4(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void facen_f32_nb4(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void limit_f32_nb4(void*, const Geom&, const Phys&, cudaStream_t);
+void mindt_f32_nb4(const void*, const DtArgs&, cudaStream_t);
+void cell_f32_nb4(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+void celln_f32_nb4(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+cudaError_t prep_f32_nb4();
+cudaError_t prepn_f32_nb4();
+void face_f32_nb8(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void facen_f32_nb8(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void limit_f32_nb8(void*, const Geom&, const Phys&, cudaStream_t);
+void mindt_f32_nb8(const void*, const DtArgs&, cudaStream_t);
+void cell_f32_nb8(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+void celln_f32_nb8(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+cudaError_t prep_f32_nb8();
+cudaError_t prepn_f32_nb8();
+void face_f32_nb10(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void facen_f32_nb10(int, const void*, void*, const FaceArgs&, cudaStream_t);
+void limit_f32_nb10(void*, const Geom&, const Phys&, cudaStream_t);
+void mindt_f32_nb10(const void*, const DtArgs&, cudaStream_t);
+void cell_f32_nb10(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+void celln_f32_nb10(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
+cudaError_t prep_f32_nb10();
+cudaError_t prepn_f32_nb10();
+
+bool kernel_set(int precision, int nb, bool noise, KernelSet* out) {
+    KernelSet k;
+    if (precision == 64 && nb == 4) {
+        k.elem_size = sizeof(double); k.nb = 4; k.nqd = 2; k.nf = 4;
+        k.prepare = noise ? &prepn_f64_nb4 : &prep_f64_nb4;
+        k.limit = &limit_f64_nb4;
+        k.face = noise ? &facen_f64_nb4 : &face_f64_nb4;
+        k.cell = noise ? &celln_f64_nb4 : &cell_f64_nb4;
+        k.mindt = &mindt_f64_nb4;
+        *out = k;
+        return true;
+    }
+    if (precision == 64 && nb == 8) {
+        k.elem_size = sizeof(double); k.nb = 8; k.nqd = 2; k.nf = 4;
+        k.prepare = noise ? &prepn_f64_nb8 : &prep_f64_nb8;
+        k.limit = &limit_f64_nb8;
+        k.face = noise ? &facen_f64_nb8 : &face_f64_nb8;
+        k.cell = noise ? &celln_f64_nb8 : &cell_f64_nb8;
+        k.mindt = &mindt_f64_nb8;
+        *out = k;
+        return true;
+    }
+    if (precision == 64 && nb == 10) {
+        k.elem_size = sizeof(double); k.nb = 10; k.nqd = 3; k.nf = 9;
+        k.prepare = noise ? &prepn_f64_nb10 : &prep_f64_nb10;
+        k.limit = &limit_f64_nb10;
+        k.face = noise ? &facen_f64_nb10 : &face_f64_nb10;
+        k.cell = noise ? &celln_f64_nb10 : &cell_f64_nb10;
+        k.mindt = &mindt_f64_nb10;
+        *out = k;
+        return true;
+    }
+    if (precision == 32 && nb == 4) {
+        k.elem_size = sizeof(float); k.nb = 4; k.nqd = 2; k.nf = 4;
+        k.prepare = noise ? &prepn_f32_nb4 : &prep_f32_nb4;
+        k.limit = &limit_f32_nb4;
+        k.face = noise ? &facen_f32_nb4 : &face_f32_nb4;
+        k.cell = noise ? &celln_f32_nb4 : &cell_f32_nb4;
+        k.mindt = &mindt_f32_nb4;
+        *out = k;
+        return true;
+    }
+    if (precision == 32 && nb == 8) {
+        k.elem_size = sizeof(float); k.nb = 8; k.nqd = 2; k.nf = 4;
+        k.prepare = noise ? &prepn_f32_nb8 : &prep_f32_nb8;
+        k.limit = &limit_f32_nb8;
+        k.face = noise ? &facen_f32_nb8 : &face_f32_nb8;
+        k.cell = noise ? &celln_f32_nb8 : &cell_f32_nb8;
+        k.mindt = &mindt_f32_nb8;
+        *out = k;
+        return true;
+    }
+    if (precision == 32 && nb == 10) {
+        k.elem_size = sizeof(float); k.nb = 10; k.nqd = 3; k.nf = 9;
+        k.prepare = noise ? &prepn_f32_nb10 : &prep_f32_nb10;
+        k.limit = &limit_f32_nb10;
+        k.face = noise ? &facen_f32_nb10 : &face_f32_nb10;
+        k.cell = noise ? &celln_f32_nb10 : &cell_f32_nb10;
+        k.mindt = &mindt_f32_nb10;
+        *out = k;
+        return true;
+    }
+    return false;
+}
+}  // namespace hermes
