@@ -326,7 +326,7 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
     res["fp32_batched_ensemble"] = {
         "value": vens, "unit": UNIT, "ms_per_step": 1e3 * el / Ke, "steps": Ke, "dtype": "f32",
         "config": {"boxes": 256, "sizes": "uniform from {16,24,32,48}^3, seed 0", "cells": ens.ncells, "dof": dof,
-                   "nbasis": 4, "ivis": 1, "stochastic_stress": True, "rk": "SSP-RK2",
+                   "nbasis": 4, "ivis": 1, "stochastic_stress": True, "rk": "SSP-RK2", "riemann": "Roe (ihllc 2)",
                    "noise": "kT/(rho dV) = 1e-3, eta = 1, Philox key = realisation id"}}
     ens.close()
     del qe, qe1
@@ -343,7 +343,56 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
     res["fp64_plain_fh_box48"] = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * el / Ke, "dtype": "f64"}
     res["fp32_batched_ensemble"]["speedup_vs_fp64_plain"] = vens / v64
     s.close()
+    res["fp32_batched_ensemble"]["accuracy"] = ensemble_accuracy(base)
+    hl = ensemble_accuracy(base.replace(ihllc=1), nbox=16, steps=20)
+    res["fp32_batched_ensemble"]["accuracy_with_hllc"] = {
+        "max_rel_l2": hl["max_rel_l2"],
+        "note": "HLLC with the stress-augmented point flux is discontinuous at S_M = 0, where an equilibrium "
+                "fluctuating state sits at every face; FP32 and FP64 then pick branches by rounding"}
     return res
+
+
+def ensemble_accuracy(base, nbox=32, steps=20):
+    """Relative L2 error of the ensemble-averaged density field of the FP32
+    batched run against the same ensemble in FP64 (same seeds, same steps),
+    per box size, and the density S(k) of the FP64 run."""
+    import numpy as np
+    import torch
+
+    from hermeshd_gb300.analysis import StructureFactor
+    from hermeshd_gb300.solver import Ensemble
+
+    rng = np.random.default_rng(1)
+    sizes = rng.choice([16, 24, 32, 48], size=nbox)
+    dims = [(int(n), int(n), int(n)) for n in sizes]
+    dx = base.lx / 48
+    lengths = [(n * dx, n * dx, n * dx) for (n, _, _) in dims]
+    states = {}
+    for prec in ("fp32", "fp64"):
+        ens = Ensemble(base.replace(precision=prec), dims, lengths, seeds=list(range(nbox)))
+        q, q1 = ens.new_state(), ens.new_state()
+        for i in range(nbox):
+            v = ens.box_view(q, i)
+            v.zero_()
+            v[0, 0].fill_(1.0)
+            v[0, 4].fill_(1.0 / (base.aindex - 1.0))
+        ens.advance(q, q1, steps)
+        states[prec] = (ens, q)
+    err = {}
+    sf = StructureFactor(kmax=8)
+    e32, q32 = states["fp32"]
+    e64, q64 = states["fp64"]
+    for n in sorted(set(sizes)):
+        idx = [i for i, s in enumerate(sizes) if s == n]
+        a32 = torch.stack([e32.box_view(q32, i)[0, 0].double() for i in idx]).mean(0)
+        a64 = torch.stack([e64.box_view(q64, i)[0, 0] for i in idx]).mean(0)
+        err[int(n)] = float((a32 - a64).norm() / a64.norm())
+    sf.add_state(q64, base.nbasis, dims, e64.offsets)
+    e32.close()
+    e64.close()
+    return {"boxes": nbox, "steps": steps, "rel_l2_ensemble_mean_density_vs_fp64": err,
+            "max_rel_l2": max(err.values()),
+            "density_S_k_fp64": {int(k): v for k, v in sf.result().items()}}
 
 
 def cpu_baseline(cfg, Q0, steps):

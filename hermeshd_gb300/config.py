@@ -218,20 +218,26 @@ def taylor_green_3d(n: int = 64, precision: str = "fp32", mach: float = 0.1, rey
 
 
 def fh_box(n: int, eta: float = 1.0, kT_over_rho_dV: float = 1.0e-3, seed: int = 0, dt_noise: float = 0.1,
-           precision: str = "fp32", **kw) -> Config:
+           precision: str = "fp32", ihllc: int = 2, **kw) -> Config:
     """One realisation of the fluctuating-hydro ensemble: 10-moment (ivis 1)
     with stochastic stress, equilibrium rho = 1, T = 1 (p = 1), v = 0, nb 4.
     kT/(rho dV) = 1e-3 fixes the cell volume dV = 1000 (dx = 10).  The shear
     viscosity eta is not given by the benchmark; eta = 1 is chosen.
-    Amplitude per unit normal: sqrt(2 eta kT / (dV dt)) with dt = dt_noise
-    (the ensemble advances with a fixed step)."""
+    Amplitude per unit normal: sqrt(2 eta kT / (dV dt_noise)).
+
+    Riemann solver: Roe (ihllc = 2).  The reference's HLLC receives the
+    stress-augmented point flux, whose star fluxes differ by P_dd,L - P_dd,R
+    on the two sides of S_M = 0 (flux.f90:87-89,623-643); an equilibrium
+    fluctuating state has S_M ~ 0 at every face, so with HLLC the branch is
+    picked by rounding and FP32 and FP64 runs part at ~1e-4 in ensemble
+    means, against ~1e-7 with the Roe solver, which is continuous there."""
     gamma = 5.0 / 3.0
     dV = 1.0 / kT_over_rho_dV
     dx = dV ** (1.0 / 3.0)
     L = n * dx
     p = 1.0
     eta_sd = math.sqrt(2.0 * eta * 1.0 / (dV * dt_noise))
-    c = Config(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, nbasis=4, iquad=2, iorder=2, ivis=1, ieos=1, ihllc=1,
+    c = Config(nx=n, ny=n, nz=n, lx=L, ly=L, lz=L, nbasis=4, iquad=2, iorder=2, ivis=1, ieos=1, ihllc=ihllc,
                aindex=gamma, coll=p / eta, colvis=p, llns=True, eta_sd=eta_sd, zeta_sd=0.0, seed=seed,
                precision=precision)
     return c.replace(**kw)

@@ -1436,3 +1436,16 @@ double orc_test_basis(const orc_ctx *c, double *cell_dev, double *face_dev) {
     if (face_dev) *face_dev = mf;
     return md > mf ? md : mf;
 }
+
+void orc_noise_sample(unsigned long long seed, unsigned long long step, unsigned stage, unsigned kind,
+                      unsigned long long site, unsigned pt, double eta, double zeta, double G9[9], double S6[6]) {
+    orc_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.p.seed = seed;
+    c.p.eta_sd = eta;
+    c.p.zeta_sd = zeta;
+    c.noise_step = step;
+    c.noise_stage = (int)stage;
+    hermes_philox_normals9(seed, step, stage, kind, site, pt, G9);
+    stress_at(&c, (int)kind, site, (int)pt, S6);
+}

@@ -79,6 +79,11 @@ void orc_advance_fixed_dt(orc_ctx *c, double *Q, double *Q1, double *Q2, double 
 /* counter for the stochastic stress; the (step, stage) part of the Philox counter */
 void orc_set_noise_counter(orc_ctx *c, unsigned long long step);
 
+/* nine Philox normals and the stochastic stress {xx,yy,zz,xy,xz,yz} of one
+ * quadrature point of one flux call (for statistical tests) */
+void orc_noise_sample(unsigned long long seed, unsigned long long step, unsigned stage, unsigned kind,
+                      unsigned long long site, unsigned pt, double eta, double zeta, double G9[9], double S6[6]);
+
 /* per-phase wall time accumulators (seconds): limiter, faces, volume, surface, source, update */
 void orc_get_timers(const orc_ctx *c, double *out6);
 void orc_reset_timers(orc_ctx *c);

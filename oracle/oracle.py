@@ -80,6 +80,9 @@ def lib():
         L.orc_reset_timers.argtypes = [C.c_void_p]
         L.orc_num_threads.restype = C.c_int
         L.orc_set_num_threads.argtypes = [C.c_int]
+        L.orc_noise_sample.argtypes = [C.c_ulonglong, C.c_ulonglong, C.c_uint, C.c_uint, C.c_ulonglong, C.c_uint,
+                                       C.c_double, C.c_double, np.ctypeslib.ndpointer(dtype=np.float64),
+                                       np.ctypeslib.ndpointer(dtype=np.float64)]
         L.orc_test_basis.restype = C.c_double
         L.orc_test_basis.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
@@ -208,3 +211,11 @@ def num_threads():
 
 def set_num_threads(n):
     lib().orc_set_num_threads(n)
+
+
+def noise_sample(seed, step, stage, kind, site, pt, eta=1.0, zeta=0.0):
+    """(9 normals, stress {xx,yy,zz,xy,xz,yz}) of one point of one flux call."""
+    G = np.zeros(9)
+    S = np.zeros(6)
+    lib().orc_noise_sample(seed, step, stage, kind, site, pt, eta, zeta, G, S)
+    return G, S

@@ -240,3 +240,33 @@ def test_reference_front_end_step():
     assert abs(float(t) - to) <= 1e-14 * to
     assert rel_l2(Qio, Qo) < STEP_TOL
     mod.cleanup(t_start)
+
+
+def test_fh_ensemble_conserves_and_fluctuates():
+    """Stochastic stress enters as a face flux: mass and momentum of every box
+    are conserved to rounding while density fluctuations develop."""
+    import torch
+    from hermeshd_gb300.analysis import StructureFactor
+    from hermeshd_gb300.solver import Ensemble
+    base = config.fh_box(8, precision="fp64", seed=0)
+    dx = base.lx / 8
+    dims = [(8, 8, 8), (12, 12, 12), (6, 10, 8)]
+    ens = Ensemble(base, dims, [(d[0] * dx, d[1] * dx, d[2] * dx) for d in dims], seeds=[3, 4, 5])
+    q, q1 = ens.new_state(), ens.new_state()
+    for i in range(ens.nbox):
+        v = ens.box_view(q, i)
+        v[0, 0].fill_(1.0)
+        v[0, 4].fill_(1.0 / (base.aindex - 1.0))
+    m0 = [float(ens.box_view(q, i)[0, 0].sum()) for i in range(ens.nbox)]
+    ens.advance(q, q1, 40)
+    sf = StructureFactor(kmax=4)
+    for i in range(ens.nbox):
+        v = ens.box_view(q, i)
+        n = v[0, 0].numel()
+        assert abs(float(v[0, 0].sum()) / m0[i] - 1) < 1e-12
+        for c in (1, 2, 3):
+            assert abs(float(v[0, c].sum())) < 1e-12 * n
+        assert float(v[0, 0].std()) > 1e-6
+        assert torch.isfinite(v).all()
+    sf.add_state(q, base.nbasis, dims, ens.offsets)
+    assert all(np.isfinite(x) and x > 0 for x in sf.result().values())
