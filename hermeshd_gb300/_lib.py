@@ -22,7 +22,8 @@ EXPORTS = ("hermes_abi_version", "hermes_config_size", "hermes_sizes", "hermes_c
            "hermes_destroy", "hermes_last_error", "hermes_stream", "hermes_get_min_dt", "hermes_limiter",
            "hermes_rhs", "hermes_euler_stage", "hermes_step", "hermes_advance", "hermes_advance_host",
            "hermes_enqueue_steps", "hermes_profile_enable", "hermes_profile_read",
-           "hermes_box_times", "hermes_set_time", "hermes_set_noise_step", "hermes_check", "hermes_rhs_noalloc")
+           "hermes_box_times", "hermes_set_time", "hermes_set_noise_step", "hermes_check", "hermes_rhs_noalloc",
+           "hermes_rhs_vjp", "hermes_stage_vjp")
 
 
 class HermesError(RuntimeError):
@@ -110,6 +111,8 @@ def lib() -> C.CDLL:
         "hermes_set_noise_step": (i32, [vp, C.c_uint64]),
         "hermes_check": (i32, [vp]),
         "hermes_rhs_noalloc": (i32, [cfgp, vp, vp, i32, vp, C.c_char_p, C.c_size_t]),
+        "hermes_rhs_vjp": (i32, [vp, vp, vp, vp]),
+        "hermes_stage_vjp": (i32, [vp, vp, vp, vp, vp, C.c_double, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

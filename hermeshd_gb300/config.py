@@ -243,12 +243,23 @@ def fh_box(n: int, eta: float = 1.0, kT_over_rho_dV: float = 1.0e-3, seed: int =
     return c.replace(**kw)
 
 
-def poiseuille_2d(nx: int = 64, ny: int = 128, viscosity: float = 0.05, body_force: float = 1.0e-3, **kw) -> Config:
+def poiseuille_2d(nx: int = 64, ny: int = 128, viscosity: float = 0.05, body_force: float = 1.0e-3,
+                  ihllc: int = 2, **kw) -> Config:
     """2-D channel: periodic x, no-slip walls in y (boundary.f90:100-122),
     10-moment ivis 1 where viscosity enters through coll = p/mu (colvis = p),
-    driven by a uniform body force in x.  rho = 1, p = 1."""
+    driven by a uniform body force in x.  rho = 1, p = 1, ly = 1.
+
+    The cells are square (lx = ly*nx/ny): the reference's time step uses the
+    x spacing only (hermeshd.f90:174), so cells thinner in y than in x run
+    above the stable CFL number in y (with lx = 2, a 16x32 grid's velocities
+    grow from 1e-3 to 0.06-0.25 within 40 steps).  Roe flux
+    (ihllc = 2) by default: with the stress-augmented point flux HLLC is
+    discontinuous at S_M = 0 (flux.f90:623-643), which at rest is everywhere
+    in the channel, and it amplifies the perturbation (1e-3 to 2.5e-2 in 240
+    steps on a 16x32 grid) where Roe and the central flux damp it."""
     p = 1.0
-    c = Config(nx=nx, ny=ny, nz=1, lx=2.0, ly=1.0, lz=1.0 / 120.0, nbasis=4, iquad=2, iorder=2, ivis=1, ieos=1,
-               ihllc=1, aindex=5.0 / 3.0, coll=p / viscosity, colvis=p, ylobc="noslip", yhibc="noslip",
-               body_force=body_force)
+    ly = 1.0
+    c = Config(nx=nx, ny=ny, nz=1, lx=ly * nx / ny, ly=ly, lz=1.0 / 120.0, nbasis=4, iquad=2, iorder=2, ivis=1,
+               ieos=1, ihllc=ihllc, aindex=5.0 / 3.0, coll=p / viscosity, colvis=p, ylobc="noslip",
+               yhibc="noslip", body_force=body_force)
     return c.replace(**kw)

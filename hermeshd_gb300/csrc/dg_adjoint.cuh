@@ -1,0 +1,347 @@
+// dg_adjoint.cuh -- vector-Jacobian products of the DG right-hand side and of
+// one forward-Euler stage (FP64), the building blocks of the hand-written
+// adjoint of the SSP-RK step.
+//
+// R(Q) = surface(F_face(traces(Q))) - volume(F_point(values(Q))) - source(Q)
+// (flux.f90:932-1022, sources.f90:12-84).  The transpose of each linear map
+// (traces, interior values, surface and volume quadrature) uses the same
+// compile-time tables as the forward kernels; the point-wise nonlinear maps
+// (numerical face flux, point fluxes, sources) contribute J^T lambda, formed
+// column by column with dual numbers run through the forward physics code.
+//
+//   k_face_adj  per face point: lambda of the face flux from mu of the two
+//               cells that own the face, J^T of the numerical flux, boundary
+//               ghost maps transposed; writes the adjoint of both traces
+//   k_cell_adj  per cell: gathers the trace adjoints, volume and source
+//               transposes; writes nu = (dR/dQ)^T mu, or mu - dt*nu
+//
+// Scope: one grid, ieos 1, no stochastic stress, ivis 0 or 1; the limiter is
+// taken as the identity (it is inactive in the smooth regime where the
+// adjoint is used; the forward pass reports if it acted).
+#pragma once
+
+#include "dg_dual.cuh"
+#include "dg_launch.cuh"
+
+namespace hermes {
+
+// one side of a face: the cell and trace it comes from and the components a
+// boundary ghost keeps (bit v set = kept); cell < 0: a zero ghost
+struct TraceSrc {
+    long long cell;
+    int plus;
+    unsigned mask;
+};
+
+template <class TB, int DIR, int P>
+__device__ __forceinline__ double trace_of(const double* __restrict__ Qb, long long nc, const TraceSrc& s, int v) {
+    if (s.cell < 0) return 0.0;
+    double acc = 0.0;
+    if (s.plus) {
+        sfor<TB::NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            constexpr double c = ftab<TB, DIR, 1>(P, b);
+            if constexpr (c != 0.0) acc = fma(c, Qb[(long long)(b * NQ + v) * nc + s.cell], acc);
+        });
+    } else {
+        sfor<TB::NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            constexpr double c = ftab<TB, DIR, 0>(P, b);
+            if constexpr (c != 0.0) acc = fma(c, Qb[(long long)(b * NQ + v) * nc + s.cell], acc);
+        });
+    }
+    return ((s.mask >> v) & 1u) ? acc : 0.0;
+}
+
+template <class TB, int DIR, int P>
+__device__ __forceinline__ void face_adj_point(const double* __restrict__ Q, const double* __restrict__ mu,
+                                               double* __restrict__ tadj, const AdjArgs& a, long long gf) {
+    const Geom& G = a.G;
+    const Phys& ph = a.ph;
+    const Box& B = G.boxes[0];
+    const long long lf = gf;
+    const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
+    const int ex = DIR == 0 ? B.nfp[0] : n0, ey = DIR == 1 ? B.nfp[1] : n1;
+    const int i = (int)(lf % ex), j = (int)((lf / ex) % ey), k = (int)(lf / ((long long)ex * ey));
+    const int n = B.n[DIR];
+    const int s = DIR == 0 ? i : DIR == 1 ? j : k;
+    const bool dedup = B.nfp[DIR] == n;
+    const long long nc = B.ncell;
+    auto cell_at = [&](int c) -> long long {
+        int ci = DIR == 0 ? c : i, cj = DIR == 1 ? c : j, ck = DIR == 2 ? c : k;
+        return (long long)ci + (long long)n0 * (cj + (long long)n1 * ck);
+    };
+    constexpr int MN = DIR == 0 ? MX : DIR == 1 ? MY : MZ;
+    const unsigned all = (1u << NQ) - 1u;
+    // sources of the two traces, boundary ghosts of boundary.f90:40-338
+    TraceSrc L{-1, 1, all}, R{-1, 0, all};
+    long long own_plus = -1, own_minus = -1;   // cells whose plus / minus face this is
+    bool ghostL_from_R = false, ghostR_from_L = false;
+    if (dedup || (s > 0 && s < n)) {
+        const int lo = s > 0 ? s - 1 : n - 1;
+        L = TraceSrc{cell_at(lo), 1, all};
+        R = TraceSrc{cell_at(s), 0, all};
+        own_plus = L.cell;
+        own_minus = R.cell;
+    } else if (s == 0) {
+        R = TraceSrc{cell_at(0), 0, all};
+        own_minus = R.cell;
+        const int code = B.bc[2 * DIR];
+        if (code != BC_PERIODIC) {
+            unsigned m = all;
+            if (code == BC_NOSLIP) m &= ~((1u << MX) | (1u << MY) | (1u << MZ));
+            else if (code == BC_WALL) m &= ~(1u << MN);
+            else if (code == BC_OUTFLOW) {
+                double mmax = -INFINITY;
+                sfor<TB::NF>([&](auto pp) {
+                    mmax = fmax(mmax, trace_var<TB, DIR, 0, decltype(pp)::value, MN>(Q, nc, R.cell));
+                });
+                if (mmax > 0.0) m &= ~(1u << MN);
+            }
+            L = TraceSrc{R.cell, 0, m};
+            ghostL_from_R = true;
+        }
+    } else {
+        L = TraceSrc{cell_at(n - 1), 1, all};
+        own_plus = L.cell;
+        const int code = B.bc[2 * DIR + 1];
+        // (a periodic high flag with a non-periodic low one is rejected by the host)
+        if (code != BC_PERIODIC && !(code == BC_OUTFLOW && DIR == 0)) {
+            unsigned m = all;
+            if (code == BC_NOSLIP) m &= ~((1u << MX) | (1u << MY) | (1u << MZ));
+            else if (code == BC_WALL) m &= ~(1u << MN);
+            else if (code == BC_OUTFLOW) {
+                double mmin = INFINITY;
+                sfor<TB::NF>([&](auto pp) {
+                    mmin = fmin(mmin, trace_var<TB, DIR, 1, decltype(pp)::value, MN>(Q, nc, L.cell));
+                });
+                if (mmin < 0.0) m &= ~(1u << MN);
+            }
+            R = TraceSrc{L.cell, 1, m};
+            ghostR_from_L = true;
+        }
+    }
+    double qL[NQ], qR[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) {
+        qL[v] = trace_of<TB, DIR, P>(Q, nc, L, v);
+        qR[v] = trace_of<TB, DIR, P>(Q, nc, R, v);
+    }
+    // adjoint of the stored face flux (F * di) from the surface assembly
+    double lamF[NQ];
+    const double di = B.di[DIR];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) {
+        double sacc = 0.0;
+        if (own_plus >= 0)
+            sfor<TB::NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr double c = stab<TB, DIR, 1>(P, b);
+                if constexpr (c != 0.0) sacc = fma(c, mu[(long long)(b * NQ + v) * nc + own_plus], sacc);
+            });
+        if (own_minus >= 0)
+            sfor<TB::NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr double c = stab<TB, DIR, 0>(P, b);
+                if constexpr (c != 0.0) sacc = fma(c, mu[(long long)(b * NQ + v) * nc + own_minus], sacc);
+            });
+        lamF[v] = di * sacc;
+    }
+    // J^T lamF, one dual pass per input component
+    double lamL[NQ], lamR[NQ];
+    const Dual S0[6] = {Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0)};
+#pragma unroll 1
+    for (int side = 0; side < 2; ++side) {
+        const TraceSrc& src = side == 0 ? L : R;
+        double* lam = side == 0 ? lamL : lamR;
+#pragma unroll 1
+        for (int jv = 0; jv < NQ; ++jv) {
+            lam[jv] = 0.0;
+            if (src.cell < 0 || !((src.mask >> jv) & 1u)) continue;
+            Dual dL[NQ], dR[NQ], F[NQ];
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) {
+                dL[v] = Dual(qL[v], (side == 0 && v == jv) ? 1.0 : 0.0);
+                dR[v] = Dual(qR[v], (side == 1 && v == jv) ? 1.0 : 0.0);
+            }
+            face_flux_fn<Dual, DIR>(ph, dL, dR, S0, S0, Dual(0.0), F);
+            double acc = 0.0;
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) acc = fma(lamF[v], F[v].d, acc);
+            lam[jv] = acc;
+        }
+    }
+    // a ghost made from a cell's own trace hands its adjoint to that trace
+    if (ghostL_from_R) {
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) { lamR[v] += lamL[v]; lamL[v] = 0.0; }
+    }
+    if (ghostR_from_L) {
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) { lamL[v] += lamR[v]; lamR[v] = 0.0; }
+    }
+    const long long nfd = (long long)ex * ey * (DIR == 2 ? B.nfp[2] : n2);
+    double* tb = tadj + 2 * B.fbase[DIR];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) {
+        tb[((long long)(0 * NQ + v) * TB::NF + P) * nfd + lf] = lamL[v];
+        tb[((long long)(1 * NQ + v) * TB::NF + P) * nfd + lf] = lamR[v];
+    }
+}
+
+template <class TB, int DIR>
+__global__ void __launch_bounds__(ADJ_TPB) k_face_adj(const double* __restrict__ Q, const double* __restrict__ mu,
+                                                      double* __restrict__ tadj, AdjArgs a) {
+    const long long gf = (long long)blockIdx.x * ADJ_TPB + threadIdx.x;
+    if (gf >= a.G.nface[DIR]) return;
+    const int p = blockIdx.y;
+    sfor<TB::NF>([&](auto pp) {
+        constexpr int P = decltype(pp)::value;
+        if (p == P) face_adj_point<TB, DIR, P>(Q, mu, tadj, a, gf);
+    });
+}
+
+template <class TB>
+__global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__ Q, const double* __restrict__ mu,
+                                                      const double* __restrict__ tadj, double* __restrict__ out, AdjArgs a) {
+    constexpr int NB = TB::NB, NF = TB::NF, NPG = TB::NPG;
+    const long long le = (long long)blockIdx.x * ADJ_TPB + threadIdx.x;
+    if (le >= a.G.ncell) return;
+    const Phys& ph = a.ph;
+    const Box& B = a.G.boxes[0];
+    const long long nc = B.ncell;
+    double nu[NB][NQ];
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) nu[b][v] = 0.0;
+    // ---- traces: transpose of the trace evaluation of both faces per direction
+    const int n0 = B.n[0], n1 = B.n[1];
+    const int c[3] = {(int)(le % n0), (int)((le / n0) % n1), (int)(le / ((long long)n0 * n1))};
+    sfor<3>([&](auto dd) {
+        constexpr int d = decltype(dd)::value;
+        const int e0 = d == 0 ? B.nfp[0] : B.n[0], e1 = d == 1 ? B.nfp[1] : B.n[1], e2 = d == 2 ? B.nfp[2] : B.n[2];
+        const long long nfd = (long long)e0 * e1 * e2;
+        int hi = c[d] + 1;
+        if (B.nfp[d] == B.n[d] && hi == B.n[d]) hi = 0;
+        const int lo = c[d];
+        int a0 = d == 0 ? lo : c[0], a1 = d == 1 ? lo : c[1], a2 = d == 2 ? lo : c[2];
+        const long long fm = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
+        a0 = d == 0 ? hi : c[0]; a1 = d == 1 ? hi : c[1]; a2 = d == 2 ? hi : c[2];
+        const long long fp = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
+        const double* tb = tadj + 2 * B.fbase[d];
+        sfor<NF>([&](auto pp) {
+            constexpr int p = decltype(pp)::value;
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) {
+                const double lm = tb[((long long)(1 * NQ + v) * NF + p) * nfd + fm];   // minus face: R slot
+                const double lp = tb[((long long)(0 * NQ + v) * NF + p) * nfd + fp];   // plus face: L slot
+                sfor<NB>([&](auto bb) {
+                    constexpr int b = decltype(bb)::value;
+                    constexpr double cm = ftab<TB, d, 0>(p, b);
+                    constexpr double cp = ftab<TB, d, 1>(p, b);
+                    if constexpr (cm != 0.0) nu[b][v] = fma(cm, lm, nu[b][v]);
+                    if constexpr (cp != 0.0) nu[b][v] = fma(cp, lp, nu[b][v]);
+                });
+            }
+        });
+    });
+    // ---- volume quadrature and sources: R -= sum_g VD di F_d(u(g)) + SRC s(u(g))
+    const double di[3] = {B.di[0], B.di[1], B.di[2]};
+    const bool src_lin = ph.ivis == 0, src_bf = ph.body_force != 0.0;
+    const Dual S0[6] = {Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0)};
+    sfor_seq<NPG>([&](auto gg) {
+        constexpr int g = decltype(gg)::value;
+        double u[NQ];
+        sfor<NQ>([&](auto vv) {
+            constexpr int v = decltype(vv)::value;
+            double s = 0.0;
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr double cI = TB::INT(g, b);
+                if constexpr (cI != 0.0) s = fma(cI, Q[(long long)(b * NQ + v) * nc + le], s);
+            });
+            u[v] = s;
+        });
+        // adjoints of the point fluxes and point sources at g
+        double lamF[3][NQ], lamS[NQ];
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) {
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, as = 0.0;
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                const double m = mu[(long long)(b * NQ + v) * nc + le];
+                constexpr double c0 = TB::VX(g, b), c1 = TB::VY(g, b), c2 = TB::VZ(g, b), cs = TB::SRC(g, b);
+                if constexpr (c0 != 0.0) a0 = fma(c0, m, a0);
+                if constexpr (c1 != 0.0) a1 = fma(c1, m, a1);
+                if constexpr (c2 != 0.0) a2 = fma(c2, m, a2);
+                if constexpr (cs != 0.0) as = fma(cs, m, as);
+            });
+            lamF[0][v] = -di[0] * a0;
+            lamF[1][v] = -di[1] * a1;
+            lamF[2][v] = -di[2] * a2;
+            lamS[v] = -as;
+        }
+        double lamu[NQ];
+#pragma unroll 1
+        for (int jv = 0; jv < NQ; ++jv) {
+            Dual ud[NQ];
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) ud[v] = Dual(u[v], v == jv ? 1.0 : 0.0);
+            const Prim<Dual> w = primitives(ph, ud);
+            double acc = 0.0;
+            sfor<3>([&](auto dd) {
+                constexpr int d = decltype(dd)::value;
+                Dual f[NQ];
+                point_flux<Dual, d>(ph, ud, w, S0, f);
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) acc = fma(lamF[d][v], f[v].d, acc);
+            });
+            // point sources (sources.f90:37-43; body force): linear in u
+            if (src_lin) {
+#pragma unroll
+                for (int v = PXX; v <= PYZ; ++v) acc = fma(lamS[v], (v == jv ? -ph.coll : 0.0), acc);
+            }
+            if (src_bf) {
+                if (jv == RH) acc = fma(lamS[MX], ph.body_force, acc);
+                if (jv == MX) acc = fma(lamS[EN], ph.body_force, acc);
+            }
+            lamu[jv] = acc;
+        }
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            constexpr double cI = TB::INT(g, b);
+            if constexpr (cI != 0.0) {
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) nu[b][v] = fma(cI, lamu[v], nu[b][v]);
+            }
+        });
+    });
+    const double dt = a.st[0].dt;
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) {
+            const long long ix = (long long)(b * NQ + v) * nc + le;
+            out[ix] = a.mode == 0 ? nu[b][v] : mu[ix] - dt * nu[b][v];
+        }
+}
+
+// launcher of one basis: the three face-adjoint passes, then the cell pass
+template <int NB, int NQD>
+cudaError_t adj_launch(const double* Q, const double* mu, double* tadj, double* out, const AdjArgs& a, cudaStream_t s) {
+    using TB = hermes_tab::Tab<NB, NQD>;
+    for (int d = 0; d < 3; ++d) {
+        const long long n = a.G.nface[d];
+        if (n <= 0) continue;
+        dim3 grid((unsigned)((n + ADJ_TPB - 1) / ADJ_TPB), TB::NF);
+        if (d == 0) k_face_adj<TB, 0><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+        else if (d == 1) k_face_adj<TB, 1><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+        else k_face_adj<TB, 2><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+    }
+    if (a.G.ncell > 0)
+        k_cell_adj<TB><<<(unsigned)((a.G.ncell + ADJ_TPB - 1) / ADJ_TPB), ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);
+    return cudaGetLastError();
+}
+
+}  // namespace hermes

@@ -254,6 +254,36 @@ struct FaceArgs {
     unsigned stage;
 };
 
+// the numerical flux at one face point from the two traces (after boundary
+// ghosts): point fluxes of both sides (flux.f90:240), central flux or LLF
+// with the freezing speed (flux.f90:243-262), then HLLC (flux.f90:264-271) or
+// Roe (SEAN monolith) for rh..en.  Shared by k_face and the adjoint.
+template <class T, int DIR>
+__device__ __forceinline__ void face_flux_fn(const Phys& ph, const T qL[NQ], const T qR[NQ], const T SL[6], const T SR[6],
+                                             T rho_i_last, T F[NQ]) {
+    T fL[NQ], fR[NQ];
+    const Prim<T> wL = primitives(ph, qL);
+    point_flux<T, DIR>(ph, qL, wL, SL, fL);
+    const Prim<T> wR = primitives(ph, qR);
+    point_flux<T, DIR>(ph, qR, wR, SR, fR);
+    if (ph.ivis >= 2) {   // ivis 3: the Grad-closure code always applies LLF (ten_moment.f90:1131-1147)
+        const T cfr = fmax(cfcal<T, DIR>(ph, qL), cfcal<T, DIR>(ph, qR));
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]) - T(0.5) * cfr * (qR[v] - qL[v]);
+    } else {
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]);
+    }
+    if (ph.ihllc == 2) {
+        T FR[NQ];
+        if (roe<T, DIR>(ph, qL, qR, fL, fR, FR)) {
+            F[RH] = FR[RH]; F[MX] = FR[MX]; F[MY] = FR[MY]; F[MZ] = FR[MZ]; F[EN] = FR[EN];
+        }
+    } else if (ph.ihllc == 1) {
+        hllc<T, DIR>(ph, qL, qR, fL, fR, wL.dni, wR.dni, rho_i_last, F);
+    }
+}
+
 template <class T, class TB, int DIR, int P, bool NOISE>
 __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restrict__ flux, const FaceArgs& a, long long gf) {
     const Geom& G = a.G;
@@ -334,27 +364,9 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
         random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P, SL);
         random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P + TB::NF, SR);
     }
-    T fL[NQ], fR[NQ], F[NQ];
-    const Prim<T> wL = primitives(ph, qL);
-    point_flux<T, DIR>(ph, qL, wL, SL, fL);
-    const Prim<T> wR = primitives(ph, qR);
-    point_flux<T, DIR>(ph, qR, wR, SR, fR);
-    // flux.f90:243-262: central flux, LLF with the freezing speed for ivis 2
-    if (ph.ivis >= 2) {   // ivis 3: the Grad-closure code always applies LLF (ten_moment.f90:1131-1147)
-        const T cfr = fmax(cfcal<T, DIR>(ph, qL), cfcal<T, DIR>(ph, qR));
-#pragma unroll
-        for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]) - T(0.5) * cfr * (qR[v] - qL[v]);
-    } else {
-#pragma unroll
-        for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]);
-    }
-    if (ph.ihllc == 2) {
-        T FR[NQ];
-        if (roe<T, DIR>(ph, qL, qR, fL, fR, FR)) {
-            F[RH] = FR[RH]; F[MX] = FR[MX]; F[MY] = FR[MY]; F[MZ] = FR[MZ]; F[EN] = FR[EN];
-        }
-    } else if (ph.ihllc == 1) {
-        T rho_i_last = T(0);
+    T F[NQ];
+    T rho_i_last = T(0);
+    if (ph.ihllc == 1) {
         if (ph.ieos == 2) {
             // 1/rho of the last point of the reference's call: the right state at point NF-1
             T rlast;
@@ -364,8 +376,8 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
             else rlast = trace_var<TB, DIR, 1, TB::NF - 1, RH>(Qb, nc, cell_at(n - 1));
             rho_i_last = T(1) / rlast;
         }
-        hllc<T, DIR>(ph, qL, qR, fL, fR, wL.dni, wR.dni, rho_i_last, F);
     }
+    face_flux_fn<T, DIR>(ph, qL, qR, SL, SR, rho_i_last, F);
     // store, scaled by the inverse spacing of this direction
     const T sc = T(B.di[DIR]);
     const long long nfd = (long long)ex * ey * (DIR == 2 ? B.nfp[2] : n2);

@@ -74,4 +74,18 @@ using PrepFn = cudaError_t (*)();
 // precision 64 or 32, nb 4/8/10; false if unsupported
 bool kernel_set(int precision, int nb, bool noise, KernelSet* out);
 
+// ---- adjoint of the right-hand side (FP64, one box; dg_adjoint.cuh) ----
+constexpr int ADJ_TPB = 64;
+
+struct AdjArgs {
+    Geom G;
+    Phys ph;
+    const BoxState* st;
+    int mode;       // 0: out = nu = (dR/dQ)^T mu; 1: out = mu - dt*nu
+};
+
+// (Q, mu, trace-adjoint scratch of 2x the face-flux size, out, args, stream)
+using AdjFn = cudaError_t (*)(const double*, const double*, double*, double*, const AdjArgs&, cudaStream_t);
+bool adjoint_launcher(int nb, AdjFn* out);
+
 }  // namespace hermes

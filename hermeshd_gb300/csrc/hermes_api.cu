@@ -55,6 +55,44 @@ __global__ void k_dt_finalize(const Box* __restrict__ boxes, int nbox, BoxState*
     st[b].vmag_bits = 0ull;
 }
 
+// adjoint stage prologue: mu = M lam_out, where M is the semi-implicit factor
+// faci on the stresses for ivis 1 (integrator.f90:174), and per-block partial
+// sums of dL/dcoll = sum_stress lam_out * dE/dcoll = sum lam_out * (-dt faci E_out)
+__global__ void __launch_bounds__(256) k_stage_pre(const double* __restrict__ lam_out, const double* __restrict__ e_out,
+                                                   double* __restrict__ mu, double* __restrict__ part, long long n,
+                                                   long long ncell, int ivis, double dt, double faci) {
+    __shared__ double red[256];
+    const long long e = (long long)blockIdx.x * 256 + threadIdx.x;
+    double c = 0.0;
+    if (e < n) {
+        const int v = (int)((e / ncell) % NQ);
+        const bool stress = v >= PXX && ivis == 1;
+        mu[e] = stress ? faci * lam_out[e] : lam_out[e];
+        if (stress && e_out) c = lam_out[e] * (-dt * faci * e_out[e]);
+    }
+    red[threadIdx.x] = c;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// fixed-order sum of the partials, so the result does not depend on scheduling
+__global__ void k_sum_partials(const double* __restrict__ part, int n, double* __restrict__ out) {
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += 256) s += part[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = red[0];
+}
+
 __global__ void k_dt_finalize_only(const Box* __restrict__ boxes, int nbox, BoxState* st) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbox) return;
@@ -92,6 +130,13 @@ struct hermes_ctx {
     std::vector<cudaEvent_t> pool;
     double prof_ms[6] = {0, 0, 0, 0, 0, 0};
     long long prof_n[6] = {0, 0, 0, 0, 0, 0};
+    // adjoint scratch, allocated on first use
+    AdjFn adj = nullptr;
+    double* d_tadj = nullptr;   // trace adjoints: 2 x the face-flux size
+    double* d_mu = nullptr;     // M lam of a stage
+    double* d_part = nullptr;   // partial sums of dL/dcoll
+    double* d_sum = nullptr;
+    int npart = 0;
 };
 
 namespace {
@@ -437,6 +482,10 @@ int hermes_destroy(hermes_ctx* c) {
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->ev_in) cudaEventDestroy(c->ev_in);
     if (c->ev_out) cudaEventDestroy(c->ev_out);
+    cudaFree(c->d_tadj);
+    cudaFree(c->d_mu);
+    cudaFree(c->d_part);
+    cudaFree(c->d_sum);
     delete c;
     return HERMES_OK;
 }
@@ -627,6 +676,79 @@ int hermes_check(hermes_ctx* c) {
     rc = launch_status(c);
     if (rc == HERMES_OK) rc = read_back(c, nullptr, nullptr);
     return leave(c, rc);
+}
+
+// ---- adjoint -------------------------------------------------------------
+namespace {
+std::string adjoint_unsupported(const hermes_config& c, int nbox) {
+    if (c.precision != 64) return "the adjoint is FP64 only";
+    if (nbox != 1) return "the adjoint takes a single grid";
+    if (c.llns) return "the adjoint does not model the stochastic stress";
+    if (c.ivis != 0 && c.ivis != 1) return "the adjoint supports ivis 0 and 1";
+    if (c.ieos != 1) return "the adjoint supports ieos 1";
+    for (int d = 0; d < 3; ++d)
+        if ((c.bc[2 * d] == HERMES_BC_PERIODIC) != (c.bc[2 * d + 1] == HERMES_BC_PERIODIC))
+            return "the adjoint needs both or neither end of a direction periodic";
+    return "";
+}
+
+int adj_prepare(hermes_ctx* c) {
+    const std::string why = adjoint_unsupported(c->cfg, c->G.nbox);
+    if (!why.empty()) return fail(c, HERMES_ERR_CONFIG, why);
+    if (!c->adj && !adjoint_launcher(c->cfg.nbasis, &c->adj)) return fail(c, HERMES_ERR_CONFIG, "no adjoint for this basis");
+    if (!c->d_tadj) {
+        c->npart = (int)((c->q_elems + 255) / 256);
+        if (cudaMalloc(&c->d_tadj, 2 * c->flux_elems * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&c->d_mu, c->q_elems * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&c->d_part, (size_t)c->npart * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&c->d_sum, sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(c, HERMES_ERR_ALLOC, "adjoint scratch");
+        }
+    }
+    return HERMES_OK;
+}
+}  // namespace
+
+int hermes_rhs_vjp(hermes_ctx* c, const void* q, const void* mu, void* nu) {
+    if (!c || !q || !mu || !nu) return fail(c, HERMES_ERR_ARG, "null argument");
+    if (nu == q || nu == mu) return fail(c, HERMES_ERR_ARG, "nu must not alias q or mu");
+    int rc = enter(c);
+    if (rc) return rc;
+    rc = adj_prepare(c);
+    if (rc) return leave(c, rc);
+    AdjArgs a{c->G, c->ph, c->d_st, 0};
+    cudaError_t e = c->adj(static_cast<const double*>(q), static_cast<const double*>(mu), c->d_tadj,
+                           static_cast<double*>(nu), a, c->stream);
+    if (e != cudaSuccess) return leave(c, cuda_fail(c, "adjoint launch", e));
+    return leave(c, HERMES_OK);
+}
+
+int hermes_stage_vjp(hermes_ctx* c, const void* q_in, const void* e_out, const void* lam_out, void* lam_in, double dt,
+                     double* dcoll) {
+    if (!c || !q_in || !lam_out || !lam_in) return fail(c, HERMES_ERR_ARG, "null argument");
+    if (lam_in == q_in || (e_out && lam_in == e_out)) return fail(c, HERMES_ERR_ARG, "lam_in must not alias q_in or e_out");
+    if (dcoll && !e_out) return fail(c, HERMES_ERR_ARG, "dcoll needs e_out");
+    if (dcoll && c->cfg.ivis != 1) return fail(c, HERMES_ERR_CONFIG, "dcoll is defined for ivis 1 (coll enters through faci)");
+    if (!(dt > 0.0)) return fail(c, HERMES_ERR_ARG, "dt must be positive");
+    int rc = enter(c);
+    if (rc) return rc;
+    rc = adj_prepare(c);
+    if (rc) return leave(c, rc);
+    k_set_dt<<<1, 32, 0, c->stream>>>(c->d_st, 1, dt);
+    const long long n = (long long)c->q_elems;
+    const double faci = 1.0 / (1.0 + dt * c->cfg.coll);
+    k_stage_pre<<<c->npart, 256, 0, c->stream>>>(static_cast<const double*>(lam_out), static_cast<const double*>(e_out),
+                                                 c->d_mu, c->d_part, n, c->G.ncell, c->cfg.ivis, dt, faci);
+    if (dcoll) k_sum_partials<<<1, 256, 0, c->stream>>>(c->d_part, c->npart, c->d_sum);
+    AdjArgs a{c->G, c->ph, c->d_st, 1};
+    cudaError_t e = c->adj(static_cast<const double*>(q_in), c->d_mu, c->d_tadj, static_cast<double*>(lam_in), a, c->stream);
+    if (e != cudaSuccess) return leave(c, cuda_fail(c, "adjoint launch", e));
+    if (dcoll) {
+        HCK(c, cudaMemcpyAsync(dcoll, c->d_sum, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        HCK(c, cudaStreamSynchronize(c->stream));
+    }
+    return leave(c, launch_status(c));
 }
 
 }  // extern "C"

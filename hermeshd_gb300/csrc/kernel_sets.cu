@@ -116,4 +116,16 @@ bool kernel_set(int precision, int nb, bool noise, KernelSet* out) {
     }
     return false;
 }
+
+cudaError_t adj_f64_nb4(const double*, const double*, double*, double*, const AdjArgs&, cudaStream_t);
+cudaError_t adj_f64_nb8(const double*, const double*, double*, double*, const AdjArgs&, cudaStream_t);
+cudaError_t adj_f64_nb10(const double*, const double*, double*, double*, const AdjArgs&, cudaStream_t);
+
+bool adjoint_launcher(int nb, AdjFn* out) {
+    if (nb == 4) *out = &adj_f64_nb4;
+    else if (nb == 8) *out = &adj_f64_nb8;
+    else if (nb == 10) *out = &adj_f64_nb10;
+    else return false;
+    return true;
+}
 }  // namespace hermes

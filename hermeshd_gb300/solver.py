@@ -92,6 +92,25 @@ class Solver:
         check(lib().hermes_euler_stage(self.ctx, self._ptr(q_in), self._ptr(out), float(dt)), self.ctx)
         return out
 
+    # ---- adjoint (FP64, one grid) -------------------------------------------
+    def rhs_vjp(self, q, mu, out=None):
+        """(dR/dq)^T mu for R = rhs(q, limit=False)."""
+        out = self.new_state() if out is None else out
+        check(lib().hermes_rhs_vjp(self.ctx, self._ptr(q), self._ptr(mu), self._ptr(out)), self.ctx)
+        return out
+
+    def stage_vjp(self, q_in, lam_out, dt: float, e_out=None, want_dcoll: bool = False, out=None):
+        """(dE/dq_in)^T lam_out for the forward-Euler stage E of
+        euler_stage(q_in, dt) (limiter inactive); with want_dcoll also
+        lam_out . dE/dcoll (ivis 1, needs e_out = E(q_in)).  Returns
+        (lam_in, dcoll or None)."""
+        out = self.new_state() if out is None else out
+        dc = C.c_double(0.0)
+        check(lib().hermes_stage_vjp(self.ctx, self._ptr(q_in), None if e_out is None else self._ptr(e_out),
+                                     self._ptr(lam_out), self._ptr(out), float(dt),
+                                     C.byref(dc) if want_dcoll else None), self.ctx)
+        return out, (dc.value if want_dcoll else None)
+
     def step(self, q, q1, q2=None, t: float = 0.0):
         """One step of hermeshd.f90:53-62; returns (t, dt)."""
         tt, dd = C.c_double(t), C.c_double(0.0)

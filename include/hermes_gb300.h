@@ -192,6 +192,25 @@ int hermes_check(hermes_ctx *ctx);
 int hermes_rhs_noalloc(const hermes_config *cfg, void *q, void *rhs, int apply_limiter, void *stream, char *err,
                        size_t errlen);
 
+/* Adjoint of the right-hand side and of one forward-Euler stage (FP64, one
+ * grid, ivis 0 or 1, ieos 1, no stochastic stress; a direction is periodic at
+ * both ends or at neither).  No counterpart in the reference, which has no
+ * derivatives; the forward map they differentiate is hermes_rhs without the
+ * limiter (flux.f90:932-1022, sources.f90:12-84) and the update of
+ * integrator.f90:147-174.  Branches (HLLC wave selection, floors, outflow
+ * ghosts) are differentiated on their active side.
+ *
+ * hermes_rhs_vjp: nu = (dR/dq)^T mu for R = hermes_rhs(q) (apply_limiter 0).
+ * hermes_stage_vjp: lam_in = (dE/dq_in)^T lam_out for the stage
+ * E(q_in) = M (q_in - dt R(q_in)), M = 1/(1 + dt coll) on the stresses for
+ * ivis 1 and 1 elsewhere.  e_out = E(q_in) (may be NULL when dcoll is NULL);
+ * dcoll, if not NULL, receives lam_out . dE/dcoll (ivis 1), and the call then
+ * synchronises.  lam_in may alias lam_out.  Scratch (2x the face-flux size
+ * plus one field) is allocated on the first call. */
+int hermes_rhs_vjp(hermes_ctx *ctx, const void *q, const void *mu, void *nu);
+int hermes_stage_vjp(hermes_ctx *ctx, const void *q_in, const void *e_out, const void *lam_out, void *lam_in, double dt,
+                     double *dcoll);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,51 @@
+"""Host-side pieces of the adjoint, on the CPU: the differentiable CFL time
+step against the oracle's get_min_dt, and the torch channel initial state
+against ic.channel."""
+import numpy as np
+import pytest
+
+from hermeshd_gb300 import config, ic
+
+
+def test_dt_of_matches_oracle():
+    torch = pytest.importorskip("torch")
+    import oracle as O
+    from hermeshd_gb300.adjoint import Rollout
+    cfg = config.Config(nx=6, ny=5, nz=4, nbasis=4, iquad=2, ivis=1, coll=2.0, colvis=1.0)
+    Q = ic.random_smooth(cfg, seed=2, amp=0.1)
+    q = torch.from_numpy(np.ascontiguousarray(Q.T))
+    dt = float(Rollout(cfg).dt_of(q))
+    assert dt == pytest.approx(O.Oracle(cfg).get_min_dt(Q), rel=1e-14)
+
+
+def test_dt_of_gradient_is_local():
+    """d dt / dq touches only the cell averages of the arg-max cell and the last cell."""
+    torch = pytest.importorskip("torch")
+    from hermeshd_gb300.adjoint import Rollout
+    cfg = config.Config(nx=5, ny=4, nz=3, nbasis=4, iquad=2)
+    Q = ic.random_smooth(cfg, seed=3, amp=0.1)
+    q = torch.from_numpy(np.ascontiguousarray(Q.T)).requires_grad_(True)
+    dt = Rollout(cfg).dt_of(q)
+    (g,) = torch.autograd.grad(dt, q)
+    nz = torch.nonzero(g)
+    assert set(nz[:, 0].tolist()) == {0}          # basis 0 only
+    assert set(nz[:, 1].tolist()) <= {0, 1, 2, 3, 4}
+    cells = {tuple(r) for r in nz[:, 2:].tolist()}
+    assert 1 <= len(cells) <= 2 and (cfg.nz - 1, cfg.ny - 1, cfg.nx - 1) in cells
+    # FD check of the smooth map
+    h = 1e-7
+    d = torch.zeros_like(q)
+    d[0, :5] = torch.randn(d[0, :5].shape, dtype=q.dtype)
+    roll = Rollout(cfg)
+    fd = (float(roll.dt_of(q.detach() + h * d)) - float(roll.dt_of(q.detach() - h * d))) / (2 * h)
+    assert fd == pytest.approx(float((g * d).sum()), rel=1e-6)
+
+
+def test_channel_state_matches_ic():
+    torch = pytest.importorskip("torch")
+    from hermeshd_gb300.adjoint import channel_perturbation, channel_state
+    cfg = config.poiseuille_2d(nx=8, ny=12)
+    pert = channel_perturbation(cfg, amplitude=1e-3, seed=0, device=torch.device("cpu"))
+    q = channel_state(cfg, pert)
+    Q = ic.channel(cfg, amplitude=1e-3, seed=0)
+    assert np.array_equal(q.numpy(), np.ascontiguousarray(Q.T))
