@@ -349,7 +349,65 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
         "max_rel_l2": hl["max_rel_l2"],
         "note": "HLLC with the stress-augmented point flux is discontinuous at S_M = 0, where an equilibrium "
                 "fluctuating state sits at every face; FP32 and FP64 then pick branches by rounding"}
+    res["adjoint_poiseuille"] = adjoint_poiseuille()
     return res
+
+
+def adjoint_poiseuille(nsteps=200, every=20):
+    """The 64x128 channel (ivis 1, Roe, body force 1e-3, mu = 0.05, velocity
+    perturbation 1e-3 seed 0): gradient of the outflow kinetic energy after
+    200 steps with respect to mu and the perturbation field by the
+    checkpointed adjoint, its wall time, and its agreement with central
+    differences of the same forward map (mu: h = 1e-4 mu; perturbation: one
+    random direction, h = 1e-4)."""
+    import time
+
+    import torch
+
+    from hermeshd_gb300 import config
+    from hermeshd_gb300.adjoint import (Rollout, channel_perturbation, channel_state, outflow_kinetic_energy,
+                                        rollout)
+
+    cfg = config.poiseuille_2d()
+    mu0, p = 0.05, 1.0
+    roll = Rollout(cfg, checkpoint_every=every)
+    pert = channel_perturbation(cfg, 1e-3, 0).requires_grad_(True)
+    mu = torch.tensor(mu0, dtype=torch.float64, device=pert.device, requires_grad=True)
+    # warm-up outside the timed region: context creation and the first launch
+    # of every kernel involved (lazy module loading)
+    pw = pert.detach().clone().requires_grad_(True)
+    cw = torch.tensor(p / mu0, dtype=torch.float64, device=pw.device)
+    outflow_kinetic_energy(rollout(channel_state(cfg, pw), cw, roll, 2), cfg).backward()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    qf = rollout(channel_state(cfg, pert), p / mu, roll, nsteps)
+    L = outflow_kinetic_energy(qf, cfg)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    L.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+
+    def loss(pt, m):
+        q, _, _ = roll.forward(channel_state(cfg, pt), p / m, nsteps)
+        return float(outflow_kinetic_energy(q, cfg))
+
+    hm = 1e-4 * mu0
+    fd_mu = (loss(pert.detach(), mu0 + hm) - loss(pert.detach(), mu0 - hm)) / (2 * hm)
+    g = torch.Generator(device=pert.device).manual_seed(7)
+    D = torch.randn(pert.shape, generator=g, dtype=pert.dtype, device=pert.device) * 1e-3
+    hp = 1e-4
+    fd_p = (loss(pert.detach() + hp * D, mu0) - loss(pert.detach() - hp * D, mu0)) / (2 * hp)
+    adj_mu, adj_p = float(mu.grad), float((D * pert.grad).sum())
+    return {"config": {"grid": "64x128x1", "nbasis": 4, "ivis": 1, "riemann": "Roe (ihllc 2)", "rk": "SSP-RK2",
+                       "steps": nsteps, "checkpoint_every": every, "mu": mu0, "body_force": 1e-3,
+                       "perturbation": "Gaussian cell-average velocity, amplitude 1e-3, seed 0",
+                       "observable": "kinetic energy of the cell column at x = lx (cell averages x dx dy)"},
+            "L": float(L.detach()), "dL_dmu": adj_mu, "dL_dpert_norm": float(pert.grad.norm()),
+            "forward_s": t1 - t0, "backward_s": t2 - t1, "backward_over_forward": (t2 - t1) / (t1 - t0),
+            "fd_dL_dmu": fd_mu, "rel_err_mu_vs_fd": abs(adj_mu - fd_mu) / abs(adj_mu),
+            "fd_dL_dpert_dir": fd_p, "rel_err_pert_vs_fd": abs(adj_p - fd_p) / abs(adj_p),
+            "limiter_events": roll.limiter_events}
 
 
 def ensemble_accuracy(base, nbox=32, steps=20):

@@ -125,10 +125,34 @@ class Rollout:
         return c.cflm_eff / ((vmag + cs_last) * (c.nx / c.lx))
 
     def _dt_grad(self, q):
+        """d dt / dq: nonzero only on the cell averages of the arg-max cell
+        and of the last cell, so the derivative is taken on those two cells."""
         torch = _torch()
+        c = self.cfg
+        with torch.no_grad():
+            a = q[0, :5].reshape(5, -1)
+            rho = a[0]
+            v = a[1:4] / rho
+            cs = torch.sqrt(c.aindex * (a[4] / rho - 0.5 * (v * v).sum(0)))
+            v0 = v.abs().amax(0) + cs
+            ok = (v0 > 0) & (rho > c.rh_mult * c.rh_floor)
+            v0 = torch.where(ok, v0, torch.full_like(v0, -math.inf))
+            imax = int(torch.argmax(v0))
+        ncell = a.shape[1]
+        g = torch.zeros_like(q)
+        if not math.isfinite(float(v0[imax])):
+            return g
         with torch.enable_grad():
-            a = q.detach().clone().requires_grad_(True)
-            (g,) = torch.autograd.grad(self.dt_of(a), a)
+            x = a[:, [imax, ncell - 1]].detach().clone().requires_grad_(True)   # (5, 2)
+            r, m, e = x[0], x[1:4], x[4]
+            vv = m / r
+            csx = torch.sqrt(c.aindex * (e / r - 0.5 * (vv * vv).sum(0)))
+            vmag = vv[:, 0].abs().max() + csx[0]
+            dt = c.cflm_eff / ((vmag + csx[1]) * (c.nx / c.lx))
+            (gx,) = torch.autograd.grad(dt, x)
+        gf = g[0, :5].reshape(5, -1)
+        gf[:, imax] += gx[:, 0]
+        gf[:, ncell - 1] += gx[:, 1]
         return g
 
     def _ddt_stage(self, x, e, lam, dt: float, coll: float) -> float:

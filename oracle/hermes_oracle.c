@@ -1449,3 +1449,8 @@ void orc_noise_sample(unsigned long long seed, unsigned long long step, unsigned
     hermes_philox_normals9(seed, step, stage, kind, site, pt, G9);
     stress_at(&c, (int)kind, site, (int)pt, S6);
 }
+
+/* one Philox-4x32-10 block, for known-answer tests of the generator */
+void orc_philox4x32_10(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]) {
+    hermes_philox4x32_10(ctr, k0, k1, out);
+}

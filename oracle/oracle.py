@@ -83,6 +83,8 @@ def lib():
         L.orc_noise_sample.argtypes = [C.c_ulonglong, C.c_ulonglong, C.c_uint, C.c_uint, C.c_ulonglong, C.c_uint,
                                        C.c_double, C.c_double, np.ctypeslib.ndpointer(dtype=np.float64),
                                        np.ctypeslib.ndpointer(dtype=np.float64)]
+        u32p = np.ctypeslib.ndpointer(dtype=np.uint32)
+        L.orc_philox4x32_10.argtypes = [u32p, C.c_uint32, C.c_uint32, u32p]
         L.orc_test_basis.restype = C.c_double
         L.orc_test_basis.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib = L
@@ -219,3 +221,11 @@ def noise_sample(seed, step, stage, kind, site, pt, eta=1.0, zeta=0.0):
     S = np.zeros(6)
     lib().orc_noise_sample(seed, step, stage, kind, site, pt, eta, zeta, G, S)
     return G, S
+
+
+def philox4x32_10(ctr, key):
+    """One Philox-4x32-10 block: ctr = 4 words, key = 2 words -> 4 words."""
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib().orc_philox4x32_10(c, int(key[0]), int(key[1]), out)
+    return [int(x) for x in out]

@@ -49,3 +49,16 @@ def test_channel_state_matches_ic():
     q = channel_state(cfg, pert)
     Q = ic.channel(cfg, amplitude=1e-3, seed=0)
     assert np.array_equal(q.numpy(), np.ascontiguousarray(Q.T))
+
+
+def test_dt_grad_two_cell_form_equals_full_autograd():
+    torch = pytest.importorskip("torch")
+    from hermeshd_gb300.adjoint import Rollout
+    for seed in (3, 4):
+        cfg = config.Config(nx=5, ny=4, nz=3, nbasis=4, iquad=2)
+        Q = ic.random_smooth(cfg, seed=seed, amp=0.1)
+        q = torch.from_numpy(np.ascontiguousarray(Q.T))
+        r = Rollout(cfg)
+        a = q.clone().requires_grad_(True)
+        (g_ref,) = torch.autograd.grad(r.dt_of(a), a)
+        assert torch.allclose(r._dt_grad(q), g_ref, rtol=1e-14, atol=1e-20)

@@ -69,3 +69,17 @@ def test_counters_give_distinct_streams():
     for i in range(len(variants)):
         for j in range(i + 1, len(variants)):
             assert not np.allclose(variants[i], variants[j])
+
+
+def test_philox_known_answers():
+    """Philox-4x32-10 known-answer vectors of the generator's authors
+    (Random123 kat_vectors: zero, all-ones and pi-digit counters/keys)."""
+    import oracle as O
+    kat = [
+        ((0, 0, 0, 0), (0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+        ((0xffffffff,) * 4, (0xffffffff, 0xffffffff), (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+        ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+         (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1)),
+    ]
+    for ctr, key, want in kat:
+        assert O.philox4x32_10(ctr, key) == list(want)
