@@ -191,7 +191,7 @@ def run_ours(args, rank, ws):
     import numpy as np
     import torch
 
-    from hermeshd_gb300 import config, ic, perfmodel
+    from hermeshd_gb300 import autotune, config, ic, perfmodel
     from hermeshd_gb300.solver import Ensemble, Solver
 
     dev = torch.device("cuda", torch.cuda.current_device())
@@ -202,6 +202,7 @@ def run_ours(args, rank, ws):
     s = Solver(cfg)
     q, q1 = s.from_numpy(Q0), s.new_state()
     s.advance(q, q1, W)
+    tune = autotune.autotune(s, q, steps=3, repeats=2, use_cache=False)
     barrier(ws)
     with ClockSampler(torch.cuda.current_device()) as clk:
         times = time_steps(s, q, q1, K, flush)
@@ -218,7 +219,9 @@ def run_ours(args, rank, ws):
            "config": {"workload": WORKLOAD, "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "nQ": 11, "nbasis": 10,
                       "dof": cfg.dof, "rk_stages": cfg.stages, "l2": "flushed: 256 MiB write before every timed step",
                       "parallelism": "replicas" if ws > 1 else "single GPU", "timing": "CUDA events per step on the kernels' stream"},
-           "clocks": clocks, "gpu_launches": launches_per_step * K}
+           "clocks": clocks, "gpu_launches": launches_per_step * K,
+           "autotune": {"launch": tune["launch"], "tuned_ms_per_step": tune["ms_per_step"],
+                        "default_ms_per_step": tune["default_ms_per_step"], "trials": len(tune["trials"])}}
 
     # ---- end to end through the C ABI with host buffers -----------------
     qh = torch.empty(cfg.shape_c, dtype=torch.float64, pin_memory=True)
@@ -284,7 +287,7 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
     import numpy as np
     import torch
 
-    from hermeshd_gb300 import config, ic
+    from hermeshd_gb300 import autotune, config, ic
     from hermeshd_gb300.solver import Ensemble, Solver
 
     K, W = args.steps, args.warmup
@@ -318,6 +321,7 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
         v[0, 0].fill_(1.0)
         v[0, 4].fill_(1.0 / (base.aindex - 1.0))
     ens.advance(qe, qe1, 2)
+    etune = autotune.autotune(ens, qe, steps=1, repeats=2, use_cache=False)
     Ke = max(2, K // 5)
     times = time_steps(ens, qe, qe1, Ke, flush)
     el = max_over_ranks(sum(times), ws)
@@ -327,7 +331,9 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
         "value": vens, "unit": UNIT, "ms_per_step": 1e3 * el / Ke, "steps": Ke, "dtype": "f32",
         "config": {"boxes": 256, "sizes": "uniform from {16,24,32,48}^3, seed 0", "cells": ens.ncells, "dof": dof,
                    "nbasis": 4, "ivis": 1, "stochastic_stress": True, "rk": "SSP-RK2", "riemann": "Roe (ihllc 2)",
-                   "noise": "kT/(rho dV) = 1e-3, eta = 1, Philox key = realisation id"}}
+                   "noise": "kT/(rho dV) = 1e-3, eta = 1, Philox key = realisation id"},
+        "autotune": {"launch": etune["launch"], "tuned_ms_per_step": etune["ms_per_step"],
+                     "default_ms_per_step": etune["default_ms_per_step"]}}
     ens.close()
     del qe, qe1
     torch.cuda.empty_cache()

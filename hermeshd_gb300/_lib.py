@@ -23,7 +23,13 @@ EXPORTS = ("hermes_abi_version", "hermes_config_size", "hermes_sizes", "hermes_c
            "hermes_rhs", "hermes_euler_stage", "hermes_step", "hermes_advance", "hermes_advance_host",
            "hermes_enqueue_steps", "hermes_profile_enable", "hermes_profile_read",
            "hermes_box_times", "hermes_set_time", "hermes_set_noise_step", "hermes_check", "hermes_rhs_noalloc",
-           "hermes_rhs_vjp", "hermes_stage_vjp")
+           "hermes_rhs_vjp", "hermes_stage_vjp", "hermes_set_launch", "hermes_get_launch")
+
+
+class HermesLaunch(C.Structure):
+    """hermes_launch of include/hermes_gb300.h."""
+    _fields_ = [("face_tpb", C.c_int32), ("dt_tpb", C.c_int32), ("steps_per_graph", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class HermesError(RuntimeError):
@@ -113,6 +119,8 @@ def lib() -> C.CDLL:
         "hermes_rhs_noalloc": (i32, [cfgp, vp, vp, i32, vp, C.c_char_p, C.c_size_t]),
         "hermes_rhs_vjp": (i32, [vp, vp, vp, vp]),
         "hermes_stage_vjp": (i32, [vp, vp, vp, vp, vp, C.c_double, dp]),
+        "hermes_set_launch": (i32, [vp, C.POINTER(HermesLaunch)]),
+        "hermes_get_launch": (i32, [vp, C.POINTER(HermesLaunch)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

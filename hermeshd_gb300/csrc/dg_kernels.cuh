@@ -252,6 +252,7 @@ struct FaceArgs {
     Phys ph;
     const unsigned long long* step;  // noise step counter (device)
     unsigned stage;
+    int tpb;                         // faces per block (32, 64 or 128; 0 = FACE_TPB)
 };
 
 // the numerical flux at one face point from the two traces (after boundary
@@ -388,7 +389,7 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
 
 template <class T, class TB, int DIR, bool NOISE>
 __global__ void __launch_bounds__(FACE_TPB, 4) k_face(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
-    long long gf = (long long)blockIdx.x * FACE_TPB + threadIdx.x;
+    long long gf = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gf >= a.G.nface[DIR]) return;
     const int p = blockIdx.y;
     sfor<TB::NF>([&](auto pp) {
@@ -779,11 +780,12 @@ struct DtArgs {
     Geom G;
     Phys ph;
     BoxState* st;
+    int tpb;   // cells per block (a multiple of 32 up to DT_TPB; 0 = DT_TPB)
 };
 
 template <class T>
 __global__ void __launch_bounds__(DT_TPB) k_mindt(const T* __restrict__ Q, DtArgs a) {
-    const long long gc = (long long)blockIdx.x * DT_TPB + threadIdx.x;
+    const long long gc = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = gc < a.G.ncell;
     int bx = 0;
     double vmag0 = 0.0;

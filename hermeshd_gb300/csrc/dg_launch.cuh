@@ -40,12 +40,13 @@ struct Launch {
     static void face(int dir, const void* Q, void* flux, const FaceArgs& a, cudaStream_t s) {
         const long long n = a.G.nface[dir];
         if (n <= 0) return;
-        dim3 grid((unsigned)((n + FACE_TPB - 1) / FACE_TPB), TB::NF);
+        const int tpb = a.tpb > 0 ? a.tpb : FACE_TPB;
+        dim3 grid((unsigned)((n + tpb - 1) / tpb), TB::NF);
         const T* q = static_cast<const T*>(Q);
         T* f = static_cast<T*>(flux);
-        if (dir == 0) k_face<T, TB, 0, NOISE><<<grid, FACE_TPB, 0, s>>>(q, f, a);
-        else if (dir == 1) k_face<T, TB, 1, NOISE><<<grid, FACE_TPB, 0, s>>>(q, f, a);
-        else k_face<T, TB, 2, NOISE><<<grid, FACE_TPB, 0, s>>>(q, f, a);
+        if (dir == 0) k_face<T, TB, 0, NOISE><<<grid, tpb, 0, s>>>(q, f, a);
+        else if (dir == 1) k_face<T, TB, 1, NOISE><<<grid, tpb, 0, s>>>(q, f, a);
+        else k_face<T, TB, 2, NOISE><<<grid, tpb, 0, s>>>(q, f, a);
     }
     template <bool NOISE>
     static void cell(const void* Qin, const void* Q0, void* out, const void* flux, const CellArgs& a, cudaStream_t s) {
@@ -56,8 +57,9 @@ struct Launch {
     }
     static void mindt(const void* Q, const DtArgs& a, cudaStream_t s) {
         if (a.G.ncell <= 0) return;
-        const unsigned nb = (unsigned)((a.G.ncell + DT_TPB - 1) / DT_TPB);
-        k_mindt<T><<<nb, DT_TPB, 0, s>>>(static_cast<const T*>(Q), a);
+        const int tpb = a.tpb > 0 ? a.tpb : DT_TPB;
+        const unsigned nb = (unsigned)((a.G.ncell + tpb - 1) / tpb);
+        k_mindt<T><<<nb, tpb, 0, s>>>(static_cast<const T*>(Q), a);
     }
 };
 

@@ -27,6 +27,7 @@ namespace {
 struct GraphEntry {
     const void* q;
     const void* q1;
+    int steps;
     cudaGraphExec_t exec;
 };
 
@@ -130,6 +131,8 @@ struct hermes_ctx {
     std::vector<cudaEvent_t> pool;
     double prof_ms[6] = {0, 0, 0, 0, 0, 0};
     long long prof_n[6] = {0, 0, 0, 0, 0, 0};
+    // launch shape (hermes_set_launch); 0 = the compiled defaults
+    int face_tpb = 0, dt_tpb = 0, graph_steps = 1;
     // adjoint scratch, allocated on first use
     AdjFn adj = nullptr;
     double* d_tadj = nullptr;   // trace adjoints: 2 x the face-flux size
@@ -278,7 +281,7 @@ void enq_limit(hermes_ctx* c, void* q) {
     }
 }
 void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
-    FaceArgs a{c->G, c->ph, c->d_step, stage};
+    FaceArgs a{c->G, c->ph, c->d_step, stage, c->face_tpb};
     for (int d = 0; d < 3; ++d) {
         ProfScope ps(c, 2 + d);
         c->K.face(d, q, c->d_flux, a, c->stream);
@@ -296,7 +299,7 @@ void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, un
     enq_cell(c, qin, q0, out, MODE_STAGE, comb, stage);
 }
 void enq_mindt(hermes_ctx* c, const void* q, bool advance) {
-    DtArgs a{c->G, c->ph, c->d_st};
+    DtArgs a{c->G, c->ph, c->d_st, c->dt_tpb};
     ProfScope ps(c, 0);
     c->K.mindt(q, a, c->stream);
     const int nb = c->G.nbox, tpb = 128;
@@ -351,12 +354,13 @@ int read_back(hermes_ctx* c, double* t, double* dt) {
     return HERMES_OK;
 }
 
-int get_graph(hermes_ctx* c, void* q, void* q1, cudaGraphExec_t* out) {
+// a graph of `steps` whole steps on (q, q1), captured on first use
+int get_graph(hermes_ctx* c, void* q, void* q1, int steps, cudaGraphExec_t* out) {
     for (auto& g : c->graphs)
-        if (g.q == q && g.q1 == q1) { *out = g.exec; return HERMES_OK; }
+        if (g.q == q && g.q1 == q1 && g.steps == steps) { *out = g.exec; return HERMES_OK; }
     cudaGraph_t graph;
     HCK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enq_step(c, q, q1);
+    for (int k = 0; k < steps; ++k) enq_step(c, q, q1);
     cudaError_t le = cudaGetLastError();
     cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
     if (le != cudaSuccess) { if (ee == cudaSuccess) cudaGraphDestroy(graph); return cuda_fail(c, "launch in capture", le); }
@@ -366,7 +370,7 @@ int get_graph(hermes_ctx* c, void* q, void* q1, cudaGraphExec_t* out) {
     cudaGraphDestroy(graph);
     HCK(c, ie);
     if (c->graphs.size() >= 8) destroy_graphs(c);
-    c->graphs.push_back(GraphEntry{q, q1, exec});
+    c->graphs.push_back(GraphEntry{q, q1, steps, exec});
     *out = exec;
     return HERMES_OK;
 }
@@ -565,10 +569,20 @@ int enqueue_steps_impl(hermes_ctx* c, void* q, void* q1, int nsteps) {
         for (int s = 0; s < nsteps; ++s) enq_step(c, q, q1);
         return launch_status(c);
     }
-    cudaGraphExec_t exec;
-    int rc = get_graph(c, q, q1, &exec);
-    if (rc) return rc;
-    for (int s = 0; s < nsteps; ++s) HCK(c, cudaGraphLaunch(exec, c->stream));
+    const int k = c->graph_steps > 1 ? c->graph_steps : 1;
+    if (nsteps >= k && k > 1) {
+        cudaGraphExec_t exec;
+        int rc = get_graph(c, q, q1, k, &exec);
+        if (rc) return rc;
+        for (int s = 0; s + k <= nsteps; s += k) HCK(c, cudaGraphLaunch(exec, c->stream));
+    }
+    const int rest = k > 1 ? nsteps % k : nsteps;
+    if (rest > 0) {
+        cudaGraphExec_t exec;
+        int rc = get_graph(c, q, q1, 1, &exec);
+        if (rc) return rc;
+        for (int s = 0; s < rest; ++s) HCK(c, cudaGraphLaunch(exec, c->stream));
+    }
     return HERMES_OK;
 }
 
@@ -597,6 +611,33 @@ int hermes_enqueue_steps(hermes_ctx* c, void* q, void* q1, int nsteps) {
     int rc = enter(c);
     if (rc) return rc;
     return leave(c, enqueue_steps_impl(c, q, q1, nsteps));
+}
+
+int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
+    if (!c || !l) return fail(c, HERMES_ERR_ARG, "null argument");
+    const int f = l->face_tpb, d = l->dt_tpb, g = l->steps_per_graph;
+    if (f != 0 && f != 32 && f != 64 && f != 128) return fail(c, HERMES_ERR_ARG, "face_tpb must be 0, 32, 64 or 128");
+    if (d != 0 && (d < 32 || d > DT_TPB || d % 32)) return fail(c, HERMES_ERR_ARG, "dt_tpb must be 0 or a multiple of 32 up to 256");
+    if (g < 0 || g > 64) return fail(c, HERMES_ERR_ARG, "steps_per_graph must be in 0..64");
+    if (f != c->face_tpb || d != c->dt_tpb) {
+        // captured graphs hold the old launch shape
+        HCK(c, cudaSetDevice(c->device));
+        HCK(c, cudaStreamSynchronize(c->stream));
+        destroy_graphs(c);
+    }
+    c->face_tpb = f;
+    c->dt_tpb = d;
+    c->graph_steps = g > 0 ? g : 1;
+    return HERMES_OK;
+}
+
+int hermes_get_launch(hermes_ctx* c, hermes_launch* l) {
+    if (!c || !l) return fail(c, HERMES_ERR_ARG, "null argument");
+    l->face_tpb = c->face_tpb > 0 ? c->face_tpb : FACE_TPB;
+    l->dt_tpb = c->dt_tpb > 0 ? c->dt_tpb : DT_TPB;
+    l->steps_per_graph = c->graph_steps;
+    l->reserved = 0;
+    return HERMES_OK;
 }
 
 int hermes_profile_enable(hermes_ctx* c, int enable) {

@@ -150,6 +150,19 @@ int hermes_advance_host(hermes_ctx *ctx, void *q_host, int nsteps, double *t, do
  * without synchronising; t and dt stay on the device (hermes_box_times). */
 int hermes_enqueue_steps(hermes_ctx *ctx, void *q, void *q1, int nsteps);
 
+/* Launch shape of a context, chosen by the autotuner (hermeshd_gb300/autotune.py)
+ * or by hand.  No counterpart in the reference (its loops have no launch
+ * shape).  Zero fields select the compiled defaults.  Changing face_tpb or
+ * dt_tpb synchronises the context's stream and drops its captured graphs. */
+typedef struct hermes_launch {
+    int32_t face_tpb;        /* faces per block of the face kernels: 32, 64 or 128 (default 128) */
+    int32_t dt_tpb;          /* cells per block of the CFL reduction: multiple of 32 up to 256 (default 256) */
+    int32_t steps_per_graph; /* whole steps per CUDA graph in hermes_advance/hermes_enqueue_steps: 1..64 (default 1) */
+    int32_t reserved;        /* 0 */
+} hermes_launch;
+int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
+int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);
+
 /* Per-kernel device timing with CUDA events on the context's stream.  While
  * enabled, steps run without the graph and every kernel launch is bracketed
  * by an event pair.  hermes_profile_read synchronises, returns accumulated

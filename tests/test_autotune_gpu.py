@@ -1,0 +1,75 @@
+"""Launch shapes and the autotuner: every launch shape gives the same result
+bit for bit, bad shapes are rejected, and tuning leaves the context where a
+fresh one would start (time and stochastic-stress step counter)."""
+import numpy as np
+import pytest
+
+from hermeshd_gb300 import config, ic
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def test_launch_defaults_and_validation():
+    from hermeshd_gb300._lib import HermesError
+    from hermeshd_gb300.solver import Solver
+    s = Solver(config.sod_1d(nx=64))
+    assert s.get_launch() == {"face_tpb": 128, "dt_tpb": 256, "steps_per_graph": 1}
+    for bad in ({"face_tpb": 96}, {"face_tpb": 256}, {"dt_tpb": 48}, {"dt_tpb": 512}, {"steps_per_graph": 65}):
+        with pytest.raises(HermesError):
+            s.set_launch(**bad)
+    s.set_launch(face_tpb=32, dt_tpb=64, steps_per_graph=4)
+    assert s.get_launch() == {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 4}
+
+
+@pytest.mark.parametrize("mk", [lambda: config.isentropic_vortex_2d(n=12),
+                                lambda: config.fh_box(6, precision="fp32", seed=3)])
+def test_every_launch_shape_is_bit_identical(mk):
+    from hermeshd_gb300.solver import Solver
+    cfg = mk()
+    Q = ic.isentropic_vortex(cfg) if cfg.nbasis == 10 else ic.equilibrium(cfg)
+    ref = None
+    for shape in ({}, {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 3},
+                  {"face_tpb": 64, "dt_tpb": 128, "steps_per_graph": 2}):
+        s = Solver(cfg)
+        s.set_launch(**shape)
+        q, q1 = s.from_numpy(Q), s.new_state()
+        t, dt = s.advance(q, q1, 7)
+        out = (s.to_numpy(q), t, dt)
+        if ref is None:
+            ref = out
+        else:
+            assert np.array_equal(out[0], ref[0]) and out[1] == ref[1] and out[2] == ref[2], shape
+
+
+def test_autotune_resets_state_and_caches(tmp_path, monkeypatch):
+    from hermeshd_gb300 import autotune
+    from hermeshd_gb300.solver import Ensemble
+    monkeypatch.setenv("HERMES_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
+    base = config.fh_box(8, precision="fp32", seed=0)
+    dims = [(8, 8, 8), (6, 6, 6), (10, 10, 10)]
+    dx = base.lx / 8
+    lengths = [(n * dx,) * 3 for (n, _, _) in dims]
+    ens = Ensemble(base, dims, lengths, seeds=[0, 1, 2])
+    q = ens.new_state()
+    for i in range(ens.nbox):
+        v = ens.box_view(q, i)
+        v[0, 0].fill_(1.0)
+        v[0, 4].fill_(1.0 / (base.aindex - 1.0))
+    r = autotune.autotune(ens, q, steps=2, repeats=2)
+    assert not r["cached"] and r["ms_per_step"] <= r["default_ms_per_step"]
+    assert set(r["launch"]) == {"face_tpb", "dt_tpb", "steps_per_graph"}
+    assert ens.get_launch() == r["launch"]
+    # tuning stepped copies of q; the context's time and noise counter are reset
+    qa, qa1 = q.clone(), ens.new_state()
+    ens.advance(qa, qa1, 5)
+    fresh = Ensemble(base, dims, lengths, seeds=[0, 1, 2])
+    qb, qb1 = q.clone(), fresh.new_state()
+    fresh.advance(qb, qb1, 5)
+    assert _torch().equal(qa, qb)
+    r2 = autotune.autotune(fresh, q, steps=2, repeats=2)
+    assert r2["cached"] and r2["launch"] == r["launch"]
