@@ -28,6 +28,7 @@ from typing import Optional
 
 import numpy as np
 
+from . import checkpoint as _ckpt
 from . import ic as _ic
 from .config import Config
 from .solver import Solver
@@ -51,16 +52,23 @@ class Hermeshd:
         self.icid: int = 3
         self.solver: Optional[Solver] = None
         self._dev = None
+        # checkpoint switches of input.f90:99-103
+        self.iwrite, self.iread, self.resuming, self.fpre, self.datadir = 0, 0, False, "Qout", "data"
 
     # ---- configuration (compile-time constants in the reference) --------
-    def configure(self, cfg: Config, icid: Optional[int] = None):
+    def configure(self, cfg: Config, icid: Optional[int] = None, iwrite: int = 0, iread: int = 0,
+                  resuming: bool = False, fpre: str = "Qout", datadir: str = "data"):
         """Select the problem: src/input.f90 and src/params.f90 at run time.
         icid follows initialcon.f90:41-69 (1/2 isentropic vortex v0/v1,
-        3/4 Sod v0/v1); other problems set their own initial state."""
+        3/4 Sod v0/v1); other problems set their own initial state.
+        iwrite = 1 writes a checkpoint at every output (odd/even dump ids);
+        iread = 1 or 2 starts from that dump, keeping its clock if resuming
+        (input.f90:99-103)."""
         cfg.validate()
         self.cfg = cfg
         if icid is not None:
             self.icid = icid
+        self.iwrite, self.iread, self.resuming, self.fpre, self.datadir = iwrite, iread, resuming, fpre, datadir
         if self.solver is not None:
             self.solver.close()
             self.solver = None
@@ -98,11 +106,19 @@ class Hermeshd:
         now = time.time()
         _set0d(t_start, now)
         _set0d(dtout, cfg.tf / cfg.ntout)                      # hermeshd.f90:84
-        Q = {1: lambda: _ic.isentropic_vortex(cfg, 0), 2: lambda: _ic.isentropic_vortex(cfg, 1),
-             3: lambda: _ic.sod(cfg), 4: lambda: _ic.sod(cfg)}.get(self.icid, lambda: _ic.equilibrium(cfg))()
+        if self.iread:
+            # initialize.f90:396-438 set_ic_from_file
+            Q, tr, dtr, nr = _ckpt.restart(self.datadir, cfg, self.iread, _get0d(dtout), self.resuming, self.fpre)
+            if self.resuming:
+                _set0d(t, tr)
+                _set0d(dt, dtr)
+                _set0d(nout, nr)
+        else:
+            Q = {1: lambda: _ic.isentropic_vortex(cfg, 0), 2: lambda: _ic.isentropic_vortex(cfg, 1),
+                 3: lambda: _ic.sod(cfg), 4: lambda: _ic.sod(cfg)}.get(self.icid, lambda: _ic.equilibrium(cfg))()
         self._write(q_io, Q)
         _set0d(t1, time.time())
-        s.set_time(0.0)
+        s.set_time(_get0d(t))
         return t, dt
 
     def _write(self, dst, Qf):
@@ -127,10 +143,14 @@ class Hermeshd:
         return tn, dtn
 
     def generate_output(self, q_r, t, dt, t1, dtout, nout):
-        """hermeshd.f90:206-266: the output cadence (VTK writing is out of
-        scope; the cadence counter advances as in the reference)."""
-        if _get0d(t) >= _get0d(nout) * _get0d(dtout):
-            _set0d(nout, int(_get0d(nout)) + 1)
+        """hermeshd.f90:206-266: when t passes the next output time, advance
+        nout and, with iwrite, write the checkpoint with the odd/even dump id
+        (hermeshd.f90:248-252)."""
+        if _get0d(t) > _get0d(nout) * _get0d(dtout):
+            n = int(_get0d(nout)) + 1
+            _set0d(nout, n)
+            if self.iwrite == 1:
+                _ckpt.write_dump(self.datadir, q_r, _get0d(t), _get0d(dt), n, prefix=self.fpre)
         return nout
 
     def cleanup(self, t_start):

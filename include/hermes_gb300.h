@@ -150,6 +150,20 @@ int hermes_advance_host(hermes_ctx *ctx, void *q_host, int nsteps, double *t, do
  * without synchronising; t and dt stay on the device (hermes_box_times). */
 int hermes_enqueue_steps(hermes_ctx *ctx, void *q, void *q1, int nsteps);
 
+/* Text checkpoints of writeQ / readQ (initialize.f90:474-565), host memory
+ * only (no context, no GPU).  q: FP64 Q(nx,ny,nz,nQ,nbasis), Fortran order.
+ * Records: one per (basis, variable, k, j) with the nx values of the row,
+ * then "t dt nout mpi_nx mpi_ny mpi_nz".  The writer prints %.16E (exact FP64
+ * round trip); the reader accepts Fortran list-directed input (blank or comma
+ * separators, continuation lines, r*c repeats, null values, D exponents, a
+ * slash ending a list), so files the reference wrote read back.  mpi_dims: 3
+ * values (NULL = 1 1 1 on write).  err (errlen bytes, may be NULL) receives a
+ * message on failure; a short or malformed file returns HERMES_ERR_SHAPE. */
+int hermes_checkpoint_write(const char *path, const double *q, int32_t nx, int32_t ny, int32_t nz, int32_t nbasis,
+                            double t, double dt, int32_t nout, const int32_t *mpi_dims, char *err, size_t errlen);
+int hermes_checkpoint_read(const char *path, double *q, int32_t nx, int32_t ny, int32_t nz, int32_t nbasis,
+                           double *t, double *dt, int32_t *nout, int32_t *mpi_dims, char *err, size_t errlen);
+
 /* Launch shape of a context, chosen by the autotuner (hermeshd_gb300/autotune.py)
  * or by hand.  No counterpart in the reference (its loops have no launch
  * shape).  Zero fields select the compiled defaults.  Changing face_tpb or
