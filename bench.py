@@ -356,6 +356,8 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
         "note": "HLLC with the stress-augmented point flux is discontinuous at S_M = 0, where an equilibrium "
                 "fluctuating state sits at every face; FP32 and FP64 then pick branches by rounding"}
     res["adjoint_poiseuille"] = adjoint_poiseuille()
+    res["derived_fields"] = derived_fields(cfg64, Q0, flush)
+    res["checkpoint_io"] = checkpoint_io(cfg64, Q0)
     return res
 
 
@@ -414,6 +416,76 @@ def adjoint_poiseuille(nsteps=200, every=20):
             "fd_dL_dmu": fd_mu, "rel_err_mu_vs_fd": abs(adj_mu - fd_mu) / abs(adj_mu),
             "fd_dL_dpert_dir": fd_p, "rel_err_pert_vs_fd": abs(adj_p - fd_p) / abs(adj_p),
             "limiter_events": roll.limiter_events}
+
+
+def derived_fields(cfg, Q0, flush, reps=20):
+    """The VTK derived fields (all 14 variables, float32) of the 128x128 vortex
+    state on the device: time per launch by CUDA events on the kernels'
+    stream, L2 flushed before each launch, and HBM throughput from the
+    algorithmic bytes (8 of the 11 variables' coefficients read, FP64; 14
+    float32 values written per sub-cell)."""
+    import torch
+
+    from hermeshd_gb300.output import VARIABLES, derived
+    from hermeshd_gb300.solver import Solver
+
+    s = Solver(cfg)
+    q = s.from_numpy(Q0)
+    st = torch.cuda.ExternalStream(s.cuda_stream)
+    res = {}
+    for nvtk in (1, 2):
+        out, _ = derived(s, q, VARIABLES, nvtk)
+        ms = []
+        for _ in range(reps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            derived(s, q, VARIABLES, nvtk, out=out)
+            b.record(st)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        ms_avg = sum(ms) / len(ms)
+        nbytes = cfg.ncells * 8 * cfg.nbasis * 8 + cfg.ncells * nvtk ** 3 * len(VARIABLES) * 4
+        gbs = nbytes / (ms_avg * 1e-3) / 1e9
+        res[f"nvtk{nvtk}"] = {"ms_per_launch": ms_avg, "algorithmic_bytes": nbytes, "achieved_gbs": gbs,
+                              "frac_hbm": gbs / peaks()["hbm_gbs"], "peak_source": peaks()["source"]}
+    s.close()
+    return res
+
+
+def checkpoint_io(cfg, Q0, reps=3):
+    """writeQ/readQ text checkpoints of the vortex state (FP64, 1.8 M values)
+    through the library: device -> pinned host copy + multi-threaded format
+    + write, and read + parse; MB of FP64 state per second."""
+    import tempfile
+    import time
+
+    import numpy as np
+    import torch
+
+    from hermeshd_gb300 import checkpoint
+    from hermeshd_gb300.solver import Solver
+
+    s = Solver(cfg)
+    q = s.from_numpy(Q0)
+    mb = Q0.size * 8 / 1e6
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, checkpoint.checkpoint_name())
+        tw, tr = [], []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            checkpoint.write(path, q, 1.0, 0.01, 2)
+            tw.append(time.perf_counter() - t0)
+            t0 = time.perf_counter()
+            R, *_ = checkpoint.read(path, cfg)
+            tr.append(time.perf_counter() - t0)
+        size = os.path.getsize(path)
+        exact = bool(np.array_equal(R, s.to_numpy(q)))
+    s.close()
+    return {"state_mb": mb, "file_mb": size / 1e6, "write_mb_s": mb / min(tw), "read_mb_s": mb / min(tr),
+            "round_trip_bit_exact": exact, "host_threads": os.cpu_count()}
 
 
 def ensemble_accuracy(base, nbox=32, steps=20):

@@ -24,13 +24,19 @@ EXPORTS = ("hermes_abi_version", "hermes_config_size", "hermes_sizes", "hermes_c
            "hermes_enqueue_steps", "hermes_profile_enable", "hermes_profile_read",
            "hermes_box_times", "hermes_set_time", "hermes_set_noise_step", "hermes_check", "hermes_rhs_noalloc",
            "hermes_rhs_vjp", "hermes_stage_vjp", "hermes_set_launch", "hermes_get_launch",
-           "hermes_checkpoint_write", "hermes_checkpoint_read")
+           "hermes_checkpoint_write", "hermes_checkpoint_read", "hermes_derived")
 
 
 class HermesLaunch(C.Structure):
     """hermes_launch of include/hermes_gb300.h."""
     _fields_ = [("face_tpb", C.c_int32), ("dt_tpb", C.c_int32), ("steps_per_graph", C.c_int32),
                 ("reserved", C.c_int32)]
+
+
+class HermesOutputUnits(C.Structure):
+    """hermes_output_units of include/hermes_gb300.h."""
+    _fields_ = [("n0", C.c_double), ("v0", C.c_double), ("t0", C.c_double), ("te0", C.c_double),
+                ("eV_per_K", C.c_double)]
 
 
 class HermesError(RuntimeError):
@@ -124,6 +130,7 @@ def lib() -> C.CDLL:
         "hermes_get_launch": (i32, [vp, C.POINTER(HermesLaunch)]),
         "hermes_checkpoint_write": (i32, [C.c_char_p, vp, i32, i32, i32, i32, C.c_double, C.c_double, i32,
                                           C.POINTER(C.c_int32), C.c_char_p, C.c_size_t]),
+        "hermes_derived": (i32, [vp, vp, vp, i32, C.c_uint32, C.POINTER(HermesOutputUnits)]),
         "hermes_checkpoint_read": (i32, [C.c_char_p, vp, i32, i32, i32, i32, dp, dp, C.POINTER(C.c_int32),
                                          C.POINTER(C.c_int32), C.c_char_p, C.c_size_t]),
     }

@@ -158,6 +158,9 @@ def emit(path: str) -> None:
         nf, npg = iq * iq, iq ** 3
         out.append(f"template <> struct Tab<{nb}, {iq}> {{")
         out.append(f"    static constexpr int NB = {nb}, NQD = {iq}, NF = {nf}, NPG = {npg}, NPGE = {6 * nf};")
+        degs = ", ".join("{" + ", ".join(str(d) for d in fam) + "}" for fam in FAMILIES[(nb, iq)])
+        out.append(f"    // Legendre degree of basis function b along axis a (x, y, z)")
+        out.append(f"    static constexpr int DEG(int b, int a) {{ const int t[{nb}][3] = {{{degs}}}; return t[b][a]; }}")
         for name, rows in T.items():
             if name in ("CB", "W2", "W3"):
                 vals = ", ".join(_lit(v) for v in rows)

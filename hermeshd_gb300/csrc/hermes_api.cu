@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "dg_launch.cuh"
+#include "dg_output.cuh"
 #include "hermes_gb300.h"
 
 using namespace hermes;
@@ -611,6 +612,28 @@ int hermes_enqueue_steps(hermes_ctx* c, void* q, void* q1, int nsteps) {
     int rc = enter(c);
     if (rc) return rc;
     return leave(c, enqueue_steps_impl(c, q, q1, nsteps));
+}
+
+int hermes_derived(hermes_ctx* c, const void* q, float* out, int32_t nvtk, uint32_t mask,
+                   const hermes_output_units* u) {
+    if (!c || !q || !out || !u) return fail(c, HERMES_ERR_ARG, "null argument");
+    if (nvtk < 1 || nvtk > 4) return fail(c, HERMES_ERR_ARG, "nvtk must be 1..4 (basis_funcs.f90:100-116)");
+    if (mask == 0 || mask >= (1u << DV_N)) return fail(c, HERMES_ERR_ARG, "mask selects none or unknown variables");
+    if (c->G.nbox != 1) return fail(c, HERMES_ERR_CONFIG, "derived fields are written per grid: use one box");
+    DerivedFn fn;
+    if (!derived_launcher(c->cfg.precision, c->cfg.nbasis, &fn)) return fail(c, HERMES_ERR_CONFIG, "no derived-field kernel");
+    DerivedArgs a{};
+    a.G = c->G;
+    a.aindex = c->cfg.aindex;
+    a.n0 = u->n0; a.v0 = u->v0; a.t0 = u->t0; a.te0 = u->te0; a.eV_per_K = u->eV_per_K;
+    a.nvtk = nvtk;
+    a.mask = mask;
+    for (int v = 0, n = 0; v < DV_N; ++v) a.slot[v] = ((mask >> v) & 1u) ? n++ : 0;
+    int rc = enter(c);
+    if (rc) return rc;
+    cudaError_t e = fn(q, out, a, c->stream);
+    if (e != cudaSuccess) return leave(c, cuda_fail(c, "derived-field launch", e));
+    return leave(c, HERMES_OK);
 }
 
 int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {

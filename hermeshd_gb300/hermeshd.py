@@ -30,6 +30,7 @@ import numpy as np
 
 from . import checkpoint as _ckpt
 from . import ic as _ic
+from . import output as _out
 from .config import Config
 from .solver import Solver
 
@@ -54,21 +55,25 @@ class Hermeshd:
         self._dev = None
         # checkpoint switches of input.f90:99-103
         self.iwrite, self.iread, self.resuming, self.fpre, self.datadir = 0, 0, False, "Qout", "data"
+        self.vtk, self.outdir, self.nvtk = False, "data", 1
 
     # ---- configuration (compile-time constants in the reference) --------
     def configure(self, cfg: Config, icid: Optional[int] = None, iwrite: int = 0, iread: int = 0,
-                  resuming: bool = False, fpre: str = "Qout", datadir: str = "data"):
+                  resuming: bool = False, fpre: str = "Qout", datadir: str = "data", vtk: bool = False,
+                  outdir: str = "data", nvtk: int = 1):
         """Select the problem: src/input.f90 and src/params.f90 at run time.
         icid follows initialcon.f90:41-69 (1/2 isentropic vortex v0/v1,
         3/4 Sod v0/v1); other problems set their own initial state.
         iwrite = 1 writes a checkpoint at every output (odd/even dump ids);
         iread = 1 or 2 starts from that dump, keeping its clock if resuming
-        (input.f90:99-103)."""
+        (input.f90:99-103).  vtk = True writes the VTK derived fields of
+        output_vtk at every output into outdir (nvtk sub-cells per axis)."""
         cfg.validate()
         self.cfg = cfg
         if icid is not None:
             self.icid = icid
         self.iwrite, self.iread, self.resuming, self.fpre, self.datadir = iwrite, iread, resuming, fpre, datadir
+        self.vtk, self.outdir, self.nvtk = vtk, outdir, nvtk
         if self.solver is not None:
             self.solver.close()
             self.solver = None
@@ -144,11 +149,16 @@ class Hermeshd:
 
     def generate_output(self, q_r, t, dt, t1, dtout, nout):
         """hermeshd.f90:206-266: when t passes the next output time, advance
-        nout and, with iwrite, write the checkpoint with the odd/even dump id
+        nout, write the VTK derived fields (output_vtk) when vtk is set and,
+        with iwrite, the checkpoint with the odd/even dump id
         (hermeshd.f90:248-252)."""
         if _get0d(t) > _get0d(nout) * _get0d(dtout):
             n = int(_get0d(nout)) + 1
             _set0d(nout, n)
+            if self.vtk:
+                s = self._need()
+                q = s.from_numpy(q_r) if isinstance(q_r, np.ndarray) else q_r
+                _out.output_vtk(s, q, n, outdir=self.outdir, nvtk=self.nvtk)
             if self.iwrite == 1:
                 _ckpt.write_dump(self.datadir, q_r, _get0d(t), _get0d(dt), n, prefix=self.fpre)
         return nout

@@ -164,6 +164,24 @@ int hermes_checkpoint_write(const char *path, const double *q, int32_t nx, int32
 int hermes_checkpoint_read(const char *path, double *q, int32_t nx, int32_t ny, int32_t nz, int32_t nbasis,
                            double *t, double *dt, int32_t *nout, int32_t *mpi_dims, char *err, size_t errlen);
 
+/* Derived fields of the VTK output (output.f90:14-317), on the device.  The
+ * state q of a one-grid context is evaluated at nvtk^3 sub-points per cell
+ * (nvtk 1..4, basis_funcs.f90:88-200) and the variables selected by mask
+ * (bit v = variable v below) are written to the device array out as float32,
+ * one array of nx*ny*nz*nvtk^3 values per selected variable in variable
+ * order, sub-cells x fastest.  Variables: 0 density*n0, 1 log10 density*n0,
+ * 2-4 velocity*v0, 5 temperature (K), 6 internal energy density, 7 total
+ * energy density, 8 entropy density, 9 pressure, 10-12 diagonal stresses,
+ * 13 vorticity.  (The reference never fills the internal-energy array and
+ * writes the previous variable's values under that name; here it is
+ * E - rho v^2/2.) */
+typedef struct hermes_output_units {
+    double n0, v0, t0, te0, eV_per_K;   /* params.f90:80-94 */
+} hermes_output_units;
+#define HERMES_DERIVED_NVARS 14
+int hermes_derived(hermes_ctx *ctx, const void *q, float *out, int32_t nvtk, uint32_t mask,
+                   const hermes_output_units *units);
+
 /* Launch shape of a context, chosen by the autotuner (hermeshd_gb300/autotune.py)
  * or by hand.  No counterpart in the reference (its loops have no launch
  * shape).  Zero fields select the compiled defaults.  Changing face_tpb or
