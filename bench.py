@@ -420,20 +420,27 @@ def adjoint_poiseuille(nsteps=200, every=20):
 
 def derived_fields(cfg, Q0, flush, reps=20):
     """The VTK derived fields (all 14 variables, float32) of the 128x128 vortex
-    state on the device: time per launch by CUDA events on the kernels'
-    stream, L2 flushed before each launch, and HBM throughput from the
-    algorithmic bytes (8 of the 11 variables' coefficients read, FP64; 14
-    float32 values written per sub-cell)."""
+    state (nvtk 1 and 2) and of a 512x512 vortex (230 MB, above L2) on the
+    device: time per launch by CUDA events on the kernels' stream, L2 flushed
+    before each launch, and HBM throughput from the algorithmic bytes (8 of
+    the 11 variables' coefficients read, FP64; 14 float32 values written per
+    sub-cell)."""
     import torch
 
     from hermeshd_gb300.output import VARIABLES, derived
     from hermeshd_gb300.solver import Solver
 
-    s = Solver(cfg)
-    q = s.from_numpy(Q0)
-    st = torch.cuda.ExternalStream(s.cuda_stream)
+    from hermeshd_gb300 import config as _config
+
     res = {}
-    for nvtk in (1, 2):
+    for n, nvtk in ((cfg.nx, 1), (cfg.nx, 2), (512, 1)):
+        c = cfg if n == cfg.nx else _config.isentropic_vortex_2d(n=n)
+        s = Solver(c)
+        if n == cfg.nx:
+            q = s.from_numpy(Q0)
+        else:
+            q = s.init_state(s.new_state(), 2)
+        st = torch.cuda.ExternalStream(s.cuda_stream)
         out, _ = derived(s, q, VARIABLES, nvtk)
         ms = []
         for _ in range(reps):
@@ -446,11 +453,12 @@ def derived_fields(cfg, Q0, flush, reps=20):
             b.synchronize()
             ms.append(a.elapsed_time(b))
         ms_avg = sum(ms) / len(ms)
-        nbytes = cfg.ncells * 8 * cfg.nbasis * 8 + cfg.ncells * nvtk ** 3 * len(VARIABLES) * 4
+        nbytes = c.ncells * 8 * c.nbasis * 8 + c.ncells * nvtk ** 3 * len(VARIABLES) * 4
         gbs = nbytes / (ms_avg * 1e-3) / 1e9
-        res[f"nvtk{nvtk}"] = {"ms_per_launch": ms_avg, "algorithmic_bytes": nbytes, "achieved_gbs": gbs,
-                              "frac_hbm": gbs / peaks()["hbm_gbs"], "peak_source": peaks()["source"]}
-    s.close()
+        res[f"vortex{n}_nvtk{nvtk}"] = {"ms_per_launch": ms_avg, "algorithmic_bytes": nbytes, "achieved_gbs": gbs,
+                                        "frac_hbm": gbs / peaks()["hbm_gbs"], "peak_source": peaks()["source"]}
+        s.close()
+        del q, out
     return res
 
 

@@ -24,7 +24,8 @@ EXPORTS = ("hermes_abi_version", "hermes_config_size", "hermes_sizes", "hermes_c
            "hermes_enqueue_steps", "hermes_profile_enable", "hermes_profile_read",
            "hermes_box_times", "hermes_set_time", "hermes_set_noise_step", "hermes_check", "hermes_rhs_noalloc",
            "hermes_rhs_vjp", "hermes_stage_vjp", "hermes_set_launch", "hermes_get_launch",
-           "hermes_checkpoint_write", "hermes_checkpoint_read", "hermes_derived")
+           "hermes_checkpoint_write", "hermes_checkpoint_read", "hermes_derived",
+           "hermes_init_state")
 
 
 class HermesLaunch(C.Structure):
@@ -130,6 +131,7 @@ def lib() -> C.CDLL:
         "hermes_get_launch": (i32, [vp, C.POINTER(HermesLaunch)]),
         "hermes_checkpoint_write": (i32, [C.c_char_p, vp, i32, i32, i32, i32, C.c_double, C.c_double, i32,
                                           C.POINTER(C.c_int32), C.c_char_p, C.c_size_t]),
+        "hermes_init_state": (i32, [vp, vp, i32, C.c_uint64]),
         "hermes_derived": (i32, [vp, vp, vp, i32, C.c_uint32, C.POINTER(HermesOutputUnits)]),
         "hermes_checkpoint_read": (i32, [C.c_char_p, vp, i32, i32, i32, i32, dp, dp, C.POINTER(C.c_int32),
                                          C.POINTER(C.c_int32), C.c_char_p, C.c_size_t]),

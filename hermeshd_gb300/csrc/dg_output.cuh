@@ -23,7 +23,7 @@
 namespace hermes {
 
 constexpr int DV_N = 14;
-constexpr int DERIVED_TPB = 256;
+constexpr int DERIVED_TPB = 128;
 
 struct DerivedArgs {
     Geom G;                       // one box

@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "dg_init.cuh"
 #include "dg_launch.cuh"
 #include "dg_output.cuh"
 #include "hermes_gb300.h"
@@ -113,7 +114,9 @@ struct hermes_ctx {
     cudaStream_t user_stream = nullptr;  // the caller's stream; work is ordered against it both ways
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     std::vector<Box> h_boxes;
+    std::vector<double> h_len;           // lx, ly, lz per box
     Box* d_boxes = nullptr;
+    double* d_len = nullptr;
     Geom G{};
     Phys ph{};
     BoxState* d_st = nullptr;
@@ -207,8 +210,10 @@ Phys make_phys(const hermes_config& c) {
 
 // geometry of nbox boxes; sizes in elements
 void make_boxes(const hermes_config& c, int nbox, const int32_t* dims, const double* lengths, const uint64_t* seeds,
-                int nf, std::vector<Box>& boxes, long long& ncell, long long nface[3], size_t& q_elems, size_t& flux_elems) {
+                int nf, std::vector<Box>& boxes, std::vector<double>& len, long long& ncell, long long nface[3],
+                size_t& q_elems, size_t& flux_elems) {
     boxes.resize(nbox);
+    len.resize(3 * (size_t)nbox);
     ncell = 0;
     nface[0] = nface[1] = nface[2] = 0;
     for (int i = 0; i < nbox; ++i) {
@@ -227,6 +232,7 @@ void make_boxes(const hermes_config& c, int nbox, const int32_t* dims, const dou
         const double L[3] = {lengths ? lengths[3 * i] : c.lx, lengths ? lengths[3 * i + 1] : c.ly,
                              lengths ? lengths[3 * i + 2] : c.lz};
         for (int d = 0; d < 3; ++d) b.di[d] = (double)b.n[d] / L[d];   // initialize.f90:317-319
+        for (int d = 0; d < 3; ++d) len[3 * (size_t)i + d] = L[d];
         b.cflm = c.cflm > 0 ? c.cflm : default_cflm(c.iquad);
         b.seed = seeds ? seeds[i] : c.seed + (uint64_t)i;
         for (int d = 0; d < 3; ++d) {
@@ -393,7 +399,7 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     cudaGetDevice(&c->device);
     c->ph = make_phys(*cfg);
     long long ncell, nface[3];
-    make_boxes(*cfg, nbox, dims, lengths, seeds, c->K.nf, c->h_boxes, ncell, nface, c->q_elems, c->flux_elems);
+    make_boxes(*cfg, nbox, dims, lengths, seeds, c->K.nf, c->h_boxes, c->h_len, ncell, nface, c->q_elems, c->flux_elems);
     c->G.nbox = nbox;
     c->G.ncell = ncell;
     for (int d = 0; d < 3; ++d) c->G.nface[d] = nface[d];
@@ -445,9 +451,10 @@ int hermes_sizes(const hermes_config* cfg, size_t* q_elems, size_t* scratch_byte
     KernelSet K;
     pick_kernels(*cfg, K);
     std::vector<Box> boxes;
+    std::vector<double> len;
     long long ncell, nface[3];
     size_t qe, fe;
-    make_boxes(*cfg, 1, nullptr, nullptr, nullptr, K.nf, boxes, ncell, nface, qe, fe);
+    make_boxes(*cfg, 1, nullptr, nullptr, nullptr, K.nf, boxes, len, ncell, nface, qe, fe);
     if (q_elems) *q_elems = qe;
     if (scratch_bytes) *scratch_bytes = fe * K.elem_size;
     return HERMES_OK;
@@ -491,6 +498,7 @@ int hermes_destroy(hermes_ctx* c) {
     cudaFree(c->d_mu);
     cudaFree(c->d_part);
     cudaFree(c->d_sum);
+    cudaFree(c->d_len);
     delete c;
     return HERMES_OK;
 }
@@ -612,6 +620,26 @@ int hermes_enqueue_steps(hermes_ctx* c, void* q, void* q1, int nsteps) {
     int rc = enter(c);
     if (rc) return rc;
     return leave(c, enqueue_steps_impl(c, q, q1, nsteps));
+}
+
+int hermes_init_state(hermes_ctx* c, void* q, int32_t icid, uint64_t seed) {
+    if (!c || !q) return fail(c, HERMES_ERR_ARG, "null argument");
+    if (icid < 0 || icid > 7) return fail(c, HERMES_ERR_ARG, "icid must be 0..7 (initialcon.f90:41-69)");
+    int rc = enter(c);
+    if (rc) return rc;
+    if (!c->d_len) {
+        if (cudaMalloc(&c->d_len, sizeof(double) * c->h_len.size()) != cudaSuccess) {
+            cudaGetLastError();
+            return leave(c, fail(c, HERMES_ERR_ALLOC, "box lengths"));
+        }
+        HCK(c, cudaMemcpyAsync(c->d_len, c->h_len.data(), sizeof(double) * c->h_len.size(), cudaMemcpyHostToDevice,
+                               c->stream));
+    }
+    InitArgs a{c->d_boxes, c->d_len, c->G.nbox, c->G.ncell, c->cfg.nbasis, icid,
+               c->cfg.aindex, c->cfg.rh_floor, c->cfg.T_floor, c->cfg.P_base, (unsigned long long)seed};
+    cudaError_t e = init_launch(c->cfg.precision, q, a, c->stream);
+    if (e != cudaSuccess) return leave(c, cuda_fail(c, "initial-state launch", e));
+    return leave(c, HERMES_OK);
 }
 
 int hermes_derived(hermes_ctx* c, const void* q, float* out, int32_t nvtk, uint32_t mask,

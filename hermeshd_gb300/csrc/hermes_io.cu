@@ -107,6 +107,24 @@ int next_value(Reader& r, double& v, std::string& bad) {
         v = r.repeat_val;
         return 1;
     }
+    // fast path: a plain number followed by a separator
+    for (;;) {
+        r.skip_blanks();
+        if (r.p < r.end && *r.p == '\n') { ++r.p; ++r.line; continue; }
+        break;
+    }
+    if (r.p < r.end && *r.p != ',' && *r.p != '/') {
+        char* e = nullptr;
+        const double x = std::strtod(r.p, &e);
+        if (e != r.p && e <= r.end &&
+            (e == r.end || *e == ' ' || *e == '\t' || *e == '\r' || *e == '\n' || *e == ',' || *e == '/')) {
+            r.p = e;
+            r.skip_blanks();
+            if (r.p < r.end && *r.p == ',') ++r.p;
+            v = x;
+            return 1;
+        }
+    }
     std::string tok;
     int kind = 0;
     if (!r.token(tok, kind)) return -1;

@@ -62,8 +62,9 @@ class Hermeshd:
                   resuming: bool = False, fpre: str = "Qout", datadir: str = "data", vtk: bool = False,
                   outdir: str = "data", nvtk: int = 1):
         """Select the problem: src/input.f90 and src/params.f90 at run time.
-        icid follows initialcon.f90:41-69 (1/2 isentropic vortex v0/v1,
-        3/4 Sod v0/v1); other problems set their own initial state.
+        icid follows initialcon.f90:41-69 (0 jet, 1/2 isentropic vortex
+        v0/v1, 3/4 Sod v0/v1, 5-7 fluid at rest), built on the device; other
+        problems set their own initial state.
         iwrite = 1 writes a checkpoint at every output (odd/even dump ids);
         iread = 1 or 2 starts from that dump, keeping its clock if resuming
         (input.f90:99-103).  vtk = True writes the VTK derived fields of
@@ -118,10 +119,15 @@ class Hermeshd:
                 _set0d(t, tr)
                 _set0d(dt, dtr)
                 _set0d(nout, nr)
+        elif 0 <= self.icid <= 7:
+            # set_ic (initialcon.f90:20-72) built on the device
+            dq = q_io if not isinstance(q_io, np.ndarray) else s.new_state()
+            s.init_state(dq, self.icid)
+            Q = s.to_numpy(dq) if isinstance(q_io, np.ndarray) else None
         else:
-            Q = {1: lambda: _ic.isentropic_vortex(cfg, 0), 2: lambda: _ic.isentropic_vortex(cfg, 1),
-                 3: lambda: _ic.sod(cfg), 4: lambda: _ic.sod(cfg)}.get(self.icid, lambda: _ic.equilibrium(cfg))()
-        self._write(q_io, Q)
+            Q = _ic.equilibrium(cfg)
+        if Q is not None:
+            self._write(q_io, Q)
         _set0d(t1, time.time())
         s.set_time(_get0d(t))
         return t, dt

@@ -23,8 +23,9 @@ def empty_state(cfg: Config, dtype=np.float64) -> np.ndarray:
 
 def cell_centres(cfg: Config):
     """params.f90:212-227 xc/yc/zc with the domain centred at the origin
-    (initialize.f90:310-326): xc(i) = -lx/2 + (i - 1/2) dx."""
-    dx, dy, dz = cfg.lx / cfg.nx, cfg.ly / cfg.ny, cfg.lz / cfg.nz
+    (initialize.f90:310-326): xc(i) = -lx/2 + (i - 1/2) dx, dx = 1/dxi,
+    dxi = nx/lx."""
+    dx, dy, dz = 1.0 / (cfg.nx / cfg.lx), 1.0 / (cfg.ny / cfg.ly), 1.0 / (cfg.nz / cfg.lz)
     xc = -cfg.lx / 2 + (np.arange(1, cfg.nx + 1) - 0.5) * dx
     yc = -cfg.ly / 2 + (np.arange(1, cfg.ny + 1) - 0.5) * dy
     zc = -cfg.lz / 2 + (np.arange(1, cfg.nz + 1) - 0.5) * dz
@@ -47,12 +48,18 @@ def _set_hydro(Q, dn, vx, vy, vz, pr, gamma):
     Q[:, :, :, EN, 0] = pr / (gamma - 1.0) + 0.5 * dn * (vx ** 2 + vy ** 2 + vz ** 2)
 
 
-def sod(cfg: Config, p_hi: float = 1.0, p_lo: float = 0.1, rh_hi: float = 1.0, rh_lo: float = 0.125) -> np.ndarray:
-    """initialcon.f90:190-235 sod_shock_tube_1d, version 0 (diaphragm at
-    xc = 0, i.e. x = 0.5 of [0, 1])."""
+def sod(cfg: Config, p_hi: float = None, p_lo: float = None, rh_hi: float = 1.0, rh_lo: float = 0.125,
+        ver: int = 0) -> np.ndarray:
+    """initialcon.f90:190-235 sod_shock_tube_1d: high state where xc + yc <= 0
+    (version 1) or xc <= 0 (version 0, the diaphragm at x = 0.5 of [0, 1]);
+    pressures 1 and 0.1 times P_base."""
+    p_hi = 1.0 * cfg.P_base if p_hi is None else p_hi
+    p_lo = 0.1 * cfg.P_base if p_lo is None else p_lo
     Q = _background(cfg)
     xc, yc, zc = cell_centres(cfg)
     X = np.broadcast_to(xc[:, None, None], (cfg.nx, cfg.ny, cfg.nz))
+    if ver == 1:
+        X = X + np.broadcast_to(yc[None, :, None], (cfg.nx, cfg.ny, cfg.nz))
     left = X <= 0
     dn = np.where(left, rh_hi, rh_lo)
     pr = np.where(left, p_hi, p_lo)
@@ -179,3 +186,77 @@ def ten_moment_stress(cfg: Config, Q: np.ndarray, p: float = 1.0, amp: float = 0
     for v, (a, b) in zip((PXX, PYY, PZZ, PXY, PXZ, PYZ), ((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2))):
         Q[:, :, :, v, 0] = m[a] * m[b] / rho + (p if a == b else 0.0) + amp * rng.standard_normal(rho.shape)
     return Q
+
+
+# ---- the remaining problems of set_ic (initialcon.f90:41-69) ---------------
+_M0, _M1, _W0, _W1 = 0xD2511F53, 0xCD9E8D57, 0x9E3779B9, 0xBB67AE85
+JET_TAG = 0x4A455400   # counter word 2 of the jet's uniforms
+
+
+def philox_uniform(seed: int, site: np.ndarray, tag: int) -> np.ndarray:
+    """Uniform numbers in [0, 1) from Philox-4x32-10 (Salmon et al., SC'11),
+    counter (site_lo, site_hi, tag, 0), key = seed: the top 53 bits of the
+    first two output words.  The device initialiser draws the same numbers."""
+    mask = np.uint64(0xFFFFFFFF)
+    site = np.asarray(site, dtype=np.uint64)
+    c0, c1 = site & mask, site >> np.uint64(32)
+    c2 = np.full_like(site, np.uint64(tag))
+    c3 = np.zeros_like(site)
+    k0, k1 = np.uint64(seed & 0xFFFFFFFF), np.uint64((seed >> 32) & 0xFFFFFFFF)
+    for _ in range(10):
+        p0 = np.uint64(_M0) * c0
+        p1 = np.uint64(_M1) * c2
+        hi0, lo0 = p0 >> np.uint64(32), p0 & mask
+        hi1, lo1 = p1 >> np.uint64(32), p1 & mask
+        c0, c1, c2, c3 = hi1 ^ c1 ^ k0, lo1, hi0 ^ c3 ^ k1, lo0
+        k0 = (k0 + np.uint64(_W0)) & mask
+        k1 = (k1 + np.uint64(_W1)) & mask
+    m = (c0 << np.uint64(21)) | (c1 >> np.uint64(11))
+    return m.astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def hydro_jet(cfg: Config, seed: int = 0, beta: float = 1.0, beta2: float = 0.005) -> np.ndarray:
+    """initialcon.f90:79-114 hydro_jet: dn = 1, T = T_floor, a jet
+    m_x = beta dn / cosh(20 yc / lyu) with a random transverse kick
+    beta2 (r - 1/2) / cosh(20 yc / lyu)^2, lyu = ly/2.  The reference draws r
+    with Fortran's random_number (unseeded); here r comes from
+    philox_uniform(seed, cell) so the state is reproducible."""
+    Q = _background(cfg)
+    xc, yc, zc = cell_centres(cfg)
+    dn, te = 1.0, cfg.T_floor
+    pr = te * dn
+    cell = np.arange(cfg.nx * cfg.ny * cfg.nz, dtype=np.uint64).reshape(cfg.nz, cfg.ny, cfg.nx).transpose(2, 1, 0)
+    rnum = philox_uniform(seed, cell, JET_TAG) - 0.5
+    lyu = cfg.ly / 2.0
+    ch = np.broadcast_to(np.cosh(20 * yc / lyu)[None, :, None], (cfg.nx, cfg.ny, cfg.nz))
+    smx = beta * dn / ch
+    smy = beta2 * rnum / ch ** 2
+    Q[:, :, :, RH, 0] = dn
+    Q[:, :, :, MX, 0] = smx
+    Q[:, :, :, MY, 0] = smy
+    Q[:, :, :, MZ, 0] = 0.0
+    Q[:, :, :, EN, 0] = pr / (cfg.aindex - 1.0) + 0.5 * (smx ** 2 + smy ** 2 + 0.0 ** 2) / dn
+    return Q
+
+
+def fluid_at_rest(cfg: Config) -> np.ndarray:
+    """initialcon.f90:244-361 poiseuille_flow / pipe_cylinder_2d: dn = 1,
+    T = T_floor, v = 0 (their inflow and cylinder boundary arrays are never
+    applied by the reference's step)."""
+    Q = _background(cfg)
+    z = np.zeros((cfg.nx, cfg.ny, cfg.nz))
+    _set_hydro(Q, z + 1.0, z, z, z, z + cfg.T_floor, cfg.aindex)
+    return Q
+
+
+def from_icid(cfg: Config, icid: int, seed: int = 0) -> np.ndarray:
+    """set_ic (initialcon.f90:20-72) by problem id."""
+    if icid == 0:
+        return hydro_jet(cfg, seed)
+    if icid in (1, 2):
+        return isentropic_vortex(cfg, icid - 1)
+    if icid in (3, 4):
+        return sod(cfg, ver=icid - 3)
+    if icid in (5, 6, 7):
+        return fluid_at_rest(cfg)
+    raise ValueError(f"unknown icid {icid}")

@@ -158,6 +158,12 @@ class Solver:
                                         C.byref(dd)), self.ctx)
         return tt.value, dd.value
 
+    def init_state(self, q, icid: int, seed: int = 0):
+        """Fill q on the device with the initial state of set_ic problem icid
+        (0 jet, 1/2 vortex v0/v1, 3/4 Sod v0/v1, 5-7 fluid at rest)."""
+        check(lib().hermes_init_state(self.ctx, self._ptr(q), int(icid), int(seed)), self.ctx)
+        return q
+
     # ---- launch shape ---------------------------------------------------------
     def get_launch(self) -> dict:
         l = _lib.HermesLaunch()

@@ -164,6 +164,14 @@ int hermes_checkpoint_write(const char *path, const double *q, int32_t nx, int32
 int hermes_checkpoint_read(const char *path, double *q, int32_t nx, int32_t ny, int32_t nz, int32_t nbasis,
                            double *t, double *dt, int32_t *nout, int32_t *mpi_dims, char *err, size_t errlen);
 
+/* Initial state of set_ic (initialcon.f90:20-361) built on the device for
+ * every box of the context: icid 0 hydrodynamic jet (its random kick from
+ * Philox-4x32-10 keyed by seed, where the reference uses Fortran's unseeded
+ * random_number), 1/2 isentropic vortex versions 0/1, 3/4 Sod shock tube
+ * versions 0/1, 5-7 fluid at rest (Poiseuille and cylinder problems).  Cell
+ * averages only; all other coefficients are written zero. */
+int hermes_init_state(hermes_ctx *ctx, void *q, int32_t icid, uint64_t seed);
+
 /* Derived fields of the VTK output (output.f90:14-317), on the device.  The
  * state q of a one-grid context is evaluated at nvtk^3 sub-points per cell
  * (nvtk 1..4, basis_funcs.f90:88-200) and the variables selected by mask
