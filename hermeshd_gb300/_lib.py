@@ -64,6 +64,7 @@ class HermesConfig(C.Structure):
         ("eta_sd", C.c_double), ("zeta_sd", C.c_double),
         ("seed", C.c_uint64),
         ("body_force", C.c_double),
+        ("inflow_u", C.c_double), ("inflow_rho", C.c_double), ("inflow_p", C.c_double),
     ]
 
 
@@ -83,6 +84,7 @@ def to_c(cfg: Config) -> HermesConfig:
     c.eta_sd, c.zeta_sd = cfg.eta_sd, cfg.zeta_sd
     c.seed = cfg.seed & ((1 << 64) - 1)
     c.body_force = cfg.body_force
+    c.inflow_u, c.inflow_rho, c.inflow_p = cfg.inflow_u, cfg.inflow_rho, cfg.inflow_pressure
     return c
 
 

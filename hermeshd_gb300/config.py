@@ -16,7 +16,7 @@ from typing import Optional, Tuple
 
 NQ = 11                      # params.f90:47
 VARS = ("rh", "mx", "my", "mz", "en", "pxx", "pyy", "pzz", "pxy", "pxz", "pyz")  # params.f90:42-46
-BC_CODES = {"periodic": 0, "outflow": 1, "wall": 2, "noslip": 3}
+BC_CODES = {"periodic": 0, "outflow": 1, "wall": 2, "noslip": 3, "inflow": 4}
 SUPPORTED_BASES = ((4, 2), (8, 2), (10, 3))          # (nbasis, iquad) with a CUDA instantiation
 ORACLE_BASES = ((4, 2), (8, 2), (10, 3), (27, 3))    # the oracle also runs (27, 3)
 
@@ -116,6 +116,11 @@ class Config:
     seed: int = 0
     # body force in x (new: the reference drives its channel by inflow)
     body_force: float = 0.0
+    # parabolic x-low inflow (xlobc = "inflow"; boundary.f90:568-612): peak
+    # velocity, density and pressure (<= 0: rho * T_floor, as poiseuille_flow)
+    inflow_u: float = 0.3
+    inflow_rho: float = 1.0
+    inflow_p: float = 0.0
     # precision of the bulk arithmetic: "fp64" or "fp32"
     precision: str = "fp64"
     # simulation end time and output cadence (input.f90 tf, ntout)
@@ -150,6 +155,10 @@ class Config:
         return self.cflm if self.cflm > 0 else default_cflm(self.iquad)
 
     @property
+    def inflow_pressure(self) -> float:
+        return self.inflow_p if self.inflow_p > 0 else self.inflow_rho * self.T_floor
+
+    @property
     def bc(self) -> Tuple[int, ...]:
         return tuple(bc_code(s) for s in (self.xlobc, self.xhibc, self.ylobc, self.yhibc, self.zlobc, self.zhibc))
 
@@ -168,6 +177,8 @@ class Config:
             raise ValueError("ihllc in {0 central/LLF, 1 HLLC, 2 Roe}")
         if self.precision not in ("fp64", "fp32"):
             raise ValueError("precision must be 'fp64' or 'fp32'")
+        if "inflow" in (self.xhibc, self.ylobc, self.yhibc, self.zlobc, self.zhibc):
+            raise ValueError("the inflow boundary is defined for the x-low face only")
 
 
 # ---------------------------------------------------------------------------

@@ -322,6 +322,20 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
             for (int v = 0; v < NQ; ++v) qL[v] = T(0);
         } else {
             for (int v = 0; v < NQ; ++v) qL[v] = qR[v];
+            if (DIR == 0 && code == BC_INFLOW) {
+                // boundary.f90:568-612: rho, m_x, E of the parabolic profile at the
+                // face row's cell centre yc(j); m_y = m_z = 0; the stresses copied
+                const double lyd = -(ph.inflow_ly / 2.0);
+                const double yc = lyd + (j + 0.5) * (1.0 / B.di[1]);
+                const double yp = yc - lyd;
+                const double vx = 4 * ph.inflow_u * yp * (ph.inflow_ly - yp) / (ph.inflow_ly * ph.inflow_ly);
+                const double den = ph.inflow_rho;
+                qL[RH] = T(den);
+                qL[MX] = T(den * vx);
+                qL[MY] = T(0);
+                qL[MZ] = T(0);
+                qL[EN] = T(ph.inflow_p / ph.aindm1 + 0.5 * den * (vx * vx));
+            }
             if (code == BC_NOSLIP) { qL[MX] = T(0); qL[MY] = T(0); qL[MZ] = T(0); }
             else if (code == BC_WALL) { qL[MN] = T(0); }
             else if (code == BC_OUTFLOW) {

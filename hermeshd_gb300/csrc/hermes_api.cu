@@ -177,7 +177,10 @@ std::string check_config(const hermes_config& c) {
     if (c.ieos != 1 && c.ieos != 2) return "ieos must be 1 or 2";
     if (c.iorder != 2 && c.iorder != 3) return "iorder must be 2 or 3";
     for (int i = 0; i < 6; ++i)
-        if (c.bc[i] < 0 || c.bc[i] > 3) return "boundary codes must be 0..3";
+        if (c.bc[i] < 0 || c.bc[i] > 4) return "boundary codes must be 0..4";
+    for (int i = 1; i < 6; ++i)
+        if (c.bc[i] == HERMES_BC_INFLOW) return "the inflow boundary is defined for the x-low face only";
+    if (c.bc[0] == HERMES_BC_INFLOW && !(c.inflow_rho > 0)) return "inflow density must be positive";
     if (!(c.lx > 0 && c.ly > 0 && c.lz > 0)) return "domain lengths must be positive";
     return "";
 }
@@ -201,6 +204,10 @@ Phys make_phys(const hermes_config& c) {
     p.eta_sd = c.eta_sd;
     p.zeta_sd = c.zeta_sd;
     p.body_force = c.body_force;
+    p.inflow_u = c.inflow_u;
+    p.inflow_rho = c.inflow_rho;
+    p.inflow_p = c.inflow_p;
+    p.inflow_ly = c.ly;
     p.ivis = c.ivis;
     p.ieos = c.ieos;
     p.ihllc = c.ihllc;
@@ -389,6 +396,10 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     std::string msg = check_config(*cfg);
     if (!msg.empty()) { fprintf(stderr, "hermes_create: %s\n", msg.c_str()); return HERMES_ERR_CONFIG; }
     if (nbox < 1) return HERMES_ERR_ARG;
+    if ((nbox > 1 || dims) && cfg->bc[0] == HERMES_BC_INFLOW) {
+        fprintf(stderr, "hermes_create: the inflow boundary takes a single grid\n");
+        return HERMES_ERR_CONFIG;
+    }
     if (dims)
         for (int i = 0; i < 3 * nbox; ++i)
             if (dims[i] < 1) return HERMES_ERR_CONFIG;
@@ -778,6 +789,7 @@ std::string adjoint_unsupported(const hermes_config& c, int nbox) {
     if (c.llns) return "the adjoint does not model the stochastic stress";
     if (c.ivis != 0 && c.ivis != 1) return "the adjoint supports ivis 0 and 1";
     if (c.ieos != 1) return "the adjoint supports ieos 1";
+    if (c.bc[0] == HERMES_BC_INFLOW) return "the adjoint does not model the inflow boundary";
     for (int d = 0; d < 3; ++d)
         if ((c.bc[2 * d] == HERMES_BC_PERIODIC) != (c.bc[2 * d + 1] == HERMES_BC_PERIODIC))
             return "the adjoint needs both or neither end of a direction periodic";

@@ -14,7 +14,7 @@ namespace hermes {
 
 constexpr int NQ = 11;  // params.f90:47
 enum Var { RH = 0, MX, MY, MZ, EN, PXX, PYY, PZZ, PXY, PXZ, PYZ };
-enum Bc { BC_PERIODIC = 0, BC_OUTFLOW = 1, BC_WALL = 2, BC_NOSLIP = 3 };
+enum Bc { BC_PERIODIC = 0, BC_OUTFLOW = 1, BC_WALL = 2, BC_NOSLIP = 3, BC_INFLOW = 4 };
 
 // device error flags (plain stores; read by the host after a step)
 enum Flag { FLAG_NONFINITE = 1 };
@@ -47,6 +47,7 @@ struct Phys {
     double aindex, aindm1, rh_floor, T_floor, P_floor, rh_mult;
     double coll, colvis, P_1, P_base;
     double eta_sd, zeta_sd, body_force;
+    double inflow_u, inflow_rho, inflow_p, inflow_ly;   // parabolic x-low inflow (BC_INFLOW)
     int ivis, ieos, ihllc, llns;
 };
 

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define HERMES_ABI_VERSION 1
+#define HERMES_ABI_VERSION 2
 
 typedef enum hermes_status {
     HERMES_OK = 0,
@@ -45,8 +45,11 @@ typedef enum hermes_status {
 } hermes_status;
 
 /* boundary condition codes: boundary.f90:789-880 ('periodic', 'outflow',
- * 'wall', 'noslip'; any other name selects periodic there, and here) */
-enum { HERMES_BC_PERIODIC = 0, HERMES_BC_OUTFLOW = 1, HERMES_BC_WALL = 2, HERMES_BC_NOSLIP = 3 };
+ * 'wall', 'noslip'; any other name selects periodic there, and here), and
+ * the parabolic inflow of boundary_custom (boundary.f90:568-612 x_bc_inflow /
+ * set_xlobc_inflow), which the reference defines but does not select: x-low
+ * face only, one grid. */
+enum { HERMES_BC_PERIODIC = 0, HERMES_BC_OUTFLOW = 1, HERMES_BC_WALL = 2, HERMES_BC_NOSLIP = 3, HERMES_BC_INFLOW = 4 };
 
 /* The run-time form of the reference's compile-time configuration
  * (src/input.f90, src/params.f90, tests/<problem>/input_*.f90). */
@@ -73,6 +76,9 @@ typedef struct hermes_config {
     double eta_sd, zeta_sd;    /* stochastic stress amplitudes per unit normal */
     uint64_t seed;             /* Philox key of the stochastic stress */
     double body_force;         /* uniform x body force (no reference counterpart) */
+    double inflow_u;           /* HERMES_BC_INFLOW: peak velocity ux_amb of the profile 4u y(ly-y)/ly^2 */
+    double inflow_rho;         /* HERMES_BC_INFLOW: density */
+    double inflow_p;           /* HERMES_BC_INFLOW: pressure */
 } hermes_config;
 
 typedef struct hermes_ctx hermes_ctx;

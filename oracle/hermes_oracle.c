@@ -766,6 +766,22 @@ static void apply_bc(const orc_ctx *c, int code, int lo, int mom, int na, int nb
             }
             for (int v = 0; v < NQ; ++v)
                 for (int p = 0; p < nf; ++p) qe[BI(a, na, b, nbb, p, nf, v)] = qi[BI(a, na, b, nbb, p, nf, v)];
+            if (code == ORC_BC_INFLOW && mom == MX && lo) {
+                /* boundary.f90:568-612 x_bc_inflow with the profile of
+                 * set_xlobc_inflow: yp = yc(j) - lyd, vx = 4 u yp (ly - yp)/ly^2 */
+                const double ly = c->p.ly, lyd = -(ly / 2.0);
+                const double yc = lyd + (a + 0.5) * (1.0 / (c->ny / ly));
+                const double yp = yc - lyd;
+                const double vx = 4 * c->p.inflow_u * yp * (ly - yp) / (ly * ly);
+                const double den = c->p.inflow_rho, pres = c->p.inflow_p;
+                for (int p = 0; p < nf; ++p) {
+                    qe[BI(a, na, b, nbb, p, nf, RH)] = den;
+                    qe[BI(a, na, b, nbb, p, nf, MX)] = den * vx;
+                    qe[BI(a, na, b, nbb, p, nf, MY)] = 0.0;
+                    qe[BI(a, na, b, nbb, p, nf, MZ)] = 0.0;
+                    qe[BI(a, na, b, nbb, p, nf, EN)] = pres / (c->p.aindex - 1.0) + 0.5 * den * (vx * vx);
+                }
+            }
             if (code == ORC_BC_NOSLIP) {
                 for (int v = MX; v <= MZ; ++v)
                     for (int p = 0; p < nf; ++p) qe[BI(a, na, b, nbb, p, nf, v)] = 0.0;

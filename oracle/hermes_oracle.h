@@ -28,7 +28,7 @@ extern "C" {
 enum { ORC_NQ = 11, ORC_NBASTOT = 30 };
 
 /* boundary condition codes, boundary.f90:789-880 (unknown names -> periodic) */
-enum { ORC_BC_PERIODIC = 0, ORC_BC_OUTFLOW = 1, ORC_BC_WALL = 2, ORC_BC_NOSLIP = 3 };
+enum { ORC_BC_PERIODIC = 0, ORC_BC_OUTFLOW = 1, ORC_BC_WALL = 2, ORC_BC_NOSLIP = 3, ORC_BC_INFLOW = 4 };
 
 typedef struct orc_params {
     int nx, ny, nz;          /* cells (input.f90 nx,ny,nz with mpi_n* = 1) */
@@ -50,6 +50,7 @@ typedef struct orc_params {
     double eta_sd, zeta_sd;  /* stochastic stress amplitudes (already scaled) */
     unsigned long long seed; /* Philox key for the stochastic stress */
     double body_force;       /* uniform x body force (no reference counterpart) */
+    double inflow_u, inflow_rho, inflow_p;   /* x-low inflow profile (boundary.f90:568-612) */
 } orc_params;
 
 typedef struct orc_ctx orc_ctx;

@@ -34,6 +34,7 @@ class OrcParams(C.Structure):
         ("llns", C.c_int), ("pad_", C.c_int),
         ("eta_sd", C.c_double), ("zeta_sd", C.c_double), ("seed", C.c_ulonglong),
         ("body_force", C.c_double),
+        ("inflow_u", C.c_double), ("inflow_rho", C.c_double), ("inflow_p", C.c_double),
     ]
 
 
@@ -105,6 +106,7 @@ def params_from_config(cfg) -> OrcParams:
     p.llns = int(cfg.llns)
     p.eta_sd, p.zeta_sd, p.seed = cfg.eta_sd, cfg.zeta_sd, cfg.seed
     p.body_force = cfg.body_force
+    p.inflow_u, p.inflow_rho, p.inflow_p = cfg.inflow_u, cfg.inflow_rho, cfg.inflow_pressure
     return p
 
 

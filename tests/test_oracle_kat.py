@@ -128,3 +128,18 @@ def test_tgv_symmetry_planes_sit_on_hllc_discontinuity():
         O.Oracle(cfg).advance(Qp, 50)
         sens = np.linalg.norm(Q - Qp) / np.linalg.norm(Q)
         assert lo <= sens < hi, (perturb, sens)
+
+
+def test_inflow_boundary_drives_a_parabolic_stream():
+    """x-low inflow (boundary.f90:568-612): fluid at rest in a no-slip channel
+    gains mass through the inlet, and the x-momentum next to the inlet follows
+    the profile's symmetry about the channel axis and peaks there."""
+    cfg = config.Config(nx=16, ny=8, nz=1, lx=2.0, ly=1.0, nbasis=4, iquad=2, ivis=1, coll=20.0, colvis=1.0,
+                        xlobc="inflow", xhibc="wall", ylobc="noslip", yhibc="noslip", inflow_u=0.3, inflow_p=1.0,
+                        ihllc=2)
+    Q = ic.channel(cfg, amplitude=0.0)
+    m0 = Q[:, :, :, 0, 0].sum()
+    O.Oracle(cfg).advance(Q, 40)
+    assert Q[:, :, :, 0, 0].sum() > m0
+    mx = Q[0, :, 0, 1, 0]
+    assert np.allclose(mx, mx[::-1], rtol=1e-9, atol=1e-14) and mx.argmax() in (3, 4) and mx.min() > 0

@@ -47,6 +47,18 @@ RHS_CASES = {
     "nb10_2d_roe_walls_ivis1": (config.Config(nx=6, ny=5, nz=1, nbasis=10, iquad=3, ihllc=2, ivis=1, coll=2.0,
                                               colvis=1.0, xlobc="wall", xhibc="wall"), 0.5),
     "nb8_3d_central_only": (config.Config(nx=4, ny=4, nz=3, nbasis=8, iquad=2, ihllc=0), 0.0),
+    # Murnaghan-Tait equation of state (ieos 2), with the HLLC sound speed's stale 1/rho (flux.f90:533-534)
+    "nb4_2d_tait_hllc_walls": (config.Config(nx=6, ny=5, nz=1, nbasis=4, iquad=2, ieos=2, P_1=0.05, P_base=1.0,
+                                             xlobc="wall", xhibc="noslip"), 0.0),
+    "nb10_2d_tait_roe": (config.Config(nx=5, ny=5, nz=1, nbasis=10, iquad=3, ieos=2, P_1=0.05, P_base=1.0,
+                                       ihllc=2), 0.0),
+    # parabolic x-low inflow (boundary.f90:568-612)
+    "nb4_2d_inflow_noslip": (config.Config(nx=6, ny=8, nz=1, nbasis=4, iquad=2, ivis=1, coll=3.0, colvis=1.0,
+                                           xlobc="inflow", xhibc="wall", ylobc="noslip", yhibc="noslip",
+                                           inflow_u=0.3, inflow_p=1.0), 0.5),
+    "nb10_2d_inflow_roe": (config.Config(nx=5, ny=6, nz=1, nbasis=10, iquad=3, ihllc=2, xlobc="inflow",
+                                         xhibc="noslip", ylobc="wall", yhibc="wall", inflow_u=0.5,
+                                         inflow_rho=1.2, inflow_p=0.8), 0.0),
     # Grad closure (ivis 3, E_ij form)
     "nb4_3d_grad": (config.Config(nx=5, ny=4, nz=3, nbasis=4, iquad=2, ivis=3, coll=1.5), 1.0),
     "nb10_2d_grad_roe": (config.Config(nx=5, ny=6, nz=1, nbasis=10, iquad=3, ivis=3, coll=0.5, ihllc=2), 1.0),
@@ -116,6 +128,13 @@ STEP_CASES = {
     "sod_256_rk2_roe": (lambda: config.sod_1d(nx=256, ihllc=2), lambda c: ic.sod(c)),
     "grad_rk2_split_source_nb4": (lambda: config.Config(nx=6, ny=5, nz=4, nbasis=4, iquad=2, ivis=3, coll=2.0, iorder=2),
                                   lambda c: ic.ten_moment_stress(c, ic.random_smooth(c, seed=9, amp=0.05), p=1.0, amp=0.01)),
+    "tait_rk2_nb4_hllc": (lambda: config.Config(nx=12, ny=10, nz=1, nbasis=4, iquad=2, ieos=2, P_1=0.05, P_base=1.0),
+                          lambda c: ic.random_smooth(c, seed=4, amp=0.05)),
+    "channel_inflow_rk2_nb4": (lambda: config.Config(nx=16, ny=8, nz=1, lx=2.0, ly=1.0, nbasis=4, iquad=2, ivis=1,
+                                                     coll=20.0, colvis=1.0, xlobc="inflow", xhibc="wall",
+                                                     ylobc="noslip", yhibc="noslip", inflow_u=0.3, inflow_p=1.0,
+                                                     ihllc=2),
+                               lambda c: ic.channel(c, amplitude=0.0)),
     "grad_rk3_nb10": (lambda: config.Config(nx=8, ny=8, nz=1, nbasis=10, iquad=3, ivis=3, coll=1.0, iorder=3),
                       lambda c: ic.ten_moment_stress(c, ic.random_smooth(c, seed=2, amp=0.05), p=1.0, amp=0.01)),
 }
