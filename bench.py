@@ -356,6 +356,8 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
         "note": "HLLC with the stress-augmented point flux is discontinuous at S_M = 0, where an equilibrium "
                 "fluctuating state sits at every face; FP32 and FP64 then pick branches by rounding"}
     res["adjoint_poiseuille"] = adjoint_poiseuille()
+    res["tgv64"] = tgv64()
+    res["sod256"] = sod256()
     res["derived_fields"] = derived_fields(cfg64, Q0, flush)
     res["checkpoint_io"] = checkpoint_io(cfg64, Q0)
     return res
@@ -416,6 +418,92 @@ def adjoint_poiseuille(nsteps=200, every=20):
             "fd_dL_dmu": fd_mu, "rel_err_mu_vs_fd": abs(adj_mu - fd_mu) / abs(adj_mu),
             "fd_dL_dpert_dir": fd_p, "rel_err_pert_vs_fd": abs(adj_p - fd_p) / abs(adj_p),
             "limiter_events": roll.limiter_events}
+
+
+def tgv64(nsteps=200):
+    """The 3-D Taylor-Green vortex, 10-moment ivis 1, 64^3, nb 4, RK3, Mach
+    0.1, Re 400 (symmetry broken by 1e-3, seed 1): 200 steps in FP64 and in
+    FP32 (FP64 CFL, limiter fixes and conservation sums), device time of the
+    200 steps by CUDA events, FP32 relative L2 from the FP64 state, and the
+    FP64 conservation sums' drift."""
+    import numpy as np
+    import torch
+
+    from hermeshd_gb300 import config, ic
+    from hermeshd_gb300.solver import Solver
+
+    out, states = {}, {}
+    for prec in ("fp64", "fp32"):
+        cfg = config.taylor_green_3d(n=64, precision=prec)
+        s = Solver(cfg)
+        q0 = s.from_numpy(ic.taylor_green(cfg, perturb=1e-3, seed=1))
+        q, q1 = q0.clone(), s.new_state()
+        s.enqueue_steps(q, q1, 1)                 # graph capture outside the timed region
+        q.copy_(q0)
+        s.set_time(0.0)
+        c0 = s.conserved(q)
+        st = torch.cuda.ExternalStream(s.cuda_stream)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        s.enqueue_steps(q, q1, nsteps)
+        b.record(st)
+        b.synchronize()
+        ms = a.elapsed_time(b)
+        c1 = s.conserved(q)
+        drift = np.abs(c1[0] - c0[0]) / np.maximum(np.abs(c0[0]), 1e-300)
+        out[prec] = {"value": cfg.dof * cfg.stages * nsteps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / nsteps,
+                     "conservation_rel_drift": {"mass": float(drift[0]), "energy": float(drift[4])}}
+        states[prec] = q.double()
+        s.close()
+    out["fp32"]["rel_l2_vs_fp64"] = float((states["fp32"] - states["fp64"]).norm() / states["fp64"].norm())
+    out["fp32"]["speedup_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    out["config"] = {"grid": "64^3", "nbasis": 4, "ivis": 1, "riemann": "HLLC", "rk": "SSP-RK3", "steps": nsteps}
+    return out
+
+
+def sod256():
+    """The 1-D Sod shock tube of the CPU-runnable configuration (256 cells,
+    nb 4, HLLC, RK2, CFL 0.3) to t = 0.2: wall time through hermes_advance on
+    the GPU (one launch of steps per CUDA graph, read-back every 50 steps)
+    and the oracle on the host cores."""
+    import time
+
+    import torch
+
+    from hermeshd_gb300 import config, ic
+    from hermeshd_gb300.solver import Solver
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    cfg = config.sod_1d(nx=256)
+    s = Solver(cfg)
+
+    def run_gpu():
+        q, q1 = s.from_numpy(ic.sod(cfg)), s.new_state()
+        t, n = 0.0, 0
+        while t < cfg.tf:
+            t, dt = s.advance(q, q1, 50, t=t)
+            n += 50
+        return n, t
+
+    run_gpu()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n, t = run_gpu()
+    gpu_s = time.perf_counter() - t0
+    o = O.Oracle(cfg)
+    Q = ic.sod(cfg)
+    t0 = time.perf_counter()
+    tt, steps = 0.0, 0
+    while tt < cfg.tf:
+        tt, _ = o.advance(Q, 50, t=tt)
+        steps += 50
+    cpu_s = time.perf_counter() - t0
+    s.close()
+    return {"steps": n, "t_end": t, "gpu_wall_s": gpu_s, "oracle_wall_s": cpu_s, "oracle_threads": O.num_threads(),
+            "note": "256 cells fill 2 of 152 SMs: launch-latency bound on the GPU"}
 
 
 def derived_fields(cfg, Q0, flush, reps=20):

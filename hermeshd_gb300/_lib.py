@@ -26,7 +26,7 @@ EXPORTS = ("hermes_abi_version", "hermes_config_size", "hermes_sizes", "hermes_c
            "hermes_box_times", "hermes_set_time", "hermes_set_noise_step", "hermes_check", "hermes_rhs_noalloc",
            "hermes_rhs_vjp", "hermes_stage_vjp", "hermes_set_launch", "hermes_get_launch",
            "hermes_checkpoint_write", "hermes_checkpoint_read", "hermes_derived",
-           "hermes_init_state")
+           "hermes_init_state", "hermes_conserved")
 
 
 class HermesLaunch(C.Structure):
@@ -135,6 +135,7 @@ def lib() -> C.CDLL:
         "hermes_checkpoint_write": (i32, [C.c_char_p, vp, i32, i32, i32, i32, C.c_double, C.c_double, i32,
                                           C.POINTER(C.c_int32), C.c_char_p, C.c_size_t]),
         "hermes_init_state": (i32, [vp, vp, i32, C.c_uint64]),
+        "hermes_conserved": (i32, [vp, vp, dp]),
         "hermes_derived": (i32, [vp, vp, vp, i32, C.c_uint32, C.POINTER(HermesOutputUnits)]),
         "hermes_checkpoint_read": (i32, [C.c_char_p, vp, i32, i32, i32, i32, dp, dp, C.POINTER(C.c_int32),
                                          C.POINTER(C.c_int32), C.c_char_p, C.c_size_t]),

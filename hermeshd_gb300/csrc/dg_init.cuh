@@ -98,3 +98,53 @@ __global__ void __launch_bounds__(INIT_TPB) k_init(T* __restrict__ Q, InitArgs a
 cudaError_t init_launch(int precision, void* Q, const InitArgs& a, cudaStream_t s);
 
 }  // namespace hermes
+
+namespace hermes {
+
+// ---------------------------------------------------------------------------
+// Conservation sums in FP64 for any precision of the state: per box, the
+// integrals of rho, m_x, m_y, m_z and E (cell averages times the cell
+// volume).  Each box is cut into chunks of CONS_CHUNK cells; one block sums a
+// chunk in a fixed order, then one block per box sums its chunks in order, so
+// the result does not depend on scheduling.
+// ---------------------------------------------------------------------------
+constexpr int CONS_TPB = 256;
+constexpr int CONS_CHUNK = 8192;
+
+struct ConsArgs {
+    const Box* boxes;
+    const int* chunk_box;       // box of each chunk
+    const int* box_chunk0;      // first chunk of each box (nbox + 1 entries)
+    double* partial;            // 5 per chunk
+    double* out;                // 5 per box
+    int nchunk;
+};
+
+template <class T>
+__global__ void __launch_bounds__(CONS_TPB) k_cons_partial(const T* __restrict__ Q, ConsArgs a) {
+    __shared__ double red[5][CONS_TPB];
+    const int ch = blockIdx.x;
+    const int bx = a.chunk_box[ch];
+    const Box& B = a.boxes[bx];
+    const long long first = (long long)(ch - a.box_chunk0[bx]) * CONS_CHUNK;
+    const long long last = first + CONS_CHUNK < B.ncell ? first + CONS_CHUNK : B.ncell;
+    const T* Qb = Q + B.q0;
+    double s[5] = {0, 0, 0, 0, 0};
+    for (long long c = first + threadIdx.x; c < last; c += CONS_TPB)
+#pragma unroll
+        for (int v = 0; v < 5; ++v) s[v] += (double)Qb[(long long)v * B.ncell + c];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) red[v][threadIdx.x] = s[v];
+    __syncthreads();
+    for (int k = CONS_TPB / 2; k > 0; k >>= 1) {
+        if (threadIdx.x < k)
+#pragma unroll
+            for (int v = 0; v < 5; ++v) red[v][threadIdx.x] += red[v][threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x < 5) a.partial[5 * ch + threadIdx.x] = red[threadIdx.x][0];
+}
+
+cudaError_t cons_launch(int precision, const void* Q, const ConsArgs& a, int nbox, cudaStream_t s);
+
+}  // namespace hermes

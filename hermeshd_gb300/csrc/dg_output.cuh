@@ -82,25 +82,27 @@ __global__ void __launch_bounds__(DERIVED_TPB) k_derived(const T* __restrict__ Q
     const double vx = u[1] * dni, vy = u[2] * dni, vz = u[3] * dni;
     const double U = u[4] - 0.5 * dn * (vx * vx + vy * vy + vz * vz);
     const double P = (a.aindex - 1.0) * U;
-    auto put = [&](int v, double val) {
-        if ((a.mask >> v) & 1u) out[(long long)a.slot[v] * total + l] = (float)val;
-    };
-    put(0, dn * a.n0);
-    put(1, log(dn * a.n0) / log(10.0));
-    put(2, a.v0 * u[1] / dn);
-    put(3, a.v0 * u[2] / dn);
-    put(4, a.v0 * u[3] / dn);
-    put(5, P * a.te0 * dni / a.eV_per_K);
-    put(6, U);
-    put(7, u[4]);
-    put(8, P * pow(dni, a.aindex - 1.0));
-    put(9, P);
-    put(10, u[5]);
-    put(11, u[6]);
-    put(12, u[7]);
-    if ((a.mask >> 13) & 1u) {
-        const double dxvy = (dn * dmyx - u[2] * drx) / (dn * dn);
-        const double dyvx = (dn * dmxy - u[1] * dry) / (dn * dn);
+    const unsigned mask = a.mask;
+    auto put = [&](int v, double val) { out[(long long)a.slot[v] * total + l] = (float)val; };
+    // quotients by rho taken as products with 1/rho (one FP64 rounding apart,
+    // below the float32 output's resolution); log and pow only when asked for
+    if (mask & (1u << 0)) put(0, dn * a.n0);
+    if (mask & (1u << 1)) put(1, log(dn * a.n0) * (1.0 / log(10.0)));
+    if (mask & (1u << 2)) put(2, a.v0 * vx);
+    if (mask & (1u << 3)) put(3, a.v0 * vy);
+    if (mask & (1u << 4)) put(4, a.v0 * vz);
+    if (mask & (1u << 5)) put(5, P * a.te0 * dni / a.eV_per_K);
+    if (mask & (1u << 6)) put(6, U);
+    if (mask & (1u << 7)) put(7, u[4]);
+    if (mask & (1u << 8)) put(8, P * pow(dni, a.aindex - 1.0));
+    if (mask & (1u << 9)) put(9, P);
+    if (mask & (1u << 10)) put(10, u[5]);
+    if (mask & (1u << 11)) put(11, u[6]);
+    if (mask & (1u << 12)) put(12, u[7]);
+    if (mask & (1u << 13)) {
+        const double dni2 = dni * dni;
+        const double dxvy = (dn * dmyx - u[2] * drx) * dni2;
+        const double dyvx = (dn * dmxy - u[1] * dry) * dni2;
         put(13, -2.0 * (dxvy - dyvx) * B.di[0] / a.t0);
     }
 }

@@ -117,6 +117,10 @@ struct hermes_ctx {
     std::vector<double> h_len;           // lx, ly, lz per box
     Box* d_boxes = nullptr;
     double* d_len = nullptr;
+    // conservation sums: chunk map and partials, built on first use
+    int* d_cons_map = nullptr;           // chunk -> box, then box -> first chunk
+    double* d_cons = nullptr;            // 5 per chunk, then 5 per box
+    int cons_nchunk = 0;
     Geom G{};
     Phys ph{};
     BoxState* d_st = nullptr;
@@ -510,6 +514,8 @@ int hermes_destroy(hermes_ctx* c) {
     cudaFree(c->d_part);
     cudaFree(c->d_sum);
     cudaFree(c->d_len);
+    cudaFree(c->d_cons_map);
+    cudaFree(c->d_cons);
     delete c;
     return HERMES_OK;
 }
@@ -650,6 +656,38 @@ int hermes_init_state(hermes_ctx* c, void* q, int32_t icid, uint64_t seed) {
                c->cfg.aindex, c->cfg.rh_floor, c->cfg.T_floor, c->cfg.P_base, (unsigned long long)seed};
     cudaError_t e = init_launch(c->cfg.precision, q, a, c->stream);
     if (e != cudaSuccess) return leave(c, cuda_fail(c, "initial-state launch", e));
+    return leave(c, HERMES_OK);
+}
+
+int hermes_conserved(hermes_ctx* c, const void* q, double* sums) {
+    if (!c || !q || !sums) return fail(c, HERMES_ERR_ARG, "null argument");
+    int rc = enter(c);
+    if (rc) return rc;
+    const int nbox = c->G.nbox;
+    if (!c->d_cons) {
+        std::vector<int> map;
+        std::vector<int> first(nbox + 1, 0);
+        for (int b = 0; b < nbox; ++b) {
+            first[b] = (int)map.size();
+            const long long n = c->h_boxes[b].ncell;
+            for (long long k = 0; k < (n + CONS_CHUNK - 1) / CONS_CHUNK; ++k) map.push_back(b);
+        }
+        first[nbox] = (int)map.size();
+        c->cons_nchunk = (int)map.size();
+        map.insert(map.end(), first.begin(), first.end());
+        if (cudaMalloc(&c->d_cons_map, sizeof(int) * map.size()) != cudaSuccess ||
+            cudaMalloc(&c->d_cons, sizeof(double) * 5 * ((size_t)c->cons_nchunk + nbox)) != cudaSuccess) {
+            cudaGetLastError();
+            return leave(c, fail(c, HERMES_ERR_ALLOC, "conservation-sum scratch"));
+        }
+        HCK(c, cudaMemcpy(c->d_cons_map, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice));
+    }
+    ConsArgs a{c->d_boxes, c->d_cons_map, c->d_cons_map + c->cons_nchunk, c->d_cons,
+               c->d_cons + 5 * (size_t)c->cons_nchunk, c->cons_nchunk};
+    cudaError_t e = cons_launch(c->cfg.precision, q, a, nbox, c->stream);
+    if (e != cudaSuccess) return leave(c, cuda_fail(c, "conservation-sum launch", e));
+    HCK(c, cudaMemcpyAsync(sums, a.out, sizeof(double) * 5 * nbox, cudaMemcpyDeviceToHost, c->stream));
+    HCK(c, cudaStreamSynchronize(c->stream));
     return leave(c, HERMES_OK);
 }
 

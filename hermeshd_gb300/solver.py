@@ -164,6 +164,12 @@ class Solver:
         check(lib().hermes_init_state(self.ctx, self._ptr(q), int(icid), int(seed)), self.ctx)
         return q
 
+    def conserved(self, q) -> np.ndarray:
+        """FP64 integrals of rho, m_x, m_y, m_z, E per box: array (nbox, 5)."""
+        out = np.zeros((self.nbox, 5))
+        check(lib().hermes_conserved(self.ctx, self._ptr(q), out.ctypes.data_as(C.POINTER(C.c_double))), self.ctx)
+        return out
+
     # ---- launch shape ---------------------------------------------------------
     def get_launch(self) -> dict:
         l = _lib.HermesLaunch()

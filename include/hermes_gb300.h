@@ -178,6 +178,13 @@ int hermes_checkpoint_read(const char *path, double *q, int32_t nx, int32_t ny, 
  * averages only; all other coefficients are written zero. */
 int hermes_init_state(hermes_ctx *ctx, void *q, int32_t icid, uint64_t seed);
 
+/* Conservation sums in FP64 whatever the precision of q: per box, the
+ * integrals of rho, m_x, m_y, m_z and E (cell averages times the cell
+ * volume), 5 doubles per box into the host array sums, summed in a fixed
+ * order (the same bits on every call).  No counterpart in the reference.
+ * Synchronises. */
+int hermes_conserved(hermes_ctx *ctx, const void *q, double *sums);
+
 /* Derived fields of the VTK output (output.f90:14-317), on the device.  The
  * state q of a one-grid context is evaluated at nvtk^3 sub-points per cell
  * (nvtk 1..4, basis_funcs.f90:88-200) and the variables selected by mask
