@@ -147,29 +147,57 @@ __device__ __forceinline__ void face_adj_point(const double* __restrict__ Q, con
             });
         lamF[v] = di * sacc;
     }
-    // J^T lamF, one dual pass per input component
+    // J^T lamF.  Hydro columns (rh..en): one dual pass each.  Stress columns:
+    // for ivis 0/1 the stresses enter only the point fluxes of the normal
+    // direction, linearly (f[M_i] += P_{d i}, f[E] += P_{d i} v_i,
+    // flux.f90:87-89), and every numerical flux takes f_L, f_R with weights
+    // w_L + w_R = 1 (central and Roe 1/2 each; HLLC 1 on the side its wave
+    // selection picks), so column P_{d i} of a side is w (lamF[M_i] + lamF[E] v_i).
     double lamL[NQ], lamR[NQ];
     const Dual S0[6] = {Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0)};
+    constexpr int PN[3] = {DIR == 0 ? PXX : DIR == 1 ? PXY : PXZ, DIR == 0 ? PXY : DIR == 1 ? PYY : PYZ,
+                           DIR == 0 ? PXZ : DIR == 1 ? PYZ : PZZ};   // P_{d x}, P_{d y}, P_{d z}
+    double wL = 0.0;
 #pragma unroll 1
+    for (int pass = -1; pass < 10; ++pass) {
+        // pass -1: seed P_{d d} of the left trace, whose derivative in the
+        // normal-momentum row is w_L; passes 0..9: hydro columns of L then R
+        const int side = pass < 0 ? 0 : pass / 5, jv = pass < 0 ? PN[DIR] : pass % 5;
+        const TraceSrc& src = side == 0 ? L : R;
+        if (pass >= 0) {
+            (side == 0 ? lamL : lamR)[jv] = 0.0;
+            if (src.cell < 0 || !((src.mask >> jv) & 1u)) continue;
+        }
+        Dual dL[NQ], dR[NQ], F[NQ];
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) {
+            dL[v] = Dual(qL[v], (side == 0 && v == jv) ? 1.0 : 0.0);
+            dR[v] = Dual(qR[v], (side == 1 && v == jv) ? 1.0 : 0.0);
+        }
+        face_flux_fn<Dual, DIR>(ph, dL, dR, S0, S0, Dual(0.0), F);
+        if (pass < 0) {
+            wL = F[MN].d;
+            continue;
+        }
+        double acc = 0.0;
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) acc = fma(lamF[v], F[v].d, acc);
+        (side == 0 ? lamL : lamR)[jv] = acc;
+    }
+#pragma unroll
     for (int side = 0; side < 2; ++side) {
         const TraceSrc& src = side == 0 ? L : R;
+        const double* qs = side == 0 ? qL : qR;
         double* lam = side == 0 ? lamL : lamR;
-#pragma unroll 1
-        for (int jv = 0; jv < NQ; ++jv) {
-            lam[jv] = 0.0;
-            if (src.cell < 0 || !((src.mask >> jv) & 1u)) continue;
-            Dual dL[NQ], dR[NQ], F[NQ];
+        const double w = side == 0 ? wL : 1.0 - wL;
+        const double dni = 1.0 / qs[RH];
+        const double vel[3] = {qs[MX] * dni, qs[MY] * dni, qs[MZ] * dni};
 #pragma unroll
-            for (int v = 0; v < NQ; ++v) {
-                dL[v] = Dual(qL[v], (side == 0 && v == jv) ? 1.0 : 0.0);
-                dR[v] = Dual(qR[v], (side == 1 && v == jv) ? 1.0 : 0.0);
-            }
-            face_flux_fn<Dual, DIR>(ph, dL, dR, S0, S0, Dual(0.0), F);
-            double acc = 0.0;
+        for (int v = PXX; v < NQ; ++v) lam[v] = 0.0;
+        if (src.cell < 0) continue;
 #pragma unroll
-            for (int v = 0; v < NQ; ++v) acc = fma(lamF[v], F[v].d, acc);
-            lam[jv] = acc;
-        }
+        for (int i = 0; i < 3; ++i)
+            if ((src.mask >> PN[i]) & 1u) lam[PN[i]] = w * fma(lamF[EN], vel[i], lamF[MX + i]);
     }
     // a ghost made from a cell's own trace hands its adjoint to that trace
     if (ghostL_from_R) {
@@ -282,9 +310,12 @@ __global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__
             lamF[2][v] = -di[2] * a2;
             lamS[v] = -as;
         }
+        // hydro columns (rh..en): one dual pass each; stress columns in closed
+        // form (the stresses enter the point fluxes linearly: f_d[M_i] +=
+        // P_{d i}, f_d[E] += P_{d i} v_i, and the ivis-0 source -coll P)
         double lamu[NQ];
 #pragma unroll 1
-        for (int jv = 0; jv < NQ; ++jv) {
+        for (int jv = 0; jv <= EN; ++jv) {
             Dual ud[NQ];
 #pragma unroll
             for (int v = 0; v < NQ; ++v) ud[v] = Dual(u[v], v == jv ? 1.0 : 0.0);
@@ -297,16 +328,23 @@ __global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__
 #pragma unroll
                 for (int v = 0; v < NQ; ++v) acc = fma(lamF[d][v], f[v].d, acc);
             });
-            // point sources (sources.f90:37-43; body force): linear in u
-            if (src_lin) {
-#pragma unroll
-                for (int v = PXX; v <= PYZ; ++v) acc = fma(lamS[v], (v == jv ? -ph.coll : 0.0), acc);
-            }
+            // body force (no reference counterpart): linear in rho and m_x
             if (src_bf) {
                 if (jv == RH) acc = fma(lamS[MX], ph.body_force, acc);
                 if (jv == MX) acc = fma(lamS[EN], ph.body_force, acc);
             }
             lamu[jv] = acc;
+        }
+        {
+            const double dni = 1.0 / u[RH];
+            const double vel[3] = {u[MX] * dni, u[MY] * dni, u[MZ] * dni};
+            constexpr int PD[3][3] = {{PXX, PXY, PXZ}, {PXY, PYY, PYZ}, {PXZ, PYZ, PZZ}};
+#pragma unroll
+            for (int v = PXX; v < NQ; ++v) lamu[v] = src_lin ? lamS[v] * -ph.coll : 0.0;   // sources.f90:37-43
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int i = 0; i < 3; ++i) lamu[PD[d][i]] += fma(lamF[d][EN], vel[i], lamF[d][MX + i]);
         }
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;

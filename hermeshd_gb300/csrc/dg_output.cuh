@@ -85,16 +85,18 @@ __global__ void __launch_bounds__(DERIVED_TPB) k_derived(const T* __restrict__ Q
     const unsigned mask = a.mask;
     auto put = [&](int v, double val) { out[(long long)a.slot[v] * total + l] = (float)val; };
     // quotients by rho taken as products with 1/rho (one FP64 rounding apart,
-    // below the float32 output's resolution); log and pow only when asked for
+    // below the float32 output's resolution); every variable only when asked for
     if (mask & (1u << 0)) put(0, dn * a.n0);
-    if (mask & (1u << 1)) put(1, log(dn * a.n0) * (1.0 / log(10.0)));
+    // log and pow in FP32: the output is float32, and the FP64 forms cost more
+    // than the rest of the kernel (single-precision results are within 2 ulps)
+    if (mask & (1u << 1)) put(1, (double)(logf((float)(dn * a.n0)) * 0.43429448190325182f));
     if (mask & (1u << 2)) put(2, a.v0 * vx);
     if (mask & (1u << 3)) put(3, a.v0 * vy);
     if (mask & (1u << 4)) put(4, a.v0 * vz);
     if (mask & (1u << 5)) put(5, P * a.te0 * dni / a.eV_per_K);
     if (mask & (1u << 6)) put(6, U);
     if (mask & (1u << 7)) put(7, u[4]);
-    if (mask & (1u << 8)) put(8, P * pow(dni, a.aindex - 1.0));
+    if (mask & (1u << 8)) put(8, (double)((float)P * powf((float)dni, (float)(a.aindex - 1.0))));
     if (mask & (1u << 9)) put(9, P);
     if (mask & (1u << 10)) put(10, u[5]);
     if (mask & (1u << 11)) put(11, u[6]);
