@@ -32,7 +32,7 @@ EXPORTS = ("hermes_abi_version", "hermes_config_size", "hermes_sizes", "hermes_c
 class HermesLaunch(C.Structure):
     """hermes_launch of include/hermes_gb300.h."""
     _fields_ = [("face_tpb", C.c_int32), ("dt_tpb", C.c_int32), ("steps_per_graph", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("noise_inline", C.c_int32)]
 
 
 class HermesOutputUnits(C.Structure):

@@ -8,7 +8,10 @@ include/hermes_gb300.h):
                        larger ones amortise scheduling on a large one;
 * ``dt_tpb``           cells per block of the CFL reduction (64/128/256);
 * ``steps_per_graph``  whole steps per CUDA graph launch (1/2/4/8): fewer
-                       launches for grids so small that a step is launch-bound.
+                       launches for grids so small that a step is launch-bound;
+* ``noise_inline``     where the stochastic stress is drawn: its own
+                       kernels staging it in device memory (0) or inside the
+                       face and cell kernels (1).
 
 The cell kernel keeps 32 cells per block: its hydro and stress thread groups
 must each fill whole warps, and its register cap is fixed at compile time.
@@ -31,6 +34,7 @@ KNOBS = {
     "face_tpb": (128, 64, 32),
     "dt_tpb": (256, 128, 64),
     "steps_per_graph": (1, 2, 4, 8),
+    "noise_inline": (0, 1),          # tuned only with the stochastic stress on
 }
 
 
@@ -106,7 +110,9 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
         if hit:
             solver.set_launch(**hit["launch"])
             return dict(hit, cached=True)
-    knobs = knobs or KNOBS
+    knobs = dict(knobs or KNOBS)
+    if not solver.cfg.llns:
+        knobs.pop("noise_inline", None)
     qt, q1t = q.clone(), q.clone()
     best = {k: v[0] for k, v in knobs.items()}
     solver.set_launch(**best)

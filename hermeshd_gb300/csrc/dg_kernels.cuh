@@ -35,6 +35,7 @@ struct Geom {
     int nbox;
     long long ncell;          // all boxes
     long long nface[3];       // all boxes, per direction
+    long long face0_dir[3];   // faces of the directions before this one (staged face-noise layout)
 };
 
 // face tables of one direction and side (0 = minus face, 1 = plus face)
@@ -253,6 +254,7 @@ struct FaceArgs {
     const unsigned long long* step;  // noise step counter (device)
     unsigned stage;
     int tpb;                         // faces per block (32, 64 or 128; 0 = FACE_TPB)
+    const void* noise;               // staged stochastic stress of the faces (k_noise_face), or null: drawn here
 };
 
 // the numerical flux at one face point from the two traces (after boundary
@@ -375,9 +377,20 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
     // point fluxes of both sides (flux.f90:240), stochastic stress per side
     T SL[6] = {T(0), T(0), T(0), T(0), T(0), T(0)}, SR[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
     if constexpr (NOISE) {
-        NoiseCtr nc_{*a.step, a.stage};
-        random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P, SL);
-        random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P + TB::NF, SR);
+        if (a.noise) {
+            // [side][component][point][face] of this direction (dg_noise.cuh)
+            const T* nb = static_cast<const T*>(a.noise) + 12ll * TB::NF * G.face0_dir[DIR];
+            const long long nfa = G.nface[DIR];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                SL[c] = nb[((long long)(0 * 6 + c) * TB::NF + P) * nfa + gf];
+                SR[c] = nb[((long long)(1 * 6 + c) * TB::NF + P) * nfa + gf];
+            }
+        } else {
+            NoiseCtr nc_{*a.step, a.stage};
+            random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P, SL);
+            random_stress<T>(ph, B.seed, nc_, DIR, (unsigned long long)lf, P + TB::NF, SR);
+        }
     }
     T F[NQ];
     T rho_i_last = T(0);
@@ -432,6 +445,7 @@ struct CellArgs {
     unsigned stage;
     int mode, comb;
     int split_source;   // Grad closure with RK2: the implicit source step after the update
+    const void* noise;  // staged interior stochastic stress (k_noise_cell), or null: drawn here
 };
 
 // RK combination of integrator.f90:62-86
@@ -499,7 +513,17 @@ __device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T
         sfor<3>([&](auto dd) {
             constexpr int d = decltype(dd)::value;
             T S[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-            if constexpr (GRP == 0 && NOISE) random_stress<T>(ph, cx.B->seed, cx.nctr, 3 + d, (unsigned long long)cx.le, g, S);
+            if constexpr (GRP == 0 && NOISE) {
+                if (a.noise) {
+                    // [direction][point][component][cell] (dg_noise.cuh)
+                    const T* nb = static_cast<const T*>(a.noise);
+                    const long long gc = cx.B->cell0 + cx.le, ncl = a.G.ncell;
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) S[c] = nb[((long long)(d * NPG + g) * 6 + c) * ncl + gc];
+                } else {
+                    random_stress<T>(ph, cx.B->seed, cx.nctr, 3 + d, (unsigned long long)cx.le, g, S);
+                }
+            }
             T f[NQ];
             point_flux<T, d>(ph, u, w, S, f);
             T fs[GNV];

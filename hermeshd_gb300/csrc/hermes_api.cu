@@ -19,6 +19,7 @@
 
 #include "dg_init.cuh"
 #include "dg_launch.cuh"
+#include "dg_noise.cuh"
 #include "dg_output.cuh"
 #include "hermes_gb300.h"
 
@@ -141,6 +142,11 @@ struct hermes_ctx {
     long long prof_n[6] = {0, 0, 0, 0, 0, 0};
     // launch shape (hermes_set_launch); 0 = the compiled defaults
     int face_tpb = 0, dt_tpb = 0, graph_steps = 1;
+    // stochastic stress staged in HBM by its own kernels (dg_noise.cuh)
+    bool noise_staged = false;
+    NoiseFn noise_fn = nullptr;
+    void* d_noise_cell = nullptr;
+    void* d_noise_face = nullptr;
     // adjoint scratch, allocated on first use
     AdjFn adj = nullptr;
     double* d_tadj = nullptr;   // trace adjoints: 2 x the face-flux size
@@ -299,7 +305,7 @@ void enq_limit(hermes_ctx* c, void* q) {
     }
 }
 void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
-    FaceArgs a{c->G, c->ph, c->d_step, stage, c->face_tpb};
+    FaceArgs a{c->G, c->ph, c->d_step, stage, c->face_tpb, c->noise_staged ? c->d_noise_face : nullptr};
     for (int d = 0; d < 3; ++d) {
         ProfScope ps(c, 2 + d);
         c->K.face(d, q, c->d_flux, a, c->stream);
@@ -307,12 +313,19 @@ void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
 }
 void enq_cell(hermes_ctx* c, const void* qin, const void* q0, void* out, int mode, int comb, unsigned stage) {
     const int split = (mode == MODE_STAGE && c->cfg.ivis == 3 && c->cfg.iorder == 2) ? 1 : 0;
-    CellArgs a{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb, split};
+    CellArgs a{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb, split,
+               c->noise_staged ? c->d_noise_cell : nullptr};
     ProfScope ps(c, 5);
     c->K.cell(qin, q0, out, c->d_flux, a, c->stream);
 }
+void enq_noise(hermes_ctx* c, unsigned stage) {
+    if (!c->noise_staged) return;
+    NoiseArgs a{c->G, c->ph, c->d_step, stage};
+    c->noise_fn(c->d_noise_cell, c->d_noise_face, a, c->stream);
+}
 void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, unsigned stage) {
     enq_limit(c, qin);
+    enq_noise(c, stage);
     enq_faces(c, qin, stage);
     enq_cell(c, qin, q0, out, MODE_STAGE, comb, stage);
 }
@@ -418,6 +431,9 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     c->G.nbox = nbox;
     c->G.ncell = ncell;
     for (int d = 0; d < 3; ++d) c->G.nface[d] = nface[d];
+    c->G.face0_dir[0] = 0;
+    c->G.face0_dir[1] = nface[0];
+    c->G.face0_dir[2] = nface[0] + nface[1];
     auto bail = [&](int code) { hermes_destroy(c); return code; };
     c->user_stream = static_cast<cudaStream_t>(stream);
     {
@@ -436,6 +452,20 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
         return bail(HERMES_ERR_ALLOC);
     }
     c->G.boxes = c->d_boxes;
+    if (cfg->llns && noise_launcher(cfg->precision, cfg->nbasis, &c->noise_fn)) {
+        // staged stochastic stress: 18 NPG values per cell, 12 NF per face
+        const size_t npg = (size_t)c->K.nqd * c->K.nqd * c->K.nqd, nf = (size_t)c->K.nf;
+        const size_t es = c->K.elem_size;
+        const size_t fcount = (size_t)(nface[0] + nface[1] + nface[2]);
+        if (cudaMalloc(&c->d_noise_cell, (size_t)ncell * 18 * npg * es) == cudaSuccess &&
+            cudaMalloc(&c->d_noise_face, fcount * 12 * nf * es) == cudaSuccess) {
+            c->noise_staged = true;
+        } else {
+            cudaGetLastError();   // no room: the face and cell kernels draw the stress themselves
+            cudaFree(c->d_noise_cell); cudaFree(c->d_noise_face);
+            c->d_noise_cell = c->d_noise_face = nullptr;
+        }
+    }
     if (cudaMemcpy(c->d_boxes, c->h_boxes.data(), sizeof(Box) * nbox, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(c->d_st, 0, sizeof(BoxState) * nbox) != cudaSuccess ||
         cudaMemset(c->d_step, 0, sizeof(unsigned long long) * 2) != cudaSuccess ||
@@ -516,6 +546,8 @@ int hermes_destroy(hermes_ctx* c) {
     cudaFree(c->d_len);
     cudaFree(c->d_cons_map);
     cudaFree(c->d_cons);
+    cudaFree(c->d_noise_cell);
+    cudaFree(c->d_noise_face);
     delete c;
     return HERMES_OK;
 }
@@ -719,7 +751,10 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     if (f != 0 && f != 32 && f != 64 && f != 128) return fail(c, HERMES_ERR_ARG, "face_tpb must be 0, 32, 64 or 128");
     if (d != 0 && (d < 32 || d > DT_TPB || d % 32)) return fail(c, HERMES_ERR_ARG, "dt_tpb must be 0 or a multiple of 32 up to 256");
     if (g < 0 || g > 64) return fail(c, HERMES_ERR_ARG, "steps_per_graph must be in 0..64");
-    if (f != c->face_tpb || d != c->dt_tpb) {
+    const bool staged = l->noise_inline == 0 && c->d_noise_cell != nullptr;
+    if (l->noise_inline == 0 && c->cfg.llns && !c->d_noise_cell)
+        return fail(c, HERMES_ERR_ALLOC, "no staged-noise buffers (device memory was short at creation)");
+    if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged) {
         // captured graphs hold the old launch shape
         HCK(c, cudaSetDevice(c->device));
         HCK(c, cudaStreamSynchronize(c->stream));
@@ -728,6 +763,7 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     c->face_tpb = f;
     c->dt_tpb = d;
     c->graph_steps = g > 0 ? g : 1;
+    c->noise_staged = staged;
     return HERMES_OK;
 }
 
@@ -736,7 +772,7 @@ int hermes_get_launch(hermes_ctx* c, hermes_launch* l) {
     l->face_tpb = c->face_tpb > 0 ? c->face_tpb : FACE_TPB;
     l->dt_tpb = c->dt_tpb > 0 ? c->dt_tpb : DT_TPB;
     l->steps_per_graph = c->graph_steps;
-    l->reserved = 0;
+    l->noise_inline = (c->cfg.llns && !c->noise_staged) ? 1 : 0;
     return HERMES_OK;
 }
 

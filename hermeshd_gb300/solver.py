@@ -174,10 +174,11 @@ class Solver:
     def get_launch(self) -> dict:
         l = _lib.HermesLaunch()
         check(lib().hermes_get_launch(self.ctx, C.byref(l)), self.ctx)
-        return {"face_tpb": l.face_tpb, "dt_tpb": l.dt_tpb, "steps_per_graph": l.steps_per_graph}
+        return {"face_tpb": l.face_tpb, "dt_tpb": l.dt_tpb, "steps_per_graph": l.steps_per_graph,
+                "noise_inline": l.noise_inline}
 
-    def set_launch(self, face_tpb: int = 0, dt_tpb: int = 0, steps_per_graph: int = 1):
-        l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), 0)
+    def set_launch(self, face_tpb: int = 0, dt_tpb: int = 0, steps_per_graph: int = 1, noise_inline: int = 0):
+        l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), int(noise_inline))
         check(lib().hermes_set_launch(self.ctx, C.byref(l)), self.ctx)
 
     def set_noise_step(self, step: int):

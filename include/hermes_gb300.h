@@ -211,7 +211,9 @@ typedef struct hermes_launch {
     int32_t face_tpb;        /* faces per block of the face kernels: 32, 64 or 128 (default 128) */
     int32_t dt_tpb;          /* cells per block of the CFL reduction: multiple of 32 up to 256 (default 256) */
     int32_t steps_per_graph; /* whole steps per CUDA graph in hermes_advance/hermes_enqueue_steps: 1..64 (default 1) */
-    int32_t reserved;        /* 0 */
+    int32_t noise_inline;    /* stochastic stress: 0 drawn by kernels of its own and staged in device
+                                memory (default; the buffers are allocated at creation), 1 drawn inside
+                                the face and cell kernels.  The same numbers either way. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
 int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);

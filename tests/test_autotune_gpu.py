@@ -18,12 +18,12 @@ def test_launch_defaults_and_validation():
     from hermeshd_gb300._lib import HermesError
     from hermeshd_gb300.solver import Solver
     s = Solver(config.sod_1d(nx=64))
-    assert s.get_launch() == {"face_tpb": 128, "dt_tpb": 256, "steps_per_graph": 1}
+    assert s.get_launch() == {"face_tpb": 128, "dt_tpb": 256, "steps_per_graph": 1, "noise_inline": 0}
     for bad in ({"face_tpb": 96}, {"face_tpb": 256}, {"dt_tpb": 48}, {"dt_tpb": 512}, {"steps_per_graph": 65}):
         with pytest.raises(HermesError):
             s.set_launch(**bad)
     s.set_launch(face_tpb=32, dt_tpb=64, steps_per_graph=4)
-    assert s.get_launch() == {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 4}
+    assert s.get_launch() == {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 4, "noise_inline": 0}
 
 
 @pytest.mark.parametrize("mk", [lambda: config.isentropic_vortex_2d(n=12),
@@ -33,8 +33,11 @@ def test_every_launch_shape_is_bit_identical(mk):
     cfg = mk()
     Q = ic.isentropic_vortex(cfg) if cfg.nbasis == 10 else ic.equilibrium(cfg)
     ref = None
-    for shape in ({}, {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 3},
-                  {"face_tpb": 64, "dt_tpb": 128, "steps_per_graph": 2}):
+    shapes = [{}, {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 3},
+              {"face_tpb": 64, "dt_tpb": 128, "steps_per_graph": 2}]
+    if cfg.llns:   # the stochastic stress drawn inside the face and cell kernels instead of staged
+        shapes.append({"noise_inline": 1})
+    for shape in shapes:
         s = Solver(cfg)
         s.set_launch(**shape)
         q, q1 = s.from_numpy(Q), s.new_state()
@@ -62,7 +65,7 @@ def test_autotune_resets_state_and_caches(tmp_path, monkeypatch):
         v[0, 4].fill_(1.0 / (base.aindex - 1.0))
     r = autotune.autotune(ens, q, steps=2, repeats=2)
     assert not r["cached"] and r["ms_per_step"] <= r["default_ms_per_step"]
-    assert set(r["launch"]) == {"face_tpb", "dt_tpb", "steps_per_graph"}
+    assert set(r["launch"]) == {"face_tpb", "dt_tpb", "steps_per_graph", "noise_inline"}
     assert ens.get_launch() == r["launch"]
     # tuning stepped copies of q; the context's time and noise counter are reset
     qa, qa1 = q.clone(), ens.new_state()
