@@ -46,23 +46,25 @@ __device__ __forceinline__ void normals9(unsigned long long seed, NoiseCtr nc, u
         c[2] = (uint32_t)nc.step;
         c[3] = (uint32_t)(nc.step >> 32);
         philox4x32_10(c, k0, k1);
+        // every rounding explicit (no contraction into FMAs), so the numbers do
+        // not depend on the kernel the generator is inlined into
         T z0, z1;
         if constexpr (std::is_same<T, double>::value) {
             // 53-bit uniforms in (0,1)
             unsigned long long m1 = ((unsigned long long)c[0] << 21) | (unsigned long long)(c[1] >> 11);
             unsigned long long m2 = ((unsigned long long)c[2] << 21) | (unsigned long long)(c[3] >> 11);
-            double u1 = ((double)m1 + 0.5) * (1.0 / 9007199254740992.0);
-            double u2 = ((double)m2 + 0.5) * (1.0 / 9007199254740992.0);
-            double r = sqrt(-2.0 * log(u1)), s, co;
-            sincos(6.283185307179586476925286766559 * u2, &s, &co);
-            z0 = r * co; z1 = r * s;
+            double u1 = __dmul_rn(__dadd_rn((double)m1, 0.5), 1.0 / 9007199254740992.0);
+            double u2 = __dmul_rn(__dadd_rn((double)m2, 0.5), 1.0 / 9007199254740992.0);
+            double r = sqrt(__dmul_rn(-2.0, log(u1))), s, co;
+            sincos(__dmul_rn(6.283185307179586476925286766559, u2), &s, &co);
+            z0 = __dmul_rn(r, co); z1 = __dmul_rn(r, s);
         } else {
             // the top 24 bits of the same words
-            float u1 = ((float)(c[0] >> 8) + 0.5f) * (1.0f / 16777216.0f);
-            float u2 = ((float)(c[2] >> 8) + 0.5f) * (1.0f / 16777216.0f);
-            float r = sqrtf(-2.0f * logf(u1)), s, co;
-            sincosf(6.2831853071795864769f * u2, &s, &co);
-            z0 = r * co; z1 = r * s;
+            float u1 = __fmul_rn(__fadd_rn((float)(c[0] >> 8), 0.5f), 1.0f / 16777216.0f);
+            float u2 = __fmul_rn(__fadd_rn((float)(c[2] >> 8), 0.5f), 1.0f / 16777216.0f);
+            float r = sqrtf(__fmul_rn(-2.0f, logf(u1))), s, co;
+            sincosf(__fmul_rn(6.2831853071795864769f, u2), &s, &co);
+            z0 = __fmul_rn(r, co); z1 = __fmul_rn(r, s);
         }
         if (2 * sub < 9) G[2 * sub] = z0;
         if (2 * sub + 1 < 9) G[2 * sub + 1] = z1;
@@ -78,14 +80,18 @@ __device__ __forceinline__ void random_stress(const Phys& ph, unsigned long long
     normals9<T>(seed, nc, kind, site, pt, G);
     const T s2i = T(0.70710678118654752440);
     const T eta = T(ph.eta_sd), zeta = T(ph.zeta_sd);
-    T Gxy = s2i * (G[1] + G[3]), Gxz = s2i * (G[2] + G[6]), Gyz = s2i * (G[5] + G[7]);
-    T trG = G[0] + G[4] + G[8], trGd3 = trG / T(3), trGz = zeta * trG;
-    S[0] = eta * (G[0] - trGd3) + trGz;
-    S[1] = eta * (G[4] - trGd3) + trGz;
-    S[2] = eta * (G[8] - trGd3) + trGz;
-    S[3] = eta * Gxy;
-    S[4] = eta * Gxz;
-    S[5] = eta * Gyz;
+    // explicit roundings, as in normals9: the same numbers in every kernel
+    auto add = [](T x, T y) { if constexpr (std::is_same<T, double>::value) return __dadd_rn(x, y); else return __fadd_rn(x, y); };
+    auto sub = [](T x, T y) { if constexpr (std::is_same<T, double>::value) return __dsub_rn(x, y); else return __fsub_rn(x, y); };
+    auto mul = [](T x, T y) { if constexpr (std::is_same<T, double>::value) return __dmul_rn(x, y); else return __fmul_rn(x, y); };
+    T Gxy = mul(s2i, add(G[1], G[3])), Gxz = mul(s2i, add(G[2], G[6])), Gyz = mul(s2i, add(G[5], G[7]));
+    T trG = add(add(G[0], G[4]), G[8]), trGd3 = trG / T(3), trGz = mul(zeta, trG);
+    S[0] = add(mul(eta, sub(G[0], trGd3)), trGz);
+    S[1] = add(mul(eta, sub(G[4], trGd3)), trGz);
+    S[2] = add(mul(eta, sub(G[8], trGd3)), trGz);
+    S[3] = mul(eta, Gxy);
+    S[4] = mul(eta, Gxz);
+    S[5] = mul(eta, Gyz);
 }
 
 // ---------------------------------------------------------------------------
