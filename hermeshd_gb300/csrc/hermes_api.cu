@@ -584,6 +584,7 @@ int hermes_rhs(hermes_ctx* c, void* q, void* rhs, int apply_limiter) {
     int rc = enter(c);
     if (rc) return rc;
     if (apply_limiter) enq_limit(c, q);
+    enq_noise(c, 0);
     enq_faces(c, q, 0);
     enq_cell(c, q, nullptr, rhs, MODE_RHS, COMB_NONE, 0);
     return leave(c, launch_status(c));
