@@ -133,6 +133,15 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def hbm_share(dof_per_s, precision, iorder):
+    """Algorithmic HBM throughput of a DOF-update rate (2s bytes per DOF for a
+    plain stage, 3s for one that folds in Q^n) and its fraction of the
+    measured HBM copy rate."""
+    from hermeshd_gb300 import perfmodel
+    gbs = dof_per_s * perfmodel.bytes_per_dof_stage(precision, iorder) / 1e9
+    return {"algorithmic_gbs": gbs, "frac_hbm": gbs / peaks()["hbm_gbs"], "peak_source": peaks()["source"]}
+
+
 def peaks():
     p = {"hbm_gbs": FALLBACK_HBM_GBS, "source": "fallback"}
     f = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -302,7 +311,8 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
     v32 = ws * c32.dof * c32.stages * K / el
     e = (q.double() - qg64).norm() / qg64.norm()
     res["fp32"] = {"value": v32, "unit": UNIT, "ms_per_step": 1e3 * el / K, "dtype": "f32",
-                   "rel_l2_vs_fp64": float(e), "speedup_vs_fp64": v32 / value64}
+                   "rel_l2_vs_fp64": float(e), "speedup_vs_fp64": v32 / value64,
+                   "hbm": hbm_share(v32, "fp32", c32.iorder)}
     s.close()
 
     # FP32 batched ensemble vs the plain FP64 path on one box of the same physics
@@ -346,8 +356,10 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
     times = time_steps(s, q, q1, Ke, flush)
     el = max_over_ranks(sum(times), ws)
     v64 = ws * c64.dof * c64.stages * Ke / el
-    res["fp64_plain_fh_box48"] = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * el / Ke, "dtype": "f64"}
+    res["fp64_plain_fh_box48"] = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * el / Ke, "dtype": "f64",
+                                  "hbm": hbm_share(v64, "fp64", c64.iorder)}
     res["fp32_batched_ensemble"]["speedup_vs_fp64_plain"] = vens / v64
+    res["fp32_batched_ensemble"]["hbm"] = hbm_share(vens, "fp32", base.iorder)
     s.close()
     res["fp32_batched_ensemble"]["accuracy"] = ensemble_accuracy(base)
     hl = ensemble_accuracy(base.replace(ihllc=1), nbox=16, steps=20)
@@ -452,7 +464,8 @@ def tgv64(nsteps=200):
         ms = a.elapsed_time(b)
         c1 = s.conserved(q)
         drift = np.abs(c1[0] - c0[0]) / np.maximum(np.abs(c0[0]), 1e-300)
-        out[prec] = {"value": cfg.dof * cfg.stages * nsteps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / nsteps,
+        val = cfg.dof * cfg.stages * nsteps / (ms * 1e-3)
+        out[prec] = {"value": val, "unit": UNIT, "ms_per_step": ms / nsteps, "hbm": hbm_share(val, prec, cfg.iorder),
                      "conservation_rel_drift": {"mass": float(drift[0]), "energy": float(drift[4])}}
         states[prec] = q.double()
         s.close()
@@ -502,7 +515,9 @@ def sod256():
         steps += 50
     cpu_s = time.perf_counter() - t0
     s.close()
+    dofs = cfg.dof * cfg.stages * n / gpu_s
     return {"steps": n, "t_end": t, "gpu_wall_s": gpu_s, "oracle_wall_s": cpu_s, "oracle_threads": O.num_threads(),
+            "value": dofs, "unit": UNIT, "hbm": hbm_share(dofs, "fp64", cfg.iorder),
             "note": "256 cells fill 2 of 152 SMs: launch-latency bound on the GPU"}
 
 

@@ -10,6 +10,7 @@
 // q = 1/3 q + 2/3 E(q1) -- the reference's arrays, with its Q_2 never needed
 // because each combination is fused into the stage that produces it.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdio>
 #include <cstring>
@@ -297,6 +298,12 @@ struct ProfScope {
     }
 };
 
+// NVTX range over a host-side enqueue (visible to Nsight tools; a no-op otherwise)
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
 // ---- enqueue helpers ---------------------------------------------------
 void enq_limit(hermes_ctx* c, void* q) {
     if (c->cfg.ieos == 1 || c->cfg.ieos == 2) {   // integrator.f90:110
@@ -324,6 +331,7 @@ void enq_noise(hermes_ctx* c, unsigned stage) {
     c->noise_fn(c->d_noise_cell, c->d_noise_face, a, c->stream);
 }
 void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, unsigned stage) {
+    NvtxRange r("hermes stage");
     enq_limit(c, qin);
     enq_noise(c, stage);
     enq_faces(c, qin, stage);
@@ -338,6 +346,7 @@ void enq_mindt(hermes_ctx* c, const void* q, bool advance) {
     else k_dt_finalize_only<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st);
 }
 void enq_step(hermes_ctx* c, void* q, void* q1) {
+    NvtxRange r("hermes step");
     enq_mindt(c, q, true);                           // hermeshd.f90:59
     enq_stage(c, q, nullptr, q1, COMB_NONE, 0);      // Q_1 = E(Q)
     if (c->cfg.iorder == 3) {
