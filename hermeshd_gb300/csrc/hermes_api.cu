@@ -139,8 +139,8 @@ struct hermes_ctx {
     struct Rec { int kind; cudaEvent_t a, b; };
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> pool;
-    double prof_ms[6] = {0, 0, 0, 0, 0, 0};
-    long long prof_n[6] = {0, 0, 0, 0, 0, 0};
+    double prof_ms[7] = {0, 0, 0, 0, 0, 0, 0};
+    long long prof_n[7] = {0, 0, 0, 0, 0, 0, 0};
     // launch shape (hermes_set_launch); 0 = the compiled defaults
     int face_tpb = 0, dt_tpb = 0, graph_steps = 1;
     // stochastic stress staged in HBM by its own kernels (dg_noise.cuh)
@@ -328,6 +328,7 @@ void enq_cell(hermes_ctx* c, const void* qin, const void* q0, void* out, int mod
 void enq_noise(hermes_ctx* c, unsigned stage) {
     if (!c->noise_staged) return;
     NoiseArgs a{c->G, c->ph, c->d_step, stage};
+    ProfScope ps(c, 6);
     c->noise_fn(c->d_noise_cell, c->d_noise_face, a, c->stream);
 }
 void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, unsigned stage) {
@@ -807,7 +808,7 @@ int hermes_profile_read(hermes_ctx* c, double* ms, int64_t* launches) {
     }
     c->recs.clear();
     cudaGetLastError();
-    for (int k = 0; k < 6; ++k) {
+    for (int k = 0; k < 7; ++k) {
         if (ms) ms[k] = c->prof_ms[k];
         if (launches) launches[k] = c->prof_n[k];
         c->prof_ms[k] = 0;

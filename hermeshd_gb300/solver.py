@@ -137,11 +137,11 @@ class Solver:
     def profile(self, enable: bool = True):
         check(lib().hermes_profile_enable(self.ctx, int(enable)), self.ctx)
 
-    KERNEL_KINDS = ("cfl_dt", "limiter", "face_x", "face_y", "face_z", "cell")
+    KERNEL_KINDS = ("cfl_dt", "limiter", "face_x", "face_y", "face_z", "cell", "noise")
 
     def profile_read(self):
-        ms = np.zeros(6)
-        n = np.zeros(6, dtype=np.int64)
+        ms = np.zeros(7)
+        n = np.zeros(7, dtype=np.int64)
         check(lib().hermes_profile_read(self.ctx, ms.ctypes.data_as(C.POINTER(C.c_double)),
                                         n.ctypes.data_as(C.POINTER(C.c_int64))), self.ctx)
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_KINDS)}

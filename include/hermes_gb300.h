@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define HERMES_ABI_VERSION 2
+#define HERMES_ABI_VERSION 3
 
 typedef enum hermes_status {
     HERMES_OK = 0,
@@ -222,9 +222,10 @@ int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);
  * enabled, steps run without the graph and every kernel launch is bracketed
  * by an event pair.  hermes_profile_read synchronises, returns accumulated
  * milliseconds and launch counts per kernel kind and resets them.  Kinds:
- * 0 CFL reduction, 1 limiter, 2 x faces, 3 y faces, 4 z faces, 5 cell update. */
+ * 0 CFL reduction, 1 limiter, 2 x faces, 3 y faces, 4 z faces, 5 cell update,
+ * 6 staged stochastic stress (the four noise kernels of a stage). */
 int hermes_profile_enable(hermes_ctx *ctx, int enable);
-int hermes_profile_read(hermes_ctx *ctx, double *ms /* [6] */, int64_t *launches /* [6] */);
+int hermes_profile_read(hermes_ctx *ctx, double *ms /* [7] */, int64_t *launches /* [7] */);
 
 /* Per-box time and last time step of an ensemble (nbox entries each). */
 int hermes_box_times(hermes_ctx *ctx, double *t, double *dt);

@@ -27,7 +27,7 @@ def test_library_exports_every_symbol(hermes_lib):
 
 
 def test_abi_version_and_config_layout(hermes_lib):
-    assert hermes_lib.hermes_abi_version() == _lib.ABI_VERSION == 2
+    assert hermes_lib.hermes_abi_version() == _lib.ABI_VERSION == 3
     assert hermes_lib.hermes_config_size() == C.sizeof(_lib.HermesConfig)
 
 
@@ -49,3 +49,19 @@ def test_bad_config_rejected_without_gpu(hermes_lib):
     cfg = _lib.to_c(config.Config(nx=0))
     assert hermes_lib.hermes_create(C.byref(cfg), None, C.byref(ctx)) == 1
     assert not ctx.value
+
+
+def test_empty_and_malformed_inputs_rejected_without_gpu(hermes_lib):
+    """An ensemble of no boxes, a box with no cells, unknown boundary codes."""
+    import numpy as np
+    cfg = _lib.to_c(config.Config(nx=4, ny=4, nz=1, nbasis=4, iquad=2))
+    ctx = C.c_void_p()
+    assert hermes_lib.hermes_ensemble_create(C.byref(cfg), 0, None, None, None, None, C.byref(ctx)) == 8
+    dims = np.array([4, 0, 1], dtype=np.int32)
+    assert hermes_lib.hermes_ensemble_create(C.byref(cfg), 1, dims.ctypes.data_as(C.POINTER(C.c_int32)), None, None,
+                                             None, C.byref(ctx)) == 1
+    bad = _lib.to_c(config.Config(nx=4, ny=4, nz=1, nbasis=4, iquad=2))
+    bad.bc[3] = 9
+    assert hermes_lib.hermes_create(C.byref(bad), None, C.byref(ctx)) == 1
+    bad.bc[3] = 4       # inflow is an x-low boundary only
+    assert hermes_lib.hermes_create(C.byref(bad), None, C.byref(ctx)) == 1

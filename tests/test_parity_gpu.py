@@ -47,6 +47,10 @@ RHS_CASES = {
     "nb10_2d_roe_walls_ivis1": (config.Config(nx=6, ny=5, nz=1, nbasis=10, iquad=3, ihllc=2, ivis=1, coll=2.0,
                                               colvis=1.0, xlobc="wall", xhibc="wall"), 0.5),
     "nb8_3d_central_only": (config.Config(nx=4, ny=4, nz=3, nbasis=8, iquad=2, ihllc=0), 0.0),
+    # degenerate extents: one cell across a direction, a single cell
+    "nb8_one_cell_x": (config.Config(nx=1, ny=5, nz=3, nbasis=8, iquad=2, ivis=1, coll=2.0, colvis=1.0), 0.5),
+    "nb4_line_walls": (config.Config(nx=7, ny=1, nz=1, nbasis=4, iquad=2, xlobc="wall", xhibc="noslip"), 0.0),
+    "nb10_single_cell": (config.Config(nx=1, ny=1, nz=1, nbasis=10, iquad=3), 0.0),
     # Murnaghan-Tait equation of state (ieos 2), with the HLLC sound speed's stale 1/rho (flux.f90:533-534)
     "nb4_2d_tait_hllc_walls": (config.Config(nx=6, ny=5, nz=1, nbasis=4, iquad=2, ieos=2, P_1=0.05, P_base=1.0,
                                              xlobc="wall", xhibc="noslip"), 0.0),
@@ -289,3 +293,26 @@ def test_fh_ensemble_conserves_and_fluctuates():
         assert torch.isfinite(v).all()
     sf.add_state(q, base.nbasis, dims, ens.offsets)
     assert all(np.isfinite(x) and x > 0 for x in sf.result().values())
+
+
+def test_periodic_shift_equivariance_at_size():
+    """A size-independent property on a 256^3 grid (16.8 M cells, 5.9 GB per
+    state): on a periodic grid, a forward-Euler stage with a given dt commutes
+    with a shift of the cells, bit for bit, in every direction."""
+    import torch
+    from hermeshd_gb300.solver import Solver
+    cfg = config.Config(nx=256, ny=256, nz=256, nbasis=4, iquad=2, ivis=1, coll=2.0, colvis=1.0, ihllc=1)
+    s = _solver(cfg)
+    q = s.new_state()
+    s.init_state(q, 6)                       # fluid at rest, then a smooth periodic perturbation
+    k = torch.arange(256, device=q.device, dtype=torch.float64) * (2 * np.pi / 256)
+    q[0, 1] += 1e-2 * torch.sin(k)[None, None, :] * torch.cos(2 * k)[None, :, None]
+    q[0, 2] += 1e-2 * torch.sin(3 * k)[:, None, None]
+    q[1, 0] += 1e-3 * torch.cos(k)[None, None, :]
+    dt = 0.5 * s.get_min_dt(q)
+    e = s.euler_stage(q.clone(), dt)
+    for dim, shift in ((4, 37), (3, -11), (2, 5)):
+        es = s.euler_stage(q.roll(shift, dims=dim).contiguous(), dt)
+        assert torch.equal(es, e.roll(shift, dims=dim)), dim
+    del e, es
+    torch.cuda.empty_cache()
