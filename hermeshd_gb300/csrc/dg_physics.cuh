@@ -59,12 +59,14 @@ __device__ __forceinline__ void normals9(unsigned long long seed, NoiseCtr nc, u
             sincos(__dmul_rn(6.283185307179586476925286766559, u2), &s, &co);
             z0 = __dmul_rn(r, co); z1 = __dmul_rn(r, s);
         } else {
-            // the top 24 bits of the same words
+            // the top 24 bits of the same words; the hardware log2 and sin/cos
+            // (absolute error ~2^-21 on (-pi, pi)), with the angle moved to
+            // (-pi, pi) by cos(t - pi) = -cos t, sin(t - pi) = -sin t
             float u1 = __fmul_rn(__fadd_rn((float)(c[0] >> 8), 0.5f), 1.0f / 16777216.0f);
             float u2 = __fmul_rn(__fadd_rn((float)(c[2] >> 8), 0.5f), 1.0f / 16777216.0f);
-            float r = sqrtf(__fmul_rn(-2.0f, logf(u1))), s, co;
-            sincosf(__fmul_rn(6.2831853071795864769f, u2), &s, &co);
-            z0 = __fmul_rn(r, co); z1 = __fmul_rn(r, s);
+            float r = sqrtf(__fmul_rn(-2.0f, __logf(u1))), s, co;
+            __sincosf(__fmul_rn(6.2831853071795864769f, __fsub_rn(u2, 0.5f)), &s, &co);
+            z0 = -__fmul_rn(r, co); z1 = -__fmul_rn(r, s);
         }
         if (2 * sub < 9) G[2 * sub] = z0;
         if (2 * sub + 1 < 9) G[2 * sub + 1] = z1;
