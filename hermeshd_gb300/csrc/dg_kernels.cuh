@@ -296,9 +296,12 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
     const long long lf = gf - B.face0[DIR];
     const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
     const int ex = DIR == 0 ? B.nfp[0] : n0, ey = DIR == 1 ? B.nfp[1] : n1;
-    const int i = (int)(lf % ex);
-    const int j = (int)((lf / ex) % ey);
-    const int k = (int)(lf / ((long long)ex * ey));
+    // 32-bit division (a box has fewer than 2^31 faces per direction, checked
+    // at context creation): a 64-bit division costs as much as an FP32 face
+    const unsigned lfu = (unsigned)lf, t = lfu / (unsigned)ex;
+    const int i = (int)(lfu - t * (unsigned)ex);
+    const int j = (int)(t % (unsigned)ey);
+    const int k = (int)(t / (unsigned)ey);
     const int n = B.n[DIR];
     const int s = DIR == 0 ? i : DIR == 1 ? j : k;       // face plane
     const bool dedup = B.nfp[DIR] == n;                    // both ends periodic: n planes
@@ -776,7 +779,8 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
     for (int d = 0; d < 3; ++d) { cx.fm[d] = 0; cx.fp[d] = 0; cx.nfd[d] = 1; }
     if (cx.act) {
         const int n0 = B.n[0], n1 = B.n[1];
-        const int c[3] = {(int)(cx.le % n0), (int)((cx.le / n0) % n1), (int)(cx.le / ((long long)n0 * n1))};
+        const unsigned leu = (unsigned)cx.le, t = leu / (unsigned)n0;   // fewer than 2^31 cells per box
+        const int c[3] = {(int)(leu - t * (unsigned)n0), (int)(t % (unsigned)n1), (int)(t / (unsigned)n1)};
         for (int d = 0; d < 3; ++d) {
             const int e0 = d == 0 ? B.nfp[0] : B.n[0], e1 = d == 1 ? B.nfp[1] : B.n[1], e2 = d == 2 ? B.nfp[2] : B.n[2];
             cx.nfd[d] = (long long)e0 * e1 * e2;

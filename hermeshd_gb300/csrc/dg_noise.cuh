@@ -7,7 +7,8 @@
 // draws are latency-bound; here every draw is one thread of a full-occupancy
 // kernel, and the consumers read 6 values per point.  The counters are the
 // same, so the staged and the inline draws are the same numbers.
-//   k_noise_cell  thread per (cell, direction, quadrature point): the
+//   k_noise_cell  thread per (cell, direction, quadrature point), the
+//                 (direction, point) pair in blockIdx.y (no 64-bit division): the
 //                 interior stress of flux call kind 3 + d, written as
 //                 [d][point][component][cell]
 //   k_noise_face  thread per (face, point, side) of one direction: the two
@@ -29,13 +30,13 @@ struct NoiseArgs {
     unsigned stage;
 };
 
+// grid (cells / NOISE_TPB, 3 NPG): blockIdx.y = d * NPG + g
 template <class T, class TB>
 __global__ void __launch_bounds__(NOISE_TPB) k_noise_cell(T* __restrict__ out, NoiseArgs a) {
     const long long ncl = a.G.ncell;
-    const long long idx = (long long)blockIdx.x * NOISE_TPB + threadIdx.x;
-    if (idx >= ncl * 3 * TB::NPG) return;
-    const long long gc = idx % ncl;
-    const int r = (int)(idx / ncl);                 // d * NPG + g
+    const long long gc = (long long)blockIdx.x * NOISE_TPB + threadIdx.x;
+    if (gc >= ncl) return;
+    const int r = blockIdx.y;
     const int d = r / TB::NPG, g = r % TB::NPG;
     const int bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
     const Box& B = a.G.boxes[bx];
@@ -45,13 +46,13 @@ __global__ void __launch_bounds__(NOISE_TPB) k_noise_cell(T* __restrict__ out, N
     for (int c = 0; c < 6; ++c) out[((long long)r * 6 + c) * ncl + gc] = S[c];
 }
 
+// grid (faces / NOISE_TPB, 2 NF): blockIdx.y = side * NF + P
 template <class T, class TB, int DIR>
 __global__ void __launch_bounds__(NOISE_TPB) k_noise_face(T* __restrict__ out, NoiseArgs a) {
     const long long nfa = a.G.nface[DIR];
-    const long long idx = (long long)blockIdx.x * NOISE_TPB + threadIdx.x;
-    if (idx >= nfa * 2 * TB::NF) return;
-    const long long gf = idx % nfa;
-    const int r = (int)(idx / nfa);                 // side * NF + P
+    const long long gf = (long long)blockIdx.x * NOISE_TPB + threadIdx.x;
+    if (gf >= nfa) return;
+    const int r = blockIdx.y;
     const int P = r % TB::NF, side = r / TB::NF;
     const int bx = find_box(a.G.boxes, a.G.nbox, gf, [](const Box& b) { return b.face0[DIR]; });
     const Box& B = a.G.boxes[bx];
@@ -66,12 +67,15 @@ __global__ void __launch_bounds__(NOISE_TPB) k_noise_face(T* __restrict__ out, N
 template <class T, int NB, int NQD>
 cudaError_t noise_launch(void* cellbuf, void* facebuf, const NoiseArgs& a, cudaStream_t s) {
     using TB = hermes_tab::Tab<NB, NQD>;
-    const long long nc = a.G.ncell * 3 * TB::NPG;
-    if (nc > 0) k_noise_cell<T, TB><<<(unsigned)((nc + NOISE_TPB - 1) / NOISE_TPB), NOISE_TPB, 0, s>>>(static_cast<T*>(cellbuf), a);
-    const long long n0 = a.G.nface[0] * 2 * TB::NF, n1 = a.G.nface[1] * 2 * TB::NF, n2 = a.G.nface[2] * 2 * TB::NF;
-    if (n0 > 0) k_noise_face<T, TB, 0><<<(unsigned)((n0 + NOISE_TPB - 1) / NOISE_TPB), NOISE_TPB, 0, s>>>(static_cast<T*>(facebuf), a);
-    if (n1 > 0) k_noise_face<T, TB, 1><<<(unsigned)((n1 + NOISE_TPB - 1) / NOISE_TPB), NOISE_TPB, 0, s>>>(static_cast<T*>(facebuf), a);
-    if (n2 > 0) k_noise_face<T, TB, 2><<<(unsigned)((n2 + NOISE_TPB - 1) / NOISE_TPB), NOISE_TPB, 0, s>>>(static_cast<T*>(facebuf), a);
+    auto blocks = [](long long n) { return (unsigned)((n + NOISE_TPB - 1) / NOISE_TPB); };
+    if (a.G.ncell > 0)
+        k_noise_cell<T, TB><<<dim3(blocks(a.G.ncell), 3 * TB::NPG), NOISE_TPB, 0, s>>>(static_cast<T*>(cellbuf), a);
+    if (a.G.nface[0] > 0)
+        k_noise_face<T, TB, 0><<<dim3(blocks(a.G.nface[0]), 2 * TB::NF), NOISE_TPB, 0, s>>>(static_cast<T*>(facebuf), a);
+    if (a.G.nface[1] > 0)
+        k_noise_face<T, TB, 1><<<dim3(blocks(a.G.nface[1]), 2 * TB::NF), NOISE_TPB, 0, s>>>(static_cast<T*>(facebuf), a);
+    if (a.G.nface[2] > 0)
+        k_noise_face<T, TB, 2><<<dim3(blocks(a.G.nface[2]), 2 * TB::NF), NOISE_TPB, 0, s>>>(static_cast<T*>(facebuf), a);
     return cudaGetLastError();
 }
 

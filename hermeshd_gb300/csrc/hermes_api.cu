@@ -430,6 +430,15 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     if (dims)
         for (int i = 0; i < 3 * nbox; ++i)
             if (dims[i] < 1) return HERMES_ERR_CONFIG;
+    // index arithmetic inside a box is 32-bit: fewer than 2^31 cells and faces per box
+    for (int i = 0; i < nbox; ++i) {
+        const long long n0 = dims ? dims[3 * i] : cfg->nx, n1 = dims ? dims[3 * i + 1] : cfg->ny,
+                        n2 = dims ? dims[3 * i + 2] : cfg->nz;
+        if ((n0 + 1) * (n1 + 1) * (n2 + 1) >= (1ll << 31)) {
+            fprintf(stderr, "hermes_create: a box holds 2^31 cells or faces or more\n");
+            return HERMES_ERR_SHAPE;
+        }
+    }
     hermes_ctx* c = new (std::nothrow) hermes_ctx();
     if (!c) return HERMES_ERR_ALLOC;
     c->cfg = *cfg;
