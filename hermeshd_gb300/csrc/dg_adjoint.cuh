@@ -10,8 +10,10 @@
 // column by column with dual numbers run through the forward physics code.
 //
 //   k_face_adj  per face point: lambda of the face flux from mu of the two
-//               cells that own the face, J^T of the numerical flux, boundary
-//               ghost maps transposed; writes the adjoint of both traces
+//               cells that own the face, J^T of the numerical flux (one
+//               hand-derived reverse sweep, dg_flux_vjp.cuh; or, as a check,
+//               forward-mode dual passes), boundary ghost maps transposed;
+//               writes the adjoint of both traces
 //   k_cell_adj  per cell: gathers the trace adjoints, volume and source
 //               transposes; writes nu = (dR/dQ)^T mu, or mu - dt*nu
 //
@@ -21,6 +23,7 @@
 #pragma once
 
 #include "dg_dual.cuh"
+#include "dg_flux_vjp.cuh"
 #include "dg_launch.cuh"
 
 namespace hermes {
@@ -53,7 +56,7 @@ __device__ __forceinline__ double trace_of(const double* __restrict__ Qb, long l
     return ((s.mask >> v) & 1u) ? acc : 0.0;
 }
 
-template <class TB, int DIR, int P>
+template <class TB, int DIR, int P, bool REV>
 __device__ __forceinline__ void face_adj_point(const double* __restrict__ Q, const double* __restrict__ mu,
                                                double* __restrict__ tadj, const AdjArgs& a, long long gf) {
     const Geom& G = a.G;
@@ -147,57 +150,69 @@ __device__ __forceinline__ void face_adj_point(const double* __restrict__ Q, con
             });
         lamF[v] = di * sacc;
     }
-    // J^T lamF.  Hydro columns (rh..en): one dual pass each.  Stress columns:
-    // for ivis 0/1 the stresses enter only the point fluxes of the normal
-    // direction, linearly (f[M_i] += P_{d i}, f[E] += P_{d i} v_i,
-    // flux.f90:87-89), and every numerical flux takes f_L, f_R with weights
-    // w_L + w_R = 1 (central and Roe 1/2 each; HLLC 1 on the side its wave
-    // selection picks), so column P_{d i} of a side is w (lamF[M_i] + lamF[E] v_i).
     double lamL[NQ], lamR[NQ];
-    const Dual S0[6] = {Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0)};
-    constexpr int PN[3] = {DIR == 0 ? PXX : DIR == 1 ? PXY : PXZ, DIR == 0 ? PXY : DIR == 1 ? PYY : PYZ,
-                           DIR == 0 ? PXZ : DIR == 1 ? PYZ : PZZ};   // P_{d x}, P_{d y}, P_{d z}
-    double wL = 0.0;
-#pragma unroll 1
-    for (int pass = -1; pass < 10; ++pass) {
-        // pass -1: seed P_{d d} of the left trace, whose derivative in the
-        // normal-momentum row is w_L; passes 0..9: hydro columns of L then R
-        const int side = pass < 0 ? 0 : pass / 5, jv = pass < 0 ? PN[DIR] : pass % 5;
-        const TraceSrc& src = side == 0 ? L : R;
-        if (pass >= 0) {
-            (side == 0 ? lamL : lamR)[jv] = 0.0;
-            if (src.cell < 0 || !((src.mask >> jv) & 1u)) continue;
-        }
-        Dual dL[NQ], dR[NQ], F[NQ];
+    if constexpr (REV) {
+        // one reverse sweep through the numerical flux (dg_flux_vjp.cuh)
+        face_flux_vjp<DIR>(ph, qL, qR, lamF, lamL, lamR);
+        // a zero ghost or a ghost component forced to zero owns no trace
 #pragma unroll
         for (int v = 0; v < NQ; ++v) {
-            dL[v] = Dual(qL[v], (side == 0 && v == jv) ? 1.0 : 0.0);
-            dR[v] = Dual(qR[v], (side == 1 && v == jv) ? 1.0 : 0.0);
+            if (L.cell < 0 || !((L.mask >> v) & 1u)) lamL[v] = 0.0;
+            if (R.cell < 0 || !((R.mask >> v) & 1u)) lamR[v] = 0.0;
         }
-        face_flux_fn<Dual, DIR>(ph, dL, dR, S0, S0, Dual(0.0), F);
-        if (pass < 0) {
-            wL = F[MN].d;
-            continue;
+    } else {
+        // J^T lamF.  Hydro columns (rh..en): one dual pass each.  Stress columns:
+        // for ivis 0/1 the stresses enter only the point fluxes of the normal
+        // direction, linearly (f[M_i] += P_{d i}, f[E] += P_{d i} v_i,
+        // flux.f90:87-89), and every numerical flux takes f_L, f_R with weights
+        // w_L + w_R = 1 (central and Roe 1/2 each; HLLC 1 on the side its wave
+        // selection picks), so column P_{d i} of a side is w (lamF[M_i] + lamF[E] v_i).
+        const Dual S0[6] = {Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0), Dual(0.0)};
+        constexpr int PN[3] = {DIR == 0 ? PXX : DIR == 1 ? PXY : PXZ, DIR == 0 ? PXY : DIR == 1 ? PYY : PYZ,
+                               DIR == 0 ? PXZ : DIR == 1 ? PYZ : PZZ};   // P_{d x}, P_{d y}, P_{d z}
+        double wL = 0.0;
+#pragma unroll 1
+        for (int pass = -1; pass < 10; ++pass) {
+            // pass -1: seed P_{d d} of the left trace, whose derivative in the
+            // normal-momentum row is w_L; passes 0..9: hydro columns of L then R
+            const int side = pass < 0 ? 0 : pass / 5, jv = pass < 0 ? PN[DIR] : pass % 5;
+            const TraceSrc& src = side == 0 ? L : R;
+            if (pass >= 0) {
+                (side == 0 ? lamL : lamR)[jv] = 0.0;
+                if (src.cell < 0 || !((src.mask >> jv) & 1u)) continue;
+            }
+            Dual dL[NQ], dR[NQ], F[NQ];
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) {
+                dL[v] = Dual(qL[v], (side == 0 && v == jv) ? 1.0 : 0.0);
+                dR[v] = Dual(qR[v], (side == 1 && v == jv) ? 1.0 : 0.0);
+            }
+            face_flux_fn<Dual, DIR>(ph, dL, dR, S0, S0, Dual(0.0), F);
+            if (pass < 0) {
+                wL = F[MN].d;
+                continue;
+            }
+            double acc = 0.0;
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) acc = fma(lamF[v], F[v].d, acc);
+            (side == 0 ? lamL : lamR)[jv] = acc;
         }
-        double acc = 0.0;
 #pragma unroll
-        for (int v = 0; v < NQ; ++v) acc = fma(lamF[v], F[v].d, acc);
-        (side == 0 ? lamL : lamR)[jv] = acc;
-    }
+        for (int side = 0; side < 2; ++side) {
+            const TraceSrc& src = side == 0 ? L : R;
+            const double* qs = side == 0 ? qL : qR;
+            double* lam = side == 0 ? lamL : lamR;
+            const double w = side == 0 ? wL : 1.0 - wL;
+            const double dni = 1.0 / qs[RH];
+            const double vel[3] = {qs[MX] * dni, qs[MY] * dni, qs[MZ] * dni};
 #pragma unroll
-    for (int side = 0; side < 2; ++side) {
-        const TraceSrc& src = side == 0 ? L : R;
-        const double* qs = side == 0 ? qL : qR;
-        double* lam = side == 0 ? lamL : lamR;
-        const double w = side == 0 ? wL : 1.0 - wL;
-        const double dni = 1.0 / qs[RH];
-        const double vel[3] = {qs[MX] * dni, qs[MY] * dni, qs[MZ] * dni};
+            for (int v = PXX; v < NQ; ++v) lam[v] = 0.0;
+            if (src.cell < 0) continue;
 #pragma unroll
-        for (int v = PXX; v < NQ; ++v) lam[v] = 0.0;
-        if (src.cell < 0) continue;
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-            if ((src.mask >> PN[i]) & 1u) lam[PN[i]] = w * fma(lamF[EN], vel[i], lamF[MX + i]);
+            for (int i = 0; i < 3; ++i)
+                if ((src.mask >> PN[i]) & 1u) lam[PN[i]] = w * fma(lamF[EN], vel[i], lamF[MX + i]);
+        }
+
     }
     // a ghost made from a cell's own trace hands its adjoint to that trace
     if (ghostL_from_R) {
@@ -217,7 +232,7 @@ __device__ __forceinline__ void face_adj_point(const double* __restrict__ Q, con
     }
 }
 
-template <class TB, int DIR>
+template <class TB, int DIR, bool REV>
 __global__ void __launch_bounds__(ADJ_TPB) k_face_adj(const double* __restrict__ Q, const double* __restrict__ mu,
                                                       double* __restrict__ tadj, AdjArgs a) {
     const long long gf = (long long)blockIdx.x * ADJ_TPB + threadIdx.x;
@@ -225,7 +240,7 @@ __global__ void __launch_bounds__(ADJ_TPB) k_face_adj(const double* __restrict__
     const int p = blockIdx.y;
     sfor<TB::NF>([&](auto pp) {
         constexpr int P = decltype(pp)::value;
-        if (p == P) face_adj_point<TB, DIR, P>(Q, mu, tadj, a, gf);
+        if (p == P) face_adj_point<TB, DIR, P, REV>(Q, mu, tadj, a, gf);
     });
 }
 
@@ -373,9 +388,15 @@ cudaError_t adj_launch(const double* Q, const double* mu, double* tadj, double* 
         const long long n = a.G.nface[d];
         if (n <= 0) continue;
         dim3 grid((unsigned)((n + ADJ_TPB - 1) / ADJ_TPB), TB::NF);
-        if (d == 0) k_face_adj<TB, 0><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
-        else if (d == 1) k_face_adj<TB, 1><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
-        else k_face_adj<TB, 2><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+        if (a.dual) {   // forward-mode dual passes (the check on the reverse sweep)
+            if (d == 0) k_face_adj<TB, 0, false><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else if (d == 1) k_face_adj<TB, 1, false><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else k_face_adj<TB, 2, false><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+        } else {
+            if (d == 0) k_face_adj<TB, 0, true><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else if (d == 1) k_face_adj<TB, 1, true><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else k_face_adj<TB, 2, true><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+        }
     }
     if (a.G.ncell > 0)
         k_cell_adj<TB><<<(unsigned)((a.G.ncell + ADJ_TPB - 1) / ADJ_TPB), ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);

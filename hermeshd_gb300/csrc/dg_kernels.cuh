@@ -417,8 +417,16 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
     for (int v = 0; v < NQ; ++v) fb[(long long)(v * TB::NF + P) * nfd + lf] = F[v] * sc;
 }
 
+// resident blocks per SM the face kernel's register allocation must allow:
+// FP64 is FP64-pipe bound at 4 (128 registers); FP32 has the arithmetic to
+// spare and gains from more resident warps (6 blocks: 80 registers)
+template <class T>
+struct FaceMinBlocks {
+    static constexpr int value = std::is_same<T, float>::value ? 6 : 4;
+};
+
 template <class T, class TB, int DIR, bool NOISE>
-__global__ void __launch_bounds__(FACE_TPB, 4) k_face(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
+__global__ void __launch_bounds__(FACE_TPB, (FaceMinBlocks<T>::value)) k_face(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
     long long gf = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gf >= a.G.nface[DIR]) return;
     const int p = blockIdx.y;

@@ -84,6 +84,7 @@ struct AdjArgs {
     Phys ph;
     const BoxState* st;
     int mode;       // 0: out = nu = (dR/dQ)^T mu; 1: out = mu - dt*nu
+    int dual;       // face flux VJP by forward-mode dual passes instead of the reverse sweep
 };
 
 // (Q, mu, trace-adjoint scratch of 2x the face-flux size, out, args, stream)

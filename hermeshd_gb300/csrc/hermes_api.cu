@@ -13,6 +13,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -890,6 +891,13 @@ std::string adjoint_unsupported(const hermes_config& c, int nbox) {
     return "";
 }
 
+// HERMES_ADJOINT_DUAL=1: the face flux VJP by forward-mode dual passes, the
+// independent check on the hand-derived reverse sweep
+int adjoint_dual() {
+    const char* e = std::getenv("HERMES_ADJOINT_DUAL");
+    return (e && e[0] == '1') ? 1 : 0;
+}
+
 int adj_prepare(hermes_ctx* c) {
     const std::string why = adjoint_unsupported(c->cfg, c->G.nbox);
     if (!why.empty()) return fail(c, HERMES_ERR_CONFIG, why);
@@ -915,7 +923,7 @@ int hermes_rhs_vjp(hermes_ctx* c, const void* q, const void* mu, void* nu) {
     if (rc) return rc;
     rc = adj_prepare(c);
     if (rc) return leave(c, rc);
-    AdjArgs a{c->G, c->ph, c->d_st, 0};
+    AdjArgs a{c->G, c->ph, c->d_st, 0, adjoint_dual()};
     cudaError_t e = c->adj(static_cast<const double*>(q), static_cast<const double*>(mu), c->d_tadj,
                            static_cast<double*>(nu), a, c->stream);
     if (e != cudaSuccess) return leave(c, cuda_fail(c, "adjoint launch", e));
@@ -939,7 +947,7 @@ int hermes_stage_vjp(hermes_ctx* c, const void* q_in, const void* e_out, const v
     k_stage_pre<<<c->npart, 256, 0, c->stream>>>(static_cast<const double*>(lam_out), static_cast<const double*>(e_out),
                                                  c->d_mu, c->d_part, n, c->G.ncell, c->cfg.ivis, dt, faci);
     if (dcoll) k_sum_partials<<<1, 256, 0, c->stream>>>(c->d_part, c->npart, c->d_sum);
-    AdjArgs a{c->G, c->ph, c->d_st, 1};
+    AdjArgs a{c->G, c->ph, c->d_st, 1, adjoint_dual()};
     cudaError_t e = c->adj(static_cast<const double*>(q_in), c->d_mu, c->d_tadj, static_cast<double*>(lam_in), a, c->stream);
     if (e != cudaSuccess) return leave(c, cuda_fail(c, "adjoint launch", e));
     if (dcoll) {
