@@ -472,6 +472,7 @@ template <class T>
 struct CellCtx {
     const T* qs_base;
     T* qs;            // shared column base of this block
+    T* ub;            // exchange buffer of the point values, [2][NQ][2][CELL_CPB]
     int lc;           // cell slot in the block
     bool act;
     int bx;
@@ -487,105 +488,196 @@ struct CellCtx {
     bool bad;
 };
 
+// The interior points in x-mirror orbits: chunk c is the pair gA (x = +xq)
+// and gB (x = -xq) with the same (y, z), or, for an odd point count, the one
+// point at x = 0.  Every table row of gB is the row of gA with the sign of
+// the basis function's parity in x (checked at compile time), so a
+// variable's values at the pair are E + O and E - O (E, O: the sums over the
+// even and the odd functions at gA), and the pair's contributions to a
+// quadrature sum are c (f_A + f_B) or c (f_A - f_B): half the table products.
+template <class TB>
+struct XOrbit {
+    static constexpr int NE = TB::NQD, NE2 = NE * NE, NPAIR = NE / 2;
+    static constexpr int NCH = (NPAIR + (NE & 1)) * NE2;
+    static constexpr bool pair(int c) { return c / NE2 < NPAIR; }
+    static constexpr int gA(int c) { return pair(c) ? (NE - 1 - c / NE2) * NE2 + c % NE2 : NPAIR * NE2 + c % NE2; }
+    static constexpr int gB(int c) { return pair(c) ? (c / NE2) * NE2 + c % NE2 : gA(c); }
+};
+
+// sum_g SRC(g, b) INT(g, b2): the quadrature of the source projection applied
+// to a field that is linear in the state.  The Gauss rules integrate these
+// products exactly and the basis is orthogonal with SRC normalised by cbasis,
+// so this is the identity to rounding (asserted where it is used): a source
+// linear in the state (ivis 0 relaxation -coll P_ij, the body force)
+// projects to the same linear map of the coefficients.
+template <class TB>
+__host__ __device__ constexpr double src_gram(int b, int b2) {
+    double s = 0.0;
+    for (int g = 0; g < TB::NPG; ++g) s += TB::SRC(g, b) * TB::INT(g, b2);
+    return s;
+}
+template <class TB>
+__host__ __device__ constexpr bool src_gram_is_identity() {
+    for (int b = 0; b < TB::NB; ++b)
+        for (int b2 = 0; b2 < TB::NB; ++b2) {
+            const double e = src_gram<TB>(b, b2) - (b == b2 ? 1.0 : 0.0);
+            if (e > 1e-14 || e < -1e-14) return false;
+        }
+    return true;
+}
+
 // phase 1: volume quadrature and point sources of one group's variables
-// (flux.f90:751-928, sources.f90:28-78); acc collects volume + source
+// (flux.f90:751-928, sources.f90:28-78); acc collects volume + source.  Each
+// thread evaluates only its own group's variables at the points and the two
+// threads of a cell swap them through the exchange buffer (one block barrier
+// per orbit; every thread of the block, active or not, runs the same loop).
 template <class T, class TB, int GRP, bool NOISE>
 __device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T (&acc)[6][TB::NB]) {
+    using XO = XOrbit<TB>;
     constexpr int NB = TB::NB, NPG = TB::NPG;
     constexpr int GV0 = GRP == 0 ? 0 : PXX;
     constexpr int GNV = GRP == 0 ? 5 : 6;
     const Phys& ph = a.ph;
-    // coefficients are re-read from shared memory at every point: held in
-    // registers across the point loop they would cost ~NB*NQ registers
     const volatile T* qs = cx.qs;
+    volatile T* ub = cx.ub;   // [2][NQ][2][CELL_CPB]
     const int lc = cx.lc;
-    // the stress thread needs the stress values at the points for the
-    // 10-moment fluxes (ivis 2, 3) and the ivis-0 source; ivis 1 needs only
-    // the velocity
-    const bool need_all = GRP == 0 || ph.ivis != 1;
-    sfor_seq<NPG>([&](auto gg) {
-        constexpr int g = decltype(gg)::value;
-        T u[NQ];
-        sfor<NQ>([&](auto vv) {
-            constexpr int v = decltype(vv)::value;
-            if (v <= MZ || need_all) {
-                T s = T(0);
+    const bool act = cx.act;
+    // the stress thread needs its own values at the points for the 10-moment
+    // fluxes (ivis 2, 3); ivis 0 and 1 need only the velocity there
+    const bool need_all = GRP == 0 || ph.ivis >= 2;
+    sfor_seq<XO::NCH>([&](auto cc) {
+        constexpr int c = decltype(cc)::value;
+        constexpr bool PAIR = XO::pair(c);
+        constexpr int gA = XO::gA(c), gB = XO::gB(c);
+        constexpr int NK = PAIR ? 2 : 1;
+        volatile T* ubc = ub + (c & 1) * (NQ * 2 * CELL_CPB);
+        if (act) {
+            sfor<GNV>([&](auto mm) {
+                constexpr int v = GV0 + decltype(mm)::value;
+                T E = T(0), O = T(0);
                 sfor<NB>([&](auto bb) {
                     constexpr int b = decltype(bb)::value;
-                    constexpr double c = TB::INT(g, b);
-                    if constexpr (c != 0.0) s = fma(T(c), qs[(b * NQ + v) * CELL_CPB + lc], s);
+                    constexpr double cA = TB::INT(gA, b), cB = TB::INT(gB, b);
+                    static_assert(cB == cA || cB == -cA, "interior table not mirror-symmetric in x");
+                    if constexpr (cA != 0.0) {
+                        const T q = qs[(b * NQ + v) * CELL_CPB + lc];
+                        if constexpr (cB == cA) E = fma(T(cA), q, E);
+                        else O = fma(T(cA), q, O);
+                    }
                 });
-                u[v] = s;
-            } else {
-                u[v] = T(0);
-            }
-        });
-        const Prim<T> w = primitives(ph, u);
-        sfor<3>([&](auto dd) {
-            constexpr int d = decltype(dd)::value;
-            T S[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-            if constexpr (GRP == 0 && NOISE) {
-                if (a.noise) {
-                    // [direction][point][component][cell] (dg_noise.cuh)
-                    const T* nb = static_cast<const T*>(a.noise);
-                    const long long gc = cx.B->cell0 + cx.le, ncl = a.G.ncell;
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) S[c] = nb[((long long)(d * NPG + g) * 6 + c) * ncl + gc];
+                if constexpr (PAIR) {
+                    ubc[(v * 2 + 0) * CELL_CPB + lc] = E + O;
+                    ubc[(v * 2 + 1) * CELL_CPB + lc] = E - O;
                 } else {
-                    random_stress<T>(ph, cx.B->seed, cx.nctr, 3 + d, (unsigned long long)cx.le, g, S);
-                }
-            }
-            T f[NQ];
-            point_flux<T, d>(ph, u, w, S, f);
-            T fs[GNV];
-            sfor<GNV>([&](auto mm) { fs[decltype(mm)::value] = f[GV0 + decltype(mm)::value] * cx.di[d]; });
-            sfor<NB>([&](auto bb) {
-                constexpr int b = decltype(bb)::value;
-                constexpr double c = vtab<TB, d>(g, b);
-                if constexpr (c != 0.0) {
-                    sfor<GNV>([&](auto mm) {
-                        constexpr int m = decltype(mm)::value;
-                        acc[m][b] = fma(T(c), fs[m], acc[m][b]);
-                    });
+                    ubc[(v * 2 + 0) * CELL_CPB + lc] = E;
                 }
             });
-        });
-        T s[GNV];
-        bool any = false;
-        sfor<GNV>([&](auto mm) { s[decltype(mm)::value] = T(0); });
-        if (GRP == 0) {
-            if (ph.body_force != 0.0) {   // body force (no reference counterpart)
-                s[MX] = u[RH] * T(ph.body_force);
-                s[EN] = u[MX] * T(ph.body_force);
-                any = true;
-            }
-        } else if (ph.ivis == 0) {        // sources.f90:37-43
-            sfor<6>([&](auto mm) { s[decltype(mm)::value] = -T(ph.coll) * u[PXX + decltype(mm)::value]; });
-            any = true;
-        } else if (ph.ivis == 2) {        // sources.f90:51-69
-            const T vx2 = w.vx * w.vx, vy2 = w.vy * w.vy, vz2 = w.vz * w.vz;
-            const T colldn = T(ph.coll) * w.dn, c1d3 = T(1.0 / 3.0);
-            s[0] = colldn * (T(2) * vx2 - vy2 - vz2) * c1d3;
-            s[1] = colldn * (T(2) * vy2 - vz2 - vx2) * c1d3;
-            s[2] = colldn * (T(2) * vz2 - vx2 - vy2) * c1d3;
-            s[3] = colldn * w.vx * w.vy;
-            s[4] = colldn * w.vx * w.vz;
-            s[5] = colldn * w.vy * w.vz;
-            any = true;
         }
-        if (any) {
-            sfor<NB>([&](auto bb) {
-                constexpr int b = decltype(bb)::value;
-                constexpr double c = TB::SRC(g, b);
-                if constexpr (c != 0.0) {
-                    sfor<GNV>([&](auto mm) {
-                        constexpr int m = decltype(mm)::value;
-                        acc[m][b] = fma(T(c), s[m], acc[m][b]);
-                    });
-                }
+        block_sync_split();
+        if (act) {
+            T u[NK][NQ];
+            Prim<T> w[NK];
+            sfor<NK>([&](auto kk) {
+                constexpr int k = decltype(kk)::value;
+                sfor<NQ>([&](auto vv) {
+                    constexpr int v = decltype(vv)::value;
+                    u[k][v] = (v <= MZ || need_all) ? T(ubc[(v * 2 + k) * CELL_CPB + lc]) : T(0);
+                });
+                w[k] = primitives(ph, u[k]);
             });
+            sfor<3>([&](auto dd) {
+                constexpr int d = decltype(dd)::value;
+                T fs[NK][GNV];
+                sfor<NK>([&](auto kk) {
+                    constexpr int k = decltype(kk)::value;
+                    constexpr int g = k == 0 ? gA : gB;
+                    T S[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+                    if constexpr (GRP == 0 && NOISE) {
+                        if (a.noise) {
+                            // [direction][point][component][cell] (dg_noise.cuh)
+                            const T* nb = static_cast<const T*>(a.noise);
+                            const long long gc = cx.B->cell0 + cx.le, ncl = a.G.ncell;
+#pragma unroll
+                            for (int s = 0; s < 6; ++s) S[s] = nb[((long long)(d * NPG + g) * 6 + s) * ncl + gc];
+                        } else {
+                            random_stress<T>(ph, cx.B->seed, cx.nctr, 3 + d, (unsigned long long)cx.le, g, S);
+                        }
+                    }
+                    T f[NQ];
+                    point_flux<T, d>(ph, u[k], w[k], S, f);
+                    sfor<GNV>([&](auto mm) { fs[k][decltype(mm)::value] = f[GV0 + decltype(mm)::value] * cx.di[d]; });
+                });
+                sfor<NB>([&](auto bb) {
+                    constexpr int b = decltype(bb)::value;
+                    constexpr double cA = vtab<TB, d>(gA, b), cB = vtab<TB, d>(gB, b);
+                    static_assert(cB == cA || cB == -cA, "volume table not mirror-symmetric in x");
+                    if constexpr (cA != 0.0) {
+                        sfor<GNV>([&](auto mm) {
+                            constexpr int m = decltype(mm)::value;
+                            T fc;
+                            if constexpr (!PAIR) fc = fs[0][m];
+                            else if constexpr (cB == cA) fc = fs[0][m] + fs[NK - 1][m];
+                            else fc = fs[0][m] - fs[NK - 1][m];
+                            acc[m][b] = fma(T(cA), fc, acc[m][b]);
+                        });
+                    }
+                });
+            });
+            // sources nonlinear in the state, by quadrature (ivis 2: sources.f90:51-69)
+            if (GRP == 1 && ph.ivis == 2) {
+                T s[NK][6];
+                sfor<NK>([&](auto kk) {
+                    constexpr int k = decltype(kk)::value;
+                    const Prim<T>& wk = w[k];
+                    const T vx2 = wk.vx * wk.vx, vy2 = wk.vy * wk.vy, vz2 = wk.vz * wk.vz;
+                    const T colldn = T(ph.coll) * wk.dn, c1d3 = T(1.0 / 3.0);
+                    s[k][0] = colldn * (T(2) * vx2 - vy2 - vz2) * c1d3;
+                    s[k][1] = colldn * (T(2) * vy2 - vz2 - vx2) * c1d3;
+                    s[k][2] = colldn * (T(2) * vz2 - vx2 - vy2) * c1d3;
+                    s[k][3] = colldn * wk.vx * wk.vy;
+                    s[k][4] = colldn * wk.vx * wk.vz;
+                    s[k][5] = colldn * wk.vy * wk.vz;
+                });
+                sfor<NB>([&](auto bb) {
+                    constexpr int b = decltype(bb)::value;
+                    constexpr double cA = TB::SRC(gA, b), cB = TB::SRC(gB, b);
+                    static_assert(cB == cA || cB == -cA, "source table not mirror-symmetric in x");
+                    if constexpr (cA != 0.0) {
+                        sfor<6>([&](auto mm) {
+                            constexpr int m = decltype(mm)::value;
+                            T sc;
+                            if constexpr (!PAIR) sc = s[0][m];
+                            else if constexpr (cB == cA) sc = s[0][m] + s[NK - 1][m];
+                            else sc = s[0][m] - s[NK - 1][m];
+                            acc[m][b] = fma(T(cA), sc, acc[m][b]);
+                        });
+                    }
+                });
+            }
         }
     });
+    if (!act) return;
+    // sources linear in the state: their projection is the same linear map of
+    // the coefficients (src_gram is the identity), sources.f90:37-43 and the
+    // body force (no reference counterpart)
+    static_assert(src_gram_is_identity<TB>(), "source projection of a linear field is not the identity");
+    if (GRP == 0 && ph.body_force != 0.0) {
+        const T bf = T(ph.body_force);
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            acc[MX][b] = fma(bf, T(qs[(b * NQ + RH) * CELL_CPB + lc]), acc[MX][b]);
+            acc[EN][b] = fma(bf, T(qs[(b * NQ + MX) * CELL_CPB + lc]), acc[EN][b]);
+        });
+    } else if (GRP == 1 && ph.ivis == 0) {
+        const T mc = -T(ph.coll);
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            sfor<6>([&](auto mm) {
+                constexpr int m = decltype(mm)::value;
+                acc[m][b] = fma(mc, T(qs[(b * NQ + PXX + m) * CELL_CPB + lc]), acc[m][b]);
+            });
+        });
+    }
 }
 
 template <class T>
@@ -623,12 +715,16 @@ __device__ __forceinline__ void cell_surface_update(const CellArgs& a, CellCtx<T
                 constexpr int p = decltype(pp)::value;
                 const T Fp = __ldg(fb + (long long)p * cx.nfd[d] + cx.fp[d]);
                 const T Fm = __ldg(fb + (long long)p * cx.nfd[d] + cx.fm[d]);
+                // the two faces share the point's tangential coordinates, so the
+                // minus-face weight is +-the plus-face weight (the parity of the
+                // function along d): one product with Fp + Fm or Fp - Fm
+                const T Fs = Fp + Fm, Fd = Fp - Fm;
                 sfor<NB>([&](auto bb) {
                     constexpr int b = decltype(bb)::value;
                     constexpr double cp = stab<TB, d, 1>(p, b);
                     constexpr double cm = stab<TB, d, 0>(p, b);
-                    if constexpr (cp != 0.0) r[b] = fma(T(cp), Fp, r[b]);
-                    if constexpr (cm != 0.0) r[b] = fma(T(cm), Fm, r[b]);
+                    static_assert(cm == cp || cm == -cp, "surface tables not mirror-symmetric");
+                    if constexpr (cp != 0.0) r[b] = fma(T(cp), cm == cp ? Fs : Fd, r[b]);
                 });
             });
         });
@@ -757,6 +853,7 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
     const int grp = tid / CELL_CPB;                   // 0 hydro, 1 stress (warp-uniform)
     CellCtx<T> cx;
     cx.qs = reinterpret_cast<T*>(smem_raw);           // [NB*NQ][CELL_CPB]
+    cx.ub = cx.qs + NB * NQ * CELL_CPB;               // [2][NQ][2][CELL_CPB]
     cx.lc = tid % CELL_CPB;
     const long long gc = (long long)blockIdx.x * CELL_CPB + cx.lc;
     cx.act = gc < a.G.ncell;
@@ -807,10 +904,9 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
     for (int m = 0; m < 6; ++m)
 #pragma unroll
         for (int b = 0; b < NB; ++b) acc[m][b] = T(0);
-    if (cx.act) {
-        if (grp == 0) cell_volume<T, TB, 0, NOISE>(a, cx, acc);
-        else cell_volume<T, TB, 1, NOISE>(a, cx, acc);
-    }
+    // every thread runs the volume phase: it holds one block barrier per orbit
+    if (grp == 0) cell_volume<T, TB, 0, NOISE>(a, cx, acc);
+    else cell_volume<T, TB, 1, NOISE>(a, cx, acc);
     __syncthreads();   // every read of the other group's coefficients is done
     if (cx.act) {
         if (grp == 0) cell_surface_update<T, TB, 0>(a, cx, flux, acc);

@@ -26,7 +26,7 @@ struct KernelSet {
 template <class T, int NB, int NQD>
 struct Launch {
     using TB = hermes_tab::Tab<NB, NQD>;
-    static size_t cell_smem() { return (size_t)NB * NQ * CELL_CPB * sizeof(T); }
+    static size_t cell_smem() { return (size_t)(NB * NQ + 4 * NQ) * CELL_CPB * sizeof(T); }
     template <bool NOISE>
     static cudaError_t prepare_cell() {
         return cudaFuncSetAttribute(k_cell<T, TB, NOISE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem());

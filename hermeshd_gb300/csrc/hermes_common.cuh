@@ -42,6 +42,11 @@ __device__ __forceinline__ void sfor_seq(F&& f) {
     }
 }
 
+// block barrier reached by different warps from different call sites (the
+// two thread groups of k_cell run different instantiations of one phase):
+// the non-.aligned barrier, which each warp reaches uniformly
+__device__ __forceinline__ void block_sync_split() { asm volatile("barrier.sync 0;" ::: "memory"); }
+
 // physics constants (params.f90 / input.f90), identical for every box
 struct Phys {
     double aindex, aindm1, rh_floor, T_floor, P_floor, rh_mult;
