@@ -11,7 +11,11 @@ include/hermes_gb300.h):
                        launches for grids so small that a step is launch-bound;
 * ``noise_inline``     where the stochastic stress is drawn: its own
                        kernels staging it in device memory (0) or inside the
-                       face and cell kernels (1).
+                       face and cell kernels (1);
+* ``face_traces``      face traces evaluated once per stage by their own
+                       kernel and read by the face kernels (1) or evaluated
+                       by the face kernels (0); tuned where the trace kernel
+                       exists (FP64, nbasis 8/10, no stochastic stress).
 
 The cell kernel keeps 32 cells per block: its hydro and stress thread groups
 must each fill whole warps, and its register cap is fixed at compile time.
@@ -35,6 +39,7 @@ KNOBS = {
     "dt_tpb": (256, 128, 64),
     "steps_per_graph": (1, 2, 4, 8),
     "noise_inline": (0, 1),          # tuned only with the stochastic stress on
+    "face_traces": (1, 0),           # tuned only where the context has the trace buffer
 }
 
 
@@ -113,6 +118,8 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
     knobs = dict(knobs or KNOBS)
     if not solver.cfg.llns:
         knobs.pop("noise_inline", None)
+    if solver.get_launch()["face_traces"] == 0:
+        knobs.pop("face_traces", None)
     qt, q1t = q.clone(), q.clone()
     best = {k: v[0] for k, v in knobs.items()}
     solver.set_launch(**best)
@@ -133,7 +140,8 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
     solver.set_time(t0)
     solver.set_noise_step(step0)
     _torch().cuda.synchronize()
-    res = {"launch": best, "ms_per_step": best_ms, "default_ms_per_step": default_ms, "trials": trials}
+    res = {"launch": solver.get_launch(), "ms_per_step": best_ms, "default_ms_per_step": default_ms,
+           "trials": trials}
     if use_cache:
         _store(key, res)
     return dict(res, cached=False)

@@ -58,6 +58,77 @@ __host__ __device__ constexpr double vtab(int g, int b) {
     else return TB::VZ(g, b);
 }
 
+// Face points in tangential mirror pairs: face point p = i*NE + m, the
+// mirror of m is NE-1-m.  Chunk c of a face is a pair (pA = i*NE + NE-1-mc,
+// pB = i*NE + mc) or, for an odd point count, the single middle point.
+template <class TB>
+struct FOrbit {
+    static constexpr int NE = TB::NQD, NPAIR = NE / 2, NMC = NPAIR + (NE & 1);
+    static constexpr int NCH = NMC * NE;
+    static constexpr bool pair(int c) { return c % NMC < NPAIR; }
+    static constexpr int pA(int c) { return (c / NMC) * NE + (pair(c) ? NE - 1 - c % NMC : NPAIR); }
+    static constexpr int pB(int c) { return pair(c) ? (c / NMC) * NE + c % NMC : pA(c); }
+};
+
+// the face tables of one direction by side: point values (SURF false) or
+// surface quadrature weights (SURF true)
+template <class TB, int DIR, bool SURF>
+__host__ __device__ constexpr double face_tab(int side, int p, int b) {
+    if constexpr (SURF) return side ? stab<TB, DIR, 1>(p, b) : stab<TB, DIR, 0>(p, b);
+    else return side ? ftab<TB, DIR, 1>(p, b) : ftab<TB, DIR, 0>(p, b);
+}
+// parity class of basis function b at chunk c: bit 0 = odd in the normal
+// coordinate (the minus-face entry is the negated plus-face entry), bit 1 =
+// odd in the tangential mirror; -1 where the entry is zero
+template <class TB, int DIR, bool SURF>
+__host__ __device__ constexpr int face_class(int c, int b) {
+    using FO = FOrbit<TB>;
+    const double a = face_tab<TB, DIR, SURF>(1, FO::pA(c), b);
+    if (a == 0.0) return -1;
+    const double mn = face_tab<TB, DIR, SURF>(0, FO::pA(c), b), tb = face_tab<TB, DIR, SURF>(1, FO::pB(c), b);
+    return (mn == a ? 0 : 1) | (tb == a ? 0 : 2);
+}
+// every entry of the four (side, point) combinations of a chunk is +-the
+// (plus, pA) entry, the (minus, pB) sign being the product of the other two
+template <class TB, int DIR, bool SURF>
+__host__ __device__ constexpr bool face_tables_symmetric() {
+    using FO = FOrbit<TB>;
+    for (int c = 0; c < FO::NCH; ++c)
+        for (int b = 0; b < TB::NB; ++b) {
+            const double a = face_tab<TB, DIR, SURF>(1, FO::pA(c), b);
+            const double mn = face_tab<TB, DIR, SURF>(0, FO::pA(c), b), tb = face_tab<TB, DIR, SURF>(1, FO::pB(c), b);
+            const double mb = face_tab<TB, DIR, SURF>(0, FO::pB(c), b);
+            if (mn != a && mn != -a) return false;
+            if (tb != a && tb != -a) return false;
+            const double sn = mn == a ? 1.0 : -1.0, st = tb == a ? 1.0 : -1.0;
+            if (mb != sn * st * a) return false;
+            if (!FO::pair(c) && tb != a) return false;
+        }
+    return true;
+}
+template <class TB, int DIR, bool SURF>
+__host__ __device__ constexpr bool face_has(int c, int k) {
+    for (int b = 0; b < TB::NB; ++b)
+        if (face_class<TB, DIR, SURF>(c, b) == k) return true;
+    return false;
+}
+
+// a + b and a - b where a or b may be an empty (compile-time zero) sum
+template <bool HA, bool HB, class T>
+__device__ __forceinline__ T sum_opt(T a, T b) {
+    if constexpr (HA && HB) return a + b;
+    else if constexpr (HA) return a;
+    else if constexpr (HB) return b;
+    else return T(0);
+}
+template <bool HA, bool HB, class T>
+__device__ __forceinline__ T diff_opt(T a, T b) {
+    if constexpr (HA && HB) return a - b;
+    else if constexpr (HA) return a;
+    else if constexpr (HB) return -b;
+    else return T(0);
+}
+
 // trace of all NQ variables of one cell at face point P: sum_b phi_b(P) Q(b,v)
 template <class TB, int DIR, int SIDE, int P, class T>
 __device__ __forceinline__ void trace_pt(const T* __restrict__ Qb, long long ncell, long long cell, T out[NQ]) {
@@ -255,6 +326,38 @@ struct FaceArgs {
     unsigned stage;
     int tpb;                         // faces per block (32, 64 or 128; 0 = FACE_TPB)
     const void* noise;               // staged stochastic stress of the faces (k_noise_face), or null: drawn here
+    const void* traces;              // face traces of every cell (k_trace), or null: evaluated here
+};
+
+// where k_face takes the traces of its two cells from: evaluated from the
+// coefficients (TRB false) or read from the buffer k_trace wrote, laid out
+// [direction][side][variable][point][cell of the whole grid]
+template <class T, class TB, int DIR, bool TRB>
+struct FaceTraces {
+    const T* Qb;          // coefficients of the box
+    long long nc;         // cells of the box
+    const T* tr;          // trace buffer
+    long long ncl;        // cells of the grid
+    long long cell0;      // first cell of the box
+    template <int SIDE>
+    __device__ __forceinline__ const T* slot(long long c) const {
+        return tr + (long long)((DIR * 2 + SIDE) * NQ) * TB::NF * ncl + cell0 + c;
+    }
+    template <int SIDE, int P>
+    __device__ __forceinline__ void pt(long long c, T q[NQ]) const {
+        if constexpr (TRB) {
+            const T* t = slot<SIDE>(c) + (long long)P * ncl;
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) q[v] = __ldg(t + (long long)v * TB::NF * ncl);
+        } else {
+            trace_pt<TB, DIR, SIDE, P>(Qb, nc, c, q);
+        }
+    }
+    template <int SIDE, int P, int V>
+    __device__ __forceinline__ T var(long long c) const {
+        if constexpr (TRB) return __ldg(slot<SIDE>(c) + (long long)(V * TB::NF + P) * ncl);
+        else return trace_var<TB, DIR, SIDE, P, V>(Qb, nc, c);
+    }
 };
 
 // the numerical flux at one face point from the two traces (after boundary
@@ -287,7 +390,7 @@ __device__ __forceinline__ void face_flux_fn(const Phys& ph, const T qL[NQ], con
     }
 }
 
-template <class T, class TB, int DIR, int P, bool NOISE>
+template <class T, class TB, int DIR, int P, bool NOISE, bool TRB>
 __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restrict__ flux, const FaceArgs& a, long long gf) {
     const Geom& G = a.G;
     const Phys& ph = a.ph;
@@ -306,7 +409,7 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
     const int s = DIR == 0 ? i : DIR == 1 ? j : k;       // face plane
     const bool dedup = B.nfp[DIR] == n;                    // both ends periodic: n planes
     const long long nc = B.ncell;
-    const T* Qb = Q + B.q0;
+    const FaceTraces<T, TB, DIR, TRB> ts{Q + B.q0, nc, static_cast<const T*>(a.traces), G.ncell, B.cell0};
     auto cell_at = [&](int c) -> long long {              // cell with plane coordinate c
         int ci = DIR == 0 ? c : i, cj = DIR == 1 ? c : j, ck = DIR == 2 ? c : k;
         return (long long)ci + (long long)n0 * (cj + (long long)n1 * ck);
@@ -315,12 +418,12 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
     T qL[NQ], qR[NQ];
     if (dedup || (s > 0 && s < n)) {
         const int lo = s > 0 ? s - 1 : n - 1;
-        trace_pt<TB, DIR, 1, P>(Qb, nc, cell_at(lo), qL);
-        trace_pt<TB, DIR, 0, P>(Qb, nc, cell_at(s), qR);
+        ts.template pt<1, P>(cell_at(lo), qL);
+        ts.template pt<0, P>(cell_at(s), qR);
     } else if (s == 0) {
         // low boundary: ghost from the first cell's minus trace (boundary.f90:40-244)
         const long long c0 = cell_at(0);
-        trace_pt<TB, DIR, 0, P>(Qb, nc, c0, qR);
+        ts.template pt<0, P>(c0, qR);
         const int code = B.bc[2 * DIR];
         if (code == BC_PERIODIC) {
             // topology not periodic (the hi flag is not): the ghost is the never-received zero trace
@@ -346,7 +449,7 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
             else if (code == BC_OUTFLOW) {
                 T mmax = -T(INFINITY);
                 sfor<TB::NF>([&](auto pp) {
-                    mmax = fmax(mmax, trace_var<TB, DIR, 0, decltype(pp)::value, MN>(Qb, nc, c0));
+                    mmax = fmax(mmax, ts.template var<0, decltype(pp)::value, MN>(c0));
                 });
                 if (mmax > T(0)) qL[MN] = T(0);
             }
@@ -354,12 +457,12 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
     } else {
         // high boundary (s == n)
         const long long cl = cell_at(n - 1);
-        trace_pt<TB, DIR, 1, P>(Qb, nc, cl, qL);
+        ts.template pt<1, P>(cl, qL);
         const int code = B.bc[2 * DIR + 1];
         if (code == BC_PERIODIC) {
             // periodic topology with a non-periodic low flag: the ghost is the
             // first cell's raw minus trace (prepare_step.f90:75-104 self-send)
-            trace_pt<TB, DIR, 0, P>(Qb, nc, cell_at(0), qR);
+            ts.template pt<0, P>(cell_at(0), qR);
         } else if (code == BC_OUTFLOW && DIR == 0) {
             // boundary.f90:246-282 never copies the interior trace: from a zero
             // ghost array the result stays zero
@@ -371,7 +474,7 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
             else if (code == BC_OUTFLOW) {
                 T mmin = T(INFINITY);
                 sfor<TB::NF>([&](auto pp) {
-                    mmin = fmin(mmin, trace_var<TB, DIR, 1, decltype(pp)::value, MN>(Qb, nc, cl));
+                    mmin = fmin(mmin, ts.template var<1, decltype(pp)::value, MN>(cl));
                 });
                 if (mmin < T(0)) qR[MN] = T(0);
             }
@@ -401,10 +504,10 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
         if (ph.ieos == 2) {
             // 1/rho of the last point of the reference's call: the right state at point NF-1
             T rlast;
-            if (dedup || s < n) rlast = trace_var<TB, DIR, 0, TB::NF - 1, RH>(Qb, nc, cell_at(s));
-            else if (B.bc[2 * DIR + 1] == BC_PERIODIC) rlast = trace_var<TB, DIR, 0, TB::NF - 1, RH>(Qb, nc, cell_at(0));
+            if (dedup || s < n) rlast = ts.template var<0, TB::NF - 1, RH>(cell_at(s));
+            else if (B.bc[2 * DIR + 1] == BC_PERIODIC) rlast = ts.template var<0, TB::NF - 1, RH>(cell_at(0));
             else if (B.bc[2 * DIR + 1] == BC_OUTFLOW && DIR == 0) rlast = T(0);
-            else rlast = trace_var<TB, DIR, 1, TB::NF - 1, RH>(Qb, nc, cell_at(n - 1));
+            else rlast = ts.template var<1, TB::NF - 1, RH>(cell_at(n - 1));
             rho_i_last = T(1) / rlast;
         }
     }
@@ -425,14 +528,14 @@ struct FaceMinBlocks {
     static constexpr int value = std::is_same<T, float>::value ? 6 : 4;
 };
 
-template <class T, class TB, int DIR, bool NOISE>
+template <class T, class TB, int DIR, bool NOISE, bool TRB>
 __global__ void __launch_bounds__(FACE_TPB, (FaceMinBlocks<T>::value)) k_face(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
     long long gf = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gf >= a.G.nface[DIR]) return;
     const int p = blockIdx.y;
     sfor<TB::NF>([&](auto pp) {
         constexpr int P = decltype(pp)::value;
-        if (p == P) face_point<T, TB, DIR, P, NOISE>(Q, flux, a, gf);
+        if (p == P) face_point<T, TB, DIR, P, NOISE, TRB>(Q, flux, a, gf);
     });
 }
 
@@ -710,21 +813,32 @@ __device__ __forceinline__ void cell_surface_update(const CellArgs& a, CellCtx<T
         sfor<NB>([&](auto bb) { r[decltype(bb)::value] = -acc[m][decltype(bb)::value]; });
         sfor<3>([&](auto dd) {
             constexpr int d = decltype(dd)::value;
+            using FO = FOrbit<TB>;
+            static_assert(face_tables_symmetric<TB, d, true>(), "surface tables not mirror-symmetric");
             const T* fb = flux + cx.B->fbase[d] + (long long)v * NF * cx.nfd[d];
-            sfor<NF>([&](auto pp) {
-                constexpr int p = decltype(pp)::value;
-                const T Fp = __ldg(fb + (long long)p * cx.nfd[d] + cx.fp[d]);
-                const T Fm = __ldg(fb + (long long)p * cx.nfd[d] + cx.fm[d]);
-                // the two faces share the point's tangential coordinates, so the
-                // minus-face weight is +-the plus-face weight (the parity of the
-                // function along d): one product with Fp + Fm or Fp - Fm
-                const T Fs = Fp + Fm, Fd = Fp - Fm;
+            // the weights of the plus and minus faces at a tangential mirror pair
+            // of points are +-one value (the parity of the function along d and
+            // along the mirror): one product per chunk with a signed sum of the
+            // four fluxes
+            sfor<FO::NCH>([&](auto cc) {
+                constexpr int c = decltype(cc)::value;
+                constexpr int pA = FO::pA(c), pB = FO::pB(c);
+                const T FpA = __ldg(fb + (long long)pA * cx.nfd[d] + cx.fp[d]);
+                const T FmA = __ldg(fb + (long long)pA * cx.nfd[d] + cx.fm[d]);
+                const T XsA = FpA + FmA, XdA = FpA - FmA;
+                T X[4];
+                if constexpr (FO::pair(c)) {
+                    const T FpB = __ldg(fb + (long long)pB * cx.nfd[d] + cx.fp[d]);
+                    const T FmB = __ldg(fb + (long long)pB * cx.nfd[d] + cx.fm[d]);
+                    const T XsB = FpB + FmB, XdB = FpB - FmB;
+                    X[0] = XsA + XsB; X[1] = XdA + XdB; X[2] = XsA - XsB; X[3] = XdA - XdB;
+                } else {
+                    X[0] = XsA; X[1] = XdA; X[2] = T(0); X[3] = T(0);
+                }
                 sfor<NB>([&](auto bb) {
                     constexpr int b = decltype(bb)::value;
-                    constexpr double cp = stab<TB, d, 1>(p, b);
-                    constexpr double cm = stab<TB, d, 0>(p, b);
-                    static_assert(cm == cp || cm == -cp, "surface tables not mirror-symmetric");
-                    if constexpr (cp != 0.0) r[b] = fma(T(cp), cm == cp ? Fs : Fd, r[b]);
+                    constexpr int k = face_class<TB, d, true>(c, b);
+                    if constexpr (k >= 0) r[b] = fma(T(stab<TB, d, 1>(pA, b)), X[k], r[b]);
                 });
             });
         });

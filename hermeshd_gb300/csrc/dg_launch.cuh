@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include "dg_kernels.cuh"
+#include "dg_trace.cuh"
 
 namespace hermes {
 
@@ -18,6 +19,9 @@ struct KernelSet {
     void (*face)(int dir, const void* Q, void* flux, const FaceArgs& a, cudaStream_t s);
     void (*cell)(const void* Qin, const void* Q0, void* out, const void* flux, const CellArgs& a, cudaStream_t s);
     void (*mindt)(const void* Q, const DtArgs& a, cudaStream_t s);
+    // face traces into a buffer for the face kernels (FaceArgs.traces); null
+    // where the face kernels evaluate the traces themselves
+    void (*trace)(const void* Q, void* tr, const Geom& G, cudaStream_t s);
 };
 
 // launchers of one (T, NB, NQD) instantiation; the stochastic-stress
@@ -36,6 +40,15 @@ struct Launch {
         const unsigned nb = (unsigned)((G.ncell + LIMIT_TPB - 1) / LIMIT_TPB);
         k_limit<T, TB><<<nb, LIMIT_TPB, 0, s>>>(static_cast<T*>(Q), G, ph);
     }
+    // the trace-buffer face kernels exist for the FP64 path of nbasis 8 and 10
+    // without the stochastic stress
+    static constexpr bool HAS_TRACE = std::is_same<T, double>::value && NB >= 8;
+    template <bool NOISE, bool TRB>
+    static void face_dirs(int dir, dim3 grid, int tpb, const T* q, T* f, const FaceArgs& a, cudaStream_t s) {
+        if (dir == 0) k_face<T, TB, 0, NOISE, TRB><<<grid, tpb, 0, s>>>(q, f, a);
+        else if (dir == 1) k_face<T, TB, 1, NOISE, TRB><<<grid, tpb, 0, s>>>(q, f, a);
+        else k_face<T, TB, 2, NOISE, TRB><<<grid, tpb, 0, s>>>(q, f, a);
+    }
     template <bool NOISE>
     static void face(int dir, const void* Q, void* flux, const FaceArgs& a, cudaStream_t s) {
         const long long n = a.G.nface[dir];
@@ -44,9 +57,19 @@ struct Launch {
         dim3 grid((unsigned)((n + tpb - 1) / tpb), TB::NF);
         const T* q = static_cast<const T*>(Q);
         T* f = static_cast<T*>(flux);
-        if (dir == 0) k_face<T, TB, 0, NOISE><<<grid, tpb, 0, s>>>(q, f, a);
-        else if (dir == 1) k_face<T, TB, 1, NOISE><<<grid, tpb, 0, s>>>(q, f, a);
-        else k_face<T, TB, 2, NOISE><<<grid, tpb, 0, s>>>(q, f, a);
+        if constexpr (HAS_TRACE && !NOISE) {
+            if (a.traces) { face_dirs<NOISE, true>(dir, grid, tpb, q, f, a, s); return; }
+        }
+        FaceArgs b = a;
+        b.traces = nullptr;
+        face_dirs<NOISE, false>(dir, grid, tpb, q, f, b, s);
+    }
+    static void trace(const void* Q, void* tr, const Geom& G, cudaStream_t s) {
+        if constexpr (HAS_TRACE) {
+            if (G.ncell <= 0) return;
+            dim3 grid((unsigned)((G.ncell + TRACE_TPB - 1) / TRACE_TPB), 3 * NQ);
+            k_trace<T, TB><<<grid, TRACE_TPB, 0, s>>>(static_cast<const T*>(Q), static_cast<T*>(tr), G);
+        }
     }
     template <bool NOISE>
     static void cell(const void* Qin, const void* Q0, void* out, const void* flux, const CellArgs& a, cudaStream_t s) {
@@ -71,6 +94,7 @@ using FaceFn = void (*)(int, const void*, void*, const FaceArgs&, cudaStream_t);
 using CellFn = void (*)(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
 using LimitFn = void (*)(void*, const Geom&, const Phys&, cudaStream_t);
 using DtFn = void (*)(const void*, const DtArgs&, cudaStream_t);
+using TraceFn = void (*)(const void*, void*, const Geom&, cudaStream_t);
 using PrepFn = cudaError_t (*)();
 
 // precision 64 or 32, nb 4/8/10; false if unsupported

@@ -140,8 +140,9 @@ struct hermes_ctx {
     struct Rec { int kind; cudaEvent_t a, b; };
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> pool;
-    double prof_ms[7] = {0, 0, 0, 0, 0, 0, 0};
-    long long prof_n[7] = {0, 0, 0, 0, 0, 0, 0};
+    static constexpr int NKIND = 8;
+    double prof_ms[NKIND] = {};
+    long long prof_n[NKIND] = {};
     // launch shape (hermes_set_launch); 0 = the compiled defaults
     int face_tpb = 0, dt_tpb = 0, graph_steps = 1;
     // stochastic stress staged in HBM by its own kernels (dg_noise.cuh)
@@ -149,6 +150,9 @@ struct hermes_ctx {
     NoiseFn noise_fn = nullptr;
     void* d_noise_cell = nullptr;
     void* d_noise_face = nullptr;
+    // face traces evaluated once per stage (dg_trace.cuh)
+    void* d_traces = nullptr;
+    bool face_traces = false;
     // adjoint scratch, allocated on first use
     AdjFn adj = nullptr;
     double* d_tadj = nullptr;   // trace adjoints: 2 x the face-flux size
@@ -313,7 +317,12 @@ void enq_limit(hermes_ctx* c, void* q) {
     }
 }
 void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
-    FaceArgs a{c->G, c->ph, c->d_step, stage, c->face_tpb, c->noise_staged ? c->d_noise_face : nullptr};
+    FaceArgs a{c->G, c->ph, c->d_step, stage, c->face_tpb, c->noise_staged ? c->d_noise_face : nullptr,
+               c->face_traces ? c->d_traces : nullptr};
+    if (c->face_traces) {
+        ProfScope ps(c, 7);
+        c->K.trace(q, c->d_traces, c->G, c->stream);
+    }
     for (int d = 0; d < 3; ++d) {
         ProfScope ps(c, 2 + d);
         c->K.face(d, q, c->d_flux, a, c->stream);
@@ -486,6 +495,12 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
             c->d_noise_cell = c->d_noise_face = nullptr;
         }
     }
+    if (c->K.trace) {
+        // face traces: 2 sides x 3 directions x NQ x NF values per cell
+        const size_t bytes = (size_t)ncell * 6 * NQ * c->K.nf * c->K.elem_size;
+        if (cudaMalloc(&c->d_traces, bytes) == cudaSuccess) c->face_traces = true;
+        else { cudaGetLastError(); c->d_traces = nullptr; }   // no room: the face kernels evaluate them
+    }
     if (cudaMemcpy(c->d_boxes, c->h_boxes.data(), sizeof(Box) * nbox, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemset(c->d_st, 0, sizeof(BoxState) * nbox) != cudaSuccess ||
         cudaMemset(c->d_step, 0, sizeof(unsigned long long) * 2) != cudaSuccess ||
@@ -568,6 +583,7 @@ int hermes_destroy(hermes_ctx* c) {
     cudaFree(c->d_cons);
     cudaFree(c->d_noise_cell);
     cudaFree(c->d_noise_face);
+    cudaFree(c->d_traces);
     delete c;
     return HERMES_OK;
 }
@@ -775,7 +791,11 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     const bool staged = l->noise_inline == 0 && c->d_noise_cell != nullptr;
     if (l->noise_inline == 0 && c->cfg.llns && !c->d_noise_cell)
         return fail(c, HERMES_ERR_ALLOC, "no staged-noise buffers (device memory was short at creation)");
-    if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged) {
+    if (l->face_traces != 0 && l->face_traces != 1) return fail(c, HERMES_ERR_ARG, "face_traces must be 0 or 1");
+    if (l->face_traces == 1 && !c->d_traces)
+        return fail(c, HERMES_ERR_ARG, "face traces need FP64, nbasis 8 or 10, no stochastic stress and room for the buffer");
+    const bool traces = l->face_traces == 1;
+    if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged || traces != c->face_traces) {
         // captured graphs hold the old launch shape
         HCK(c, cudaSetDevice(c->device));
         HCK(c, cudaStreamSynchronize(c->stream));
@@ -785,6 +805,7 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     c->dt_tpb = d;
     c->graph_steps = g > 0 ? g : 1;
     c->noise_staged = staged;
+    c->face_traces = traces;
     return HERMES_OK;
 }
 
@@ -794,6 +815,7 @@ int hermes_get_launch(hermes_ctx* c, hermes_launch* l) {
     l->dt_tpb = c->dt_tpb > 0 ? c->dt_tpb : DT_TPB;
     l->steps_per_graph = c->graph_steps;
     l->noise_inline = (c->cfg.llns && !c->noise_staged) ? 1 : 0;
+    l->face_traces = c->face_traces ? 1 : 0;
     return HERMES_OK;
 }
 
@@ -818,7 +840,7 @@ int hermes_profile_read(hermes_ctx* c, double* ms, int64_t* launches) {
     }
     c->recs.clear();
     cudaGetLastError();
-    for (int k = 0; k < 7; ++k) {
+    for (int k = 0; k < hermes_ctx::NKIND; ++k) {
         if (ms) ms[k] = c->prof_ms[k];
         if (launches) launches[k] = c->prof_n[k];
         c->prof_ms[k] = 0;

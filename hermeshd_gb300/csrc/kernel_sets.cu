@@ -15,6 +15,7 @@ void face_f64_nb8(int, const void*, void*, const FaceArgs&, cudaStream_t);
 void facen_f64_nb8(int, const void*, void*, const FaceArgs&, cudaStream_t);
 void limit_f64_nb8(void*, const Geom&, const Phys&, cudaStream_t);
 void mindt_f64_nb8(const void*, const DtArgs&, cudaStream_t);
+void trace_f64_nb8(const void*, void*, const Geom&, cudaStream_t);
 void cell_f64_nb8(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
 void celln_f64_nb8(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
 cudaError_t prep_f64_nb8();
@@ -23,6 +24,7 @@ void face_f64_nb10(int, const void*, void*, const FaceArgs&, cudaStream_t);
 void facen_f64_nb10(int, const void*, void*, const FaceArgs&, cudaStream_t);
 void limit_f64_nb10(void*, const Geom&, const Phys&, cudaStream_t);
 void mindt_f64_nb10(const void*, const DtArgs&, cudaStream_t);
+void trace_f64_nb10(const void*, void*, const Geom&, cudaStream_t);
 void cell_f64_nb10(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
 void celln_f64_nb10(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
 cudaError_t prep_f64_nb10();
@@ -54,6 +56,7 @@ cudaError_t prepn_f32_nb10();
 
 bool kernel_set(int precision, int nb, bool noise, KernelSet* out) {
     KernelSet k;
+    k.trace = nullptr;
     if (precision == 64 && nb == 4) {
         k.elem_size = sizeof(double); k.nb = 4; k.nqd = 2; k.nf = 4;
         k.prepare = noise ? &prepn_f64_nb4 : &prep_f64_nb4;
@@ -71,6 +74,7 @@ bool kernel_set(int precision, int nb, bool noise, KernelSet* out) {
         k.face = noise ? &facen_f64_nb8 : &face_f64_nb8;
         k.cell = noise ? &celln_f64_nb8 : &cell_f64_nb8;
         k.mindt = &mindt_f64_nb8;
+        k.trace = noise ? nullptr : &trace_f64_nb8;
         *out = k;
         return true;
     }
@@ -81,6 +85,7 @@ bool kernel_set(int precision, int nb, bool noise, KernelSet* out) {
         k.face = noise ? &facen_f64_nb10 : &face_f64_nb10;
         k.cell = noise ? &celln_f64_nb10 : &cell_f64_nb10;
         k.mindt = &mindt_f64_nb10;
+        k.trace = noise ? nullptr : &trace_f64_nb10;
         *out = k;
         return true;
     }

@@ -137,11 +137,11 @@ class Solver:
     def profile(self, enable: bool = True):
         check(lib().hermes_profile_enable(self.ctx, int(enable)), self.ctx)
 
-    KERNEL_KINDS = ("cfl_dt", "limiter", "face_x", "face_y", "face_z", "cell", "noise")
+    KERNEL_KINDS = ("cfl_dt", "limiter", "face_x", "face_y", "face_z", "cell", "noise", "trace")
 
     def profile_read(self):
-        ms = np.zeros(7)
-        n = np.zeros(7, dtype=np.int64)
+        ms = np.zeros(len(self.KERNEL_KINDS))
+        n = np.zeros(len(self.KERNEL_KINDS), dtype=np.int64)
         check(lib().hermes_profile_read(self.ctx, ms.ctypes.data_as(C.POINTER(C.c_double)),
                                         n.ctypes.data_as(C.POINTER(C.c_int64))), self.ctx)
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_KINDS)}
@@ -175,10 +175,15 @@ class Solver:
         l = _lib.HermesLaunch()
         check(lib().hermes_get_launch(self.ctx, C.byref(l)), self.ctx)
         return {"face_tpb": l.face_tpb, "dt_tpb": l.dt_tpb, "steps_per_graph": l.steps_per_graph,
-                "noise_inline": l.noise_inline}
+                "noise_inline": l.noise_inline, "face_traces": l.face_traces}
 
-    def set_launch(self, face_tpb: int = 0, dt_tpb: int = 0, steps_per_graph: int = 1, noise_inline: int = 0):
-        l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), int(noise_inline))
+    def set_launch(self, face_tpb: int = 0, dt_tpb: int = 0, steps_per_graph: int = 1, noise_inline: int = 0,
+                   face_traces=None):
+        """face_traces None keeps the context's current choice (on by default
+        where the trace kernel exists: FP64, nbasis 8/10, no stochastic stress)."""
+        if face_traces is None:
+            face_traces = self.get_launch()["face_traces"]
+        l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), int(noise_inline), int(face_traces))
         check(lib().hermes_set_launch(self.ctx, C.byref(l)), self.ctx)
 
     def set_noise_step(self, step: int):

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define HERMES_ABI_VERSION 3
+#define HERMES_ABI_VERSION 4
 
 typedef enum hermes_status {
     HERMES_OK = 0,
@@ -214,6 +214,10 @@ typedef struct hermes_launch {
     int32_t noise_inline;    /* stochastic stress: 0 drawn by kernels of its own and staged in device
                                 memory (default; the buffers are allocated at creation), 1 drawn inside
                                 the face and cell kernels.  The same numbers either way. */
+    int32_t face_traces;     /* 1: the face traces of every cell are evaluated once per stage by a
+                                kernel of their own and read by the face kernels (FP64, nbasis 8/10,
+                                no stochastic stress; the default there, the buffer is allocated at
+                                creation); 0: the face kernels evaluate them.  Equal to rounding. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
 int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);
@@ -223,9 +227,9 @@ int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);
  * by an event pair.  hermes_profile_read synchronises, returns accumulated
  * milliseconds and launch counts per kernel kind and resets them.  Kinds:
  * 0 CFL reduction, 1 limiter, 2 x faces, 3 y faces, 4 z faces, 5 cell update,
- * 6 staged stochastic stress (the four noise kernels of a stage). */
+ * 6 staged stochastic stress (the four noise kernels of a stage), 7 face traces. */
 int hermes_profile_enable(hermes_ctx *ctx, int enable);
-int hermes_profile_read(hermes_ctx *ctx, double *ms /* [7] */, int64_t *launches /* [7] */);
+int hermes_profile_read(hermes_ctx *ctx, double *ms /* [8] */, int64_t *launches /* [8] */);
 
 /* Per-box time and last time step of an ensemble (nbox entries each). */
 int hermes_box_times(hermes_ctx *ctx, double *t, double *dt);

@@ -18,12 +18,16 @@ def test_launch_defaults_and_validation():
     from hermeshd_gb300._lib import HermesError
     from hermeshd_gb300.solver import Solver
     s = Solver(config.sod_1d(nx=64))
-    assert s.get_launch() == {"face_tpb": 128, "dt_tpb": 256, "steps_per_graph": 1, "noise_inline": 0}
+    assert s.get_launch() == {"face_tpb": 128, "dt_tpb": 256, "steps_per_graph": 1, "noise_inline": 0,
+                              "face_traces": 0}
     for bad in ({"face_tpb": 96}, {"face_tpb": 256}, {"dt_tpb": 48}, {"dt_tpb": 512}, {"steps_per_graph": 65}):
         with pytest.raises(HermesError):
             s.set_launch(**bad)
     s.set_launch(face_tpb=32, dt_tpb=64, steps_per_graph=4)
-    assert s.get_launch() == {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 4, "noise_inline": 0}
+    assert s.get_launch() == {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 4, "noise_inline": 0,
+                              "face_traces": 0}
+    with pytest.raises(HermesError):   # no trace kernel for nbasis 4
+        s.set_launch(face_traces=1)
 
 
 @pytest.mark.parametrize("mk", [lambda: config.isentropic_vortex_2d(n=12),
@@ -49,6 +53,29 @@ def test_every_launch_shape_is_bit_identical(mk):
             assert np.array_equal(out[0], ref[0]) and out[1] == ref[1] and out[2] == ref[2], shape
 
 
+def test_face_traces_match_face_evaluation():
+    """The trace kernel's values (mirror-pair sums) against the face kernels'
+    own evaluation: the same right-hand side to rounding, and 7 steps apart by
+    rounding only; with traces off the launch shapes stay bit-identical."""
+    from hermeshd_gb300.solver import Solver
+    cfg = config.isentropic_vortex_2d(n=12)
+    Q = ic.isentropic_vortex(cfg)
+    out = {}
+    for ft in (1, 0):
+        s = Solver(cfg)
+        assert s.get_launch()["face_traces"] == 1
+        s.set_launch(face_traces=ft)
+        assert s.get_launch()["face_traces"] == ft
+        q, q1 = s.from_numpy(Q), s.new_state()
+        r = s.rhs(q, limit=False)
+        s.advance(q, q1, 7)
+        out[ft] = (r, q)
+    torch = _torch()
+    rel = lambda a, b: float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+    assert rel(out[1][0], out[0][0]) < 1e-14
+    assert rel(out[1][1], out[0][1]) < 1e-13
+
+
 def test_autotune_resets_state_and_caches(tmp_path, monkeypatch):
     from hermeshd_gb300 import autotune
     from hermeshd_gb300.solver import Ensemble
@@ -65,7 +92,7 @@ def test_autotune_resets_state_and_caches(tmp_path, monkeypatch):
         v[0, 4].fill_(1.0 / (base.aindex - 1.0))
     r = autotune.autotune(ens, q, steps=2, repeats=2)
     assert not r["cached"] and r["ms_per_step"] <= r["default_ms_per_step"]
-    assert set(r["launch"]) == {"face_tpb", "dt_tpb", "steps_per_graph", "noise_inline"}
+    assert set(r["launch"]) == {"face_tpb", "dt_tpb", "steps_per_graph", "noise_inline", "face_traces"}
     assert ens.get_launch() == r["launch"]
     # tuning stepped copies of q; the context's time and noise counter are reset
     qa, qa1 = q.clone(), ens.new_state()
