@@ -34,8 +34,14 @@ sys.path.insert(0, ROOT)
 
 METRIC = "DOF-updates/s per RK stage, FP64 plain vs FP32 batched at stated L2 error"
 UNIT = "DOF-updates/s"
-WORKLOAD = ("2D isentropic vortex 128x128x1 periodic, 5-moment Euler, quadratic Legendre basis "
+WORKLOAD = ("2D isentropic vortex {n}x{n}x1 periodic, 5-moment Euler, quadratic Legendre basis "
             "(nbasis 10, iquad 3), HLLC, SSP-RK3, FP64")
+# FP64 arithmetic instructions the kernels execute per cell and stage on this
+# workload, from one ncu launch of each kernel at 256x256 (2 * dfma + dadd +
+# dmul thread instructions / cells, profiles/fp64_ops_vortex256_f64.txt); the
+# reference algorithm's count (perfmodel) is larger: the kernels use the
+# mirror symmetries of the tables
+EXECUTED_FLOPS_VORTEX = {"cell": 13223.0, "face_x": 2289.4, "face_y": 2289.4, "face_z": 2465.0, "trace": 2442.0}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -225,7 +231,7 @@ def run_ours(args, rank, ws):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "nQ": 11, "nbasis": 10,
+           "config": {"workload": WORKLOAD.format(n=cfg.nx), "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "nQ": 11, "nbasis": 10,
                       "dof": cfg.dof, "rk_stages": cfg.stages, "l2": "flushed: 256 MiB write before every timed step",
                       "parallelism": "replicas" if ws > 1 else "single GPU", "timing": "CUDA events per step on the kernels' stream"},
            "clocks": clocks, "gpu_launches": launches_per_step * K,
@@ -268,11 +274,11 @@ def run_ours(args, rank, ws):
     per_launch = {"cell": cfg.dof * sbytes, "face_x": cfg.dof * 8.0, "face_y": cfg.dof * 8.0,
                   "face_z": cfg.dof * 8.0, "limiter": cfg.dof * 8.0 * 5 / 11, "cfl_dt": cfg.ncells * 5 * 8.0}
     ach = per_launch[top] / (kern[top]["ms_avg"] * 1e-3) / 1e9
-    # DRAM bytes of one k_cell launch from ncu (256x256: 279 MB read + 85 MB written,
+    # DRAM bytes of one k_cell launch from ncu (256x256: 285 MB read + 95 MB written,
     # profiles/k_cell_vortex256_f64.txt), scaled by the cell count to this grid;
     # the excess over the algorithmic bytes is the face-flux intermediate the
     # cell kernel reads (each face's 9 x 11 fluxes by both its cells) and spills
-    traffic = 364e6 * cfg.ncells / (256 * 256) if top == "cell" else None
+    traffic = 380e6 * cfg.ncells / (256 * 256) if top == "cell" else None
     out["roofline"] = {"bound": "hbm", "kernel": top, "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                        "frac": ach / pk["hbm_gbs"], "peak_source": pk["source"], "traffic": traffic,
                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_cell launch at "
@@ -286,7 +292,14 @@ def run_ours(args, rank, ws):
     step_flops = fl["total"] * cfg.ncells * cfg.stages
     out["alu"] = {"bound_by": "fp64 pipe", "flops_per_cell_stage": fl, "achieved_tflops": step_flops / (ms_per_step * 1e-3) / 1e12,
                   "peak": ap, "frac_fp64": (step_flops / (ms_per_step * 1e-3) / 1e12) / ap["fp64_tflops"] if "fp64_tflops" in ap else None,
-                  "flop_model": "algorithmic: nonzero table products (FMA = 2), division/sqrt = 1"}
+                  "flop_model": "reference algorithm: nonzero table products (FMA = 2), division/sqrt = 1"}
+    ex_flops = sum(EXECUTED_FLOPS_VORTEX.values()) * cfg.ncells * cfg.stages
+    ex_tf = ex_flops / (ms_per_step * 1e-3) / 1e12
+    out["alu"]["executed"] = {
+        "flops_per_cell_stage": EXECUTED_FLOPS_VORTEX, "achieved_tflops": ex_tf,
+        "frac_fp64": ex_tf / ap["fp64_tflops"] if "fp64_tflops" in ap else None,
+        "source": "ncu smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum, one launch per kernel "
+                  "at 256x256, per cell (profiles/fp64_ops_vortex256_f64.txt)"}
     s.close()
 
     # ---- variants -------------------------------------------------------
@@ -683,7 +696,7 @@ def run_reference(args, rank, ws):
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "dof": cfg.dof},
+            "config": {"workload": WORKLOAD.format(n=cfg.nx), "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "dof": cfg.dof},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": f"{args.steps} full SSP-RK3 steps after {args.warmup} warm-up steps"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

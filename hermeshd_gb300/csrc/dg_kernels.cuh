@@ -629,6 +629,146 @@ __host__ __device__ constexpr bool src_gram_is_identity() {
     return true;
 }
 
+// the values of one thread group's variables at the points of x-orbit chunk
+// c, written to the exchange buffer slot ubc ([NQ][2][CELL_CPB])
+template <class T, class TB, int GRP, int c>
+__device__ __forceinline__ void chunk_eval(const volatile T* qs, volatile T* ubc, int lc) {
+    using XO = XOrbit<TB>;
+    constexpr int NB = TB::NB;
+    constexpr int GV0 = GRP == 0 ? 0 : PXX;
+    constexpr int GNV = GRP == 0 ? 5 : 6;
+    constexpr bool PAIR = XO::pair(c);
+    constexpr int gA = XO::gA(c), gB = XO::gB(c);
+    sfor<GNV>([&](auto mm) {
+        constexpr int v = GV0 + decltype(mm)::value;
+        T E = T(0), O = T(0);
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            constexpr double cA = TB::INT(gA, b), cB = TB::INT(gB, b);
+            static_assert(cB == cA || cB == -cA, "interior table not mirror-symmetric in x");
+            if constexpr (cA != 0.0) {
+                const T q = qs[(b * NQ + v) * CELL_CPB + lc];
+                if constexpr (cB == cA) E = fma(T(cA), q, E);
+                else O = fma(T(cA), q, O);
+            }
+        });
+        if constexpr (PAIR) {
+            ubc[(v * 2 + 0) * CELL_CPB + lc] = E + O;
+            ubc[(v * 2 + 1) * CELL_CPB + lc] = E - O;
+        } else {
+            ubc[(v * 2 + 0) * CELL_CPB + lc] = E;
+        }
+    });
+}
+
+// some point of the volume table of direction d has a nonzero weight for b
+template <class TB, int d>
+__host__ __device__ constexpr bool vtab_any(int b) {
+    for (int g = 0; g < TB::NPG; ++g)
+        if (vtab<TB, d>(g, b) != 0.0) return true;
+    return false;
+}
+
+// phase 1 of the stress group for ivis 0 and 1: the stress fluxes are
+// colvis-weighted velocity components (flux.f90:57-62 and the y, z rows),
+// f_d[m] = K(d, m) v_j(d, m), so the volume quadrature of all six rows is
+// made of the nine sums V[d][j][b] = sum_g vtab_d(g, b) v_j(g), combined with
+// the constants once at the end: three products per point and direction
+// instead of six, and no per-point flux rows.
+template <class T, class TB, bool NOISE>
+__device__ __forceinline__ void cell_volume_linear_stress(const CellArgs& a, CellCtx<T>& cx, T (&acc)[6][TB::NB]) {
+    using XO = XOrbit<TB>;
+    constexpr int NB = TB::NB;
+    const Phys& ph = a.ph;
+    const volatile T* qs = cx.qs;
+    volatile T* ub = cx.ub;
+    const int lc = cx.lc;
+    const bool act = cx.act;
+    T V[3][3][NB];
+    sfor<3>([&](auto dd) { sfor<3>([&](auto jj) { sfor<NB>([&](auto bb) {
+        V[decltype(dd)::value][decltype(jj)::value][decltype(bb)::value] = T(0); }); }); });
+    sfor_seq<XO::NCH>([&](auto cc) {
+        constexpr int c = decltype(cc)::value;
+        constexpr bool PAIR = XO::pair(c);
+        constexpr int gA = XO::gA(c), gB = XO::gB(c);
+        constexpr int NK = PAIR ? 2 : 1;
+        volatile T* ubc = ub + (c & 1) * (NQ * 2 * CELL_CPB);
+        if (act) chunk_eval<T, TB, 1, c>(qs, ubc, lc);
+        block_sync_split();
+        if (act) {
+            T vel[NK][3];
+            sfor<NK>([&](auto kk) {
+                constexpr int k = decltype(kk)::value;
+                const T dni = T(1) / T(ubc[(RH * 2 + k) * CELL_CPB + lc]);
+                sfor<3>([&](auto jj) {
+                    constexpr int j = decltype(jj)::value;
+                    vel[k][j] = T(ubc[((MX + j) * 2 + k) * CELL_CPB + lc]) * dni;
+                });
+            });
+            T vs[3], vd[3];
+            sfor<3>([&](auto jj) {
+                constexpr int j = decltype(jj)::value;
+                if constexpr (PAIR) { vs[j] = vel[0][j] + vel[NK - 1][j]; vd[j] = vel[0][j] - vel[NK - 1][j]; }
+                else { vs[j] = vel[0][j]; vd[j] = vel[0][j]; }
+            });
+            sfor<3>([&](auto dd) {
+                constexpr int d = decltype(dd)::value;
+                sfor<NB>([&](auto bb) {
+                    constexpr int b = decltype(bb)::value;
+                    constexpr double cA = vtab<TB, d>(gA, b), cB = vtab<TB, d>(gB, b);
+                    static_assert(cB == cA || cB == -cA, "volume table not mirror-symmetric in x");
+                    if constexpr (cA != 0.0) {
+                        sfor<3>([&](auto jj) {
+                            constexpr int j = decltype(jj)::value;
+                            V[d][j][b] = fma(T(cA), (!PAIR || cB == cA) ? vs[j] : vd[j], V[d][j][b]);
+                        });
+                    }
+                });
+            });
+        }
+    });
+    if (!act) return;
+    // K(d, m) di_d: diagonal rows (4/3, -2/3, -2/3) colvis v_d, off-diagonal colvis v_other
+    const T cv = T(ph.colvis), c4 = T(4.0 / 3.0) * cv, c2 = -(T(2.0 / 3.0) * cv);
+    sfor<3>([&](auto dd) {
+        constexpr int d = decltype(dd)::value;
+        const T di = cx.di[d];
+        const T kdiag = c4 * di, koff = c2 * di, kcv = cv * di;
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            if constexpr (vtab_any<TB, d>(b)) {
+                // rows pxx, pyy, pzz: v_d with 4/3 on the row of d, -2/3 on the others
+                sfor<3>([&](auto ii) {
+                    constexpr int i = decltype(ii)::value;
+                    acc[i][b] = fma(i == d ? kdiag : koff, V[d][d][b], acc[i][b]);
+                });
+                // pxy (m 3), pxz (m 4), pyz (m 5): colvis times the other index's velocity
+                if constexpr (d == 0) {
+                    acc[3][b] = fma(kcv, V[0][1][b], acc[3][b]);
+                    acc[4][b] = fma(kcv, V[0][2][b], acc[4][b]);
+                } else if constexpr (d == 1) {
+                    acc[3][b] = fma(kcv, V[1][0][b], acc[3][b]);
+                    acc[5][b] = fma(kcv, V[1][2][b], acc[5][b]);
+                } else {
+                    acc[4][b] = fma(kcv, V[2][0][b], acc[4][b]);
+                    acc[5][b] = fma(kcv, V[2][1][b], acc[5][b]);
+                }
+            }
+        });
+    });
+    if (ph.ivis == 0) {   // sources.f90:37-43, linear: the coefficients themselves (src_gram)
+        static_assert(src_gram_is_identity<TB>(), "source projection of a linear field is not the identity");
+        const T mc = -T(ph.coll);
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            sfor<6>([&](auto mm) {
+                constexpr int m = decltype(mm)::value;
+                acc[m][b] = fma(mc, T(qs[(b * NQ + PXX + m) * CELL_CPB + lc]), acc[m][b]);
+            });
+        });
+    }
+}
+
 // phase 1: volume quadrature and point sources of one group's variables
 // (flux.f90:751-928, sources.f90:28-78); acc collects volume + source.  Each
 // thread evaluates only its own group's variables at the points and the two
@@ -641,41 +781,25 @@ __device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T
     constexpr int GV0 = GRP == 0 ? 0 : PXX;
     constexpr int GNV = GRP == 0 ? 5 : 6;
     const Phys& ph = a.ph;
+    if constexpr (GRP == 1) {
+        if (ph.ivis < 2) {   // uniform over the block: both groups run the same number of barriers
+            cell_volume_linear_stress<T, TB, NOISE>(a, cx, acc);
+            return;
+        }
+    }
     const volatile T* qs = cx.qs;
     volatile T* ub = cx.ub;   // [2][NQ][2][CELL_CPB]
     const int lc = cx.lc;
     const bool act = cx.act;
-    // the stress thread needs its own values at the points for the 10-moment
-    // fluxes (ivis 2, 3); ivis 0 and 1 need only the velocity there
-    const bool need_all = GRP == 0 || ph.ivis >= 2;
+    // the stress thread (here ivis 2, 3) needs its own values at the points
+    const bool need_all = true;
     sfor_seq<XO::NCH>([&](auto cc) {
         constexpr int c = decltype(cc)::value;
         constexpr bool PAIR = XO::pair(c);
         constexpr int gA = XO::gA(c), gB = XO::gB(c);
         constexpr int NK = PAIR ? 2 : 1;
         volatile T* ubc = ub + (c & 1) * (NQ * 2 * CELL_CPB);
-        if (act) {
-            sfor<GNV>([&](auto mm) {
-                constexpr int v = GV0 + decltype(mm)::value;
-                T E = T(0), O = T(0);
-                sfor<NB>([&](auto bb) {
-                    constexpr int b = decltype(bb)::value;
-                    constexpr double cA = TB::INT(gA, b), cB = TB::INT(gB, b);
-                    static_assert(cB == cA || cB == -cA, "interior table not mirror-symmetric in x");
-                    if constexpr (cA != 0.0) {
-                        const T q = qs[(b * NQ + v) * CELL_CPB + lc];
-                        if constexpr (cB == cA) E = fma(T(cA), q, E);
-                        else O = fma(T(cA), q, O);
-                    }
-                });
-                if constexpr (PAIR) {
-                    ubc[(v * 2 + 0) * CELL_CPB + lc] = E + O;
-                    ubc[(v * 2 + 1) * CELL_CPB + lc] = E - O;
-                } else {
-                    ubc[(v * 2 + 0) * CELL_CPB + lc] = E;
-                }
-            });
-        }
+        if (act) chunk_eval<T, TB, GRP, c>(qs, ubc, lc);
         block_sync_split();
         if (act) {
             T u[NK][NQ];
@@ -816,6 +940,22 @@ __device__ __forceinline__ void cell_surface_update(const CellArgs& a, CellCtx<T
             using FO = FOrbit<TB>;
             static_assert(face_tables_symmetric<TB, d, true>(), "surface tables not mirror-symmetric");
             const T* fb = flux + cx.B->fbase[d] + (long long)v * NF * cx.nfd[d];
+            if constexpr (!std::is_same<T, double>::value) {
+                // FP32 (not bound by its arithmetic): the two faces of a point
+                // only, which keeps the register footprint of the FP32 kernels
+                sfor<NF>([&](auto pp) {
+                    constexpr int p = decltype(pp)::value;
+                    const T Fp = __ldg(fb + (long long)p * cx.nfd[d] + cx.fp[d]);
+                    const T Fm = __ldg(fb + (long long)p * cx.nfd[d] + cx.fm[d]);
+                    const T Fs = Fp + Fm, Fd = Fp - Fm;
+                    sfor<NB>([&](auto bb) {
+                        constexpr int b = decltype(bb)::value;
+                        constexpr double cp = stab<TB, d, 1>(p, b), cm = stab<TB, d, 0>(p, b);
+                        if constexpr (cp != 0.0) r[b] = fma(T(cp), cm == cp ? Fs : Fd, r[b]);
+                    });
+                });
+                return;
+            }
             // the weights of the plus and minus faces at a tangential mirror pair
             // of points are +-one value (the parity of the function along d and
             // along the mirror): one product per chunk with a signed sum of the
