@@ -72,8 +72,8 @@ class Rollout:
         return s
 
     # ---- forward ------------------------------------------------------------
-    def _stage(self, S: Solver, x, dt: float):
-        if self.check_limiter:
+    def _stage(self, S: Solver, x, dt: float, check: bool):
+        if check:
             x0 = x.clone()
             e = S.euler_stage(x, dt)
             if not _torch().equal(x, x0):
@@ -81,16 +81,19 @@ class Rollout:
             return e
         return S.euler_stage(x, dt)
 
-    def step(self, S: Solver, q, dt: float) -> Tuple[object, List[Tuple[object, object]]]:
-        """One step at a given dt; returns (q_new, [(stage input, E(input))])."""
+    def step(self, S: Solver, q, dt: float, check: Optional[bool] = None) -> Tuple[object, List[Tuple[object, object]]]:
+        """One step at a given dt; returns (q_new, [(stage input, E(input))]).
+        check: count the stages the limiter changed (default: check_limiter;
+        the backward pass's recomputation skips it, the forward counted)."""
+        ck = self.check_limiter if check is None else check
         if self.cfg.iorder == 2:
-            e1 = self._stage(S, q, dt)
-            e2 = self._stage(S, e1, dt)
+            e1 = self._stage(S, q, dt, ck)
+            e2 = self._stage(S, e1, dt, ck)
             return 0.5 * (q + e2), [(q, e1), (e1, e2)]
-        e1 = self._stage(S, q, dt)
-        e2 = self._stage(S, e1, dt)
+        e1 = self._stage(S, q, dt, ck)
+        e2 = self._stage(S, e1, dt, ck)
         x2 = 0.75 * q + 0.25 * e2
-        e3 = self._stage(S, x2, dt)
+        e3 = self._stage(S, x2, dt, ck)
         return (1.0 / 3.0) * q + (2.0 / 3.0) * e3, [(q, e1), (e1, e2), (x2, e3)]
 
     def forward(self, q0, coll: float, nsteps: int):
@@ -124,98 +127,111 @@ class Rollout:
         cs_last = cs.reshape(-1)[-1]
         return c.cflm_eff / ((vmag + cs_last) * (c.nx / c.lx))
 
-    def _dt_grad(self, q):
-        """d dt / dq: nonzero only on the cell averages of the arg-max cell
-        and of the last cell, so the derivative is taken on those two cells."""
+    def _dt_grad(self, q, dt: float):
+        """d dt / dq, on the device without a host synchronisation.
+
+        dt = cflm / ((vmag + cs_last) dxi) depends on the cell averages of the
+        arg-max cell of vmag = max_d |v_d| + cs and of the last cell (cs_last):
+        d dt = -dt^2 dxi / cflm (d vmag + d cs_last), with, per cell,
+        d|v_k| = sgn(v_k) dm_k / rho - |v_k| drho / rho (k the arg-max
+        direction) and cs^2 = gamma (E/rho - |v|^2/2)."""
         torch = _torch()
         c = self.cfg
-        with torch.no_grad():
-            a = q[0, :5].reshape(5, -1)
-            rho = a[0]
-            v = a[1:4] / rho
-            cs = torch.sqrt(c.aindex * (a[4] / rho - 0.5 * (v * v).sum(0)))
-            v0 = v.abs().amax(0) + cs
-            ok = (v0 > 0) & (rho > c.rh_mult * c.rh_floor)
-            v0 = torch.where(ok, v0, torch.full_like(v0, -math.inf))
-            imax = int(torch.argmax(v0))
+        a = q[0, :5].reshape(5, -1)
+        rho, m, en = a[0], a[1:4], a[4]
+        v = m / rho
+        v2 = (v * v).sum(0)
+        cs = torch.sqrt(c.aindex * (en / rho - 0.5 * v2))
+        av, k = v.abs().max(0)
+        v0 = av + cs
+        ok = (v0 > 0) & (rho > c.rh_mult * c.rh_floor)
+        imax = torch.argmax(torch.where(ok, v0, torch.full_like(v0, -math.inf)))
         ncell = a.shape[1]
+        h = c.aindex / (2.0 * cs * rho)
+        gcs = torch.stack([h * (-en / rho + v2), -h * v[0], -h * v[1], -h * v[2], h])   # d cs / d(rho, m, E)
+        gv = torch.zeros_like(gcs)
+        sg = torch.sign(v.gather(0, k[None])[0])
+        gv[0] = -av / rho
+        gv.scatter_(0, (k + 1)[None], (sg / rho)[None])
+        cells = torch.arange(ncell, device=q.device)
+        sel_i = ((cells == imax) & ok.any()).to(q.dtype)
+        sel_l = (cells == ncell - 1).to(q.dtype)
+        scale = -dt * dt * (c.nx / c.lx) / c.cflm_eff
         g = torch.zeros_like(q)
-        if not math.isfinite(float(v0[imax])):
-            return g
-        with torch.enable_grad():
-            x = a[:, [imax, ncell - 1]].detach().clone().requires_grad_(True)   # (5, 2)
-            r, m, e = x[0], x[1:4], x[4]
-            vv = m / r
-            csx = torch.sqrt(c.aindex * (e / r - 0.5 * (vv * vv).sum(0)))
-            vmag = vv[:, 0].abs().max() + csx[0]
-            dt = c.cflm_eff / ((vmag + csx[1]) * (c.nx / c.lx))
-            (gx,) = torch.autograd.grad(dt, x)
-        gf = g[0, :5].reshape(5, -1)
-        gf[:, imax] += gx[:, 0]
-        gf[:, ncell - 1] += gx[:, 1]
+        g[0, :5] = (scale * (sel_i * (gv + gcs) + sel_l * gcs)).reshape(g[0, :5].shape)
         return g
 
-    def _ddt_stage(self, x, e, lam, dt: float, coll: float) -> float:
-        """lam . dE/ddt for the stage e = E(x)."""
+    def _ddt_stage(self, x, e, lam, dt: float, coll: float):
+        """lam . dE/ddt for the stage e = E(x), a 0-d device tensor."""
         g = (e - x) / dt
         if self.cfg.ivis == 1:
             faci = 1.0 / (1.0 + dt * coll)
             es, xs = e[:, PXX:], x[:, PXX:]
             g[:, PXX:] = (es - faci * xs) / dt - coll * faci * es
-        return float((lam * g).sum())
+        return (lam * g).sum()
+
+    def _dcoll_stage(self, e, lam, dt: float, coll: float):
+        """lam . dE/dcoll for the stage e = E(x) (ivis 1: the stresses are
+        faci (x - dt R) with faci = 1/(1 + dt coll), so dE/dcoll = -dt faci E
+        there), a 0-d device tensor."""
+        faci = 1.0 / (1.0 + dt * coll)
+        return (lam[:, PXX:] * e[:, PXX:]).sum() * (-dt * faci)
 
     # ---- backward -----------------------------------------------------------
     def step_vjp(self, S: Solver, recs, lam, dt: float, coll: float, with_dt: bool = True):
-        """Transpose of one step: (lam_q, dL/dcoll) from lam of its output."""
+        """Transpose of one step: (lam_q, dL/dcoll as a 0-d device tensor) from
+        lam of its output.  Nothing in it waits for the device."""
+        torch = _torch()
         want = self.cfg.ivis == 1
-        dcoll = 0.0
-        ddt = 0.0
+        dcoll = torch.zeros((), dtype=lam.dtype, device=lam.device)
+        ddt = torch.zeros((), dtype=lam.dtype, device=lam.device)
         if self.cfg.iorder == 2:
             (x0, e1), (x1, e2) = recs
             lam_e2 = 0.5 * lam
-            lam_x1, dc = S.stage_vjp(x1, lam_e2, dt, e_out=e2, want_dcoll=want)
-            dcoll += dc or 0.0
+            lam_x1, _ = S.stage_vjp(x1, lam_e2, dt)
+            if want:
+                dcoll = dcoll + self._dcoll_stage(e2, lam_e2, dt, coll) + self._dcoll_stage(e1, lam_x1, dt, coll)
             if with_dt:
-                ddt += self._ddt_stage(x1, e2, lam_e2, dt, coll) + self._ddt_stage(x0, e1, lam_x1, dt, coll)
-            lam_x0, dc = S.stage_vjp(x0, lam_x1, dt, e_out=e1, want_dcoll=want)
-            dcoll += dc or 0.0
+                ddt = ddt + self._ddt_stage(x1, e2, lam_e2, dt, coll) + self._ddt_stage(x0, e1, lam_x1, dt, coll)
+            lam_x0, _ = S.stage_vjp(x0, lam_x1, dt)
             lam_x0 += 0.5 * lam
         else:
             (x0, e1), (x1, e2), (x2, e3) = recs
             lam_e3 = (2.0 / 3.0) * lam
-            lam_x2, dc = S.stage_vjp(x2, lam_e3, dt, e_out=e3, want_dcoll=want)
-            dcoll += dc or 0.0
+            lam_x2, _ = S.stage_vjp(x2, lam_e3, dt)
             lam_e2 = 0.25 * lam_x2
-            lam_x1, dc = S.stage_vjp(x1, lam_e2, dt, e_out=e2, want_dcoll=want)
-            dcoll += dc or 0.0
+            lam_x1, _ = S.stage_vjp(x1, lam_e2, dt)
+            if want:
+                dcoll = (dcoll + self._dcoll_stage(e3, lam_e3, dt, coll) + self._dcoll_stage(e2, lam_e2, dt, coll)
+                         + self._dcoll_stage(e1, lam_x1, dt, coll))
             if with_dt:
-                ddt += (self._ddt_stage(x2, e3, lam_e3, dt, coll) + self._ddt_stage(x1, e2, lam_e2, dt, coll)
-                        + self._ddt_stage(x0, e1, lam_x1, dt, coll))
-            lam_x0, dc = S.stage_vjp(x0, lam_x1, dt, e_out=e1, want_dcoll=want)
-            dcoll += dc or 0.0
+                ddt = (ddt + self._ddt_stage(x2, e3, lam_e3, dt, coll) + self._ddt_stage(x1, e2, lam_e2, dt, coll)
+                       + self._ddt_stage(x0, e1, lam_x1, dt, coll))
+            lam_x0, _ = S.stage_vjp(x0, lam_x1, dt)
             lam_x0 += (1.0 / 3.0) * lam + 0.75 * lam_x2
-        if with_dt and ddt != 0.0:
-            lam_x0 += ddt * self._dt_grad(x0)
+        if with_dt:
+            lam_x0 += ddt * self._dt_grad(x0, dt)
         return lam_x0, dcoll
 
     def backward(self, coll: float, ckpts, dts, lam, with_dt: bool = True):
         """(lam_q0, dL/dcoll) from lam of the final state."""
+        torch = _torch()
         S = self.solver(coll)
         nsteps = len(dts)
         lam = lam.detach().clone().contiguous()
-        dcoll = 0.0
+        dcoll = torch.zeros((), dtype=lam.dtype, device=lam.device)
         for start in sorted(ckpts, reverse=True):
             end = min(start + self.checkpoint_every, nsteps)
             q = ckpts[start].clone()
             seg = []
             for n in range(start, end):
-                q, recs = self.step(S, q, dts[n])
+                q, recs = self.step(S, q, dts[n], check=False)
                 seg.append(recs)
             for n in range(end - 1, start - 1, -1):
                 lam, dc = self.step_vjp(S, seg[n - start], lam, dts[n], coll, with_dt)
-                dcoll += dc
+                dcoll = dcoll + dc
             del seg
-        return lam, dcoll
+        return lam, float(dcoll)
 
 
 def _rollout_fn():

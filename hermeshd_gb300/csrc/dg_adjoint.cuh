@@ -6,8 +6,10 @@
 // (flux.f90:932-1022, sources.f90:12-84).  The transpose of each linear map
 // (traces, interior values, surface and volume quadrature) uses the same
 // compile-time tables as the forward kernels; the point-wise nonlinear maps
-// (numerical face flux, point fluxes, sources) contribute J^T lambda, formed
-// column by column with dual numbers run through the forward physics code.
+// (numerical face flux, point fluxes, sources) contribute J^T lambda, by
+// hand-derived reverse sweeps (dg_flux_vjp.cuh) or, as an independent check
+// (HERMES_ADJOINT_DUAL=1), column by column with dual numbers run through the
+// forward physics code.
 //
 //   k_face_adj  per face point: lambda of the face flux from mu of the two
 //               cells that own the face, J^T of the numerical flux (one
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(ADJ_TPB) k_face_adj(const double* __restrict__
     });
 }
 
-template <class TB>
+template <class TB, bool REV>
 __global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__ Q, const double* __restrict__ mu,
                                                       const double* __restrict__ tadj, double* __restrict__ out, AdjArgs a) {
     constexpr int NB = TB::NB, NF = TB::NF, NPG = TB::NPG;
@@ -325,10 +327,29 @@ __global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__
             lamF[2][v] = -di[2] * a2;
             lamS[v] = -as;
         }
+        double lamu[NQ];
+        if constexpr (REV) {
+            // one reverse sweep of the primitives and the three point fluxes
+            // (dg_flux_vjp.cuh), then the linear sources
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) lamu[v] = 0.0;
+            const SideRev sp = side_primal(ph, u);
+            sfor<3>([&](auto dd) {
+                constexpr int d = decltype(dd)::value;
+                point_flux_rev<d>(ph, u, sp, lamF[d], lamu);
+            });
+            if (src_lin) {   // sources.f90:37-43
+#pragma unroll
+                for (int v = PXX; v < NQ; ++v) lamu[v] = fma(lamS[v], -ph.coll, lamu[v]);
+            }
+            if (src_bf) {    // body force (no reference counterpart): linear in rho and m_x
+                lamu[RH] = fma(lamS[MX], ph.body_force, lamu[RH]);
+                lamu[MX] = fma(lamS[EN], ph.body_force, lamu[MX]);
+            }
+        } else {
         // hydro columns (rh..en): one dual pass each; stress columns in closed
         // form (the stresses enter the point fluxes linearly: f_d[M_i] +=
         // P_{d i}, f_d[E] += P_{d i} v_i, and the ivis-0 source -coll P)
-        double lamu[NQ];
 #pragma unroll 1
         for (int jv = 0; jv <= EN; ++jv) {
             Dual ud[NQ];
@@ -360,6 +381,7 @@ __global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__
             for (int d = 0; d < 3; ++d)
 #pragma unroll
                 for (int i = 0; i < 3; ++i) lamu[PD[d][i]] += fma(lamF[d][EN], vel[i], lamF[d][MX + i]);
+        }
         }
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
@@ -398,8 +420,11 @@ cudaError_t adj_launch(const double* Q, const double* mu, double* tadj, double* 
             else k_face_adj<TB, 2, true><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
         }
     }
-    if (a.G.ncell > 0)
-        k_cell_adj<TB><<<(unsigned)((a.G.ncell + ADJ_TPB - 1) / ADJ_TPB), ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);
+    if (a.G.ncell > 0) {
+        const unsigned nblk = (unsigned)((a.G.ncell + ADJ_TPB - 1) / ADJ_TPB);
+        if (a.dual) k_cell_adj<TB, false><<<nblk, ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);
+        else k_cell_adj<TB, true><<<nblk, ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);
+    }
     return cudaGetLastError();
 }
 

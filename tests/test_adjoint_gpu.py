@@ -244,10 +244,11 @@ def test_adjoint_rejects_unsupported():
 
 @pytest.mark.parametrize("name", sorted(VJP_CASES))
 def test_reverse_sweep_matches_dual_passes(name, monkeypatch):
-    """The face flux VJP has two implementations: a hand-derived reverse sweep
-    (the default) and forward-mode dual numbers, one pass per input column
-    (HERMES_ADJOINT_DUAL=1).  Both are exact derivatives of the same flux, so
-    they agree to rounding."""
+    """The point-wise VJPs (numerical face flux; primitives and point fluxes at
+    the quadrature points) have two implementations: hand-derived reverse
+    sweeps (the default) and forward-mode dual numbers, one pass per input
+    column (HERMES_ADJOINT_DUAL=1).  Both are exact derivatives of the same
+    maps, so they agree to rounding."""
     from hermeshd_gb300.solver import Solver
     cfg, seed = VJP_CASES[name]
     S = Solver(cfg)

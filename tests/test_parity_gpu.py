@@ -37,6 +37,8 @@ RHS_CASES = {
                                        xlobc="outflow", xhibc="wall", ylobc="noslip", yhibc="outflow",
                                        zlobc="wall", zhibc="noslip"), 0.5),
     "nb4_3d_ivis2": (config.Config(nx=5, ny=4, nz=3, nbasis=4, iquad=2, ivis=2, coll=1.5, colvis=1.0), 1.0),
+    "nb8_3d_ivis2_walls": (config.Config(nx=4, ny=5, nz=3, nbasis=8, iquad=2, ivis=2, coll=1.5, colvis=1.0,
+                                         ylobc="wall", yhibc="noslip"), 1.0),
     "nb8_3d_noise": (config.Config(nx=4, ny=4, nz=4, nbasis=8, iquad=2, ivis=1, coll=1.0, colvis=1.0, llns=True,
                                    eta_sd=0.05, zeta_sd=0.01, seed=1234), 0.5),
     "nb4_2d_bodyforce_noslip": (config.Config(nx=6, ny=8, nz=1, nbasis=4, iquad=2, ivis=1, coll=5.0, colvis=1.0,
@@ -215,11 +217,20 @@ def test_nonfinite_is_reported_and_context_survives():
     assert np.isfinite(s.to_numpy(q)).all() and dt > 0
 
 
-def test_ensemble_equals_single_boxes():
+@pytest.mark.parametrize("kind", ["fh_nb4", "nb10_face_traces"])
+def test_ensemble_equals_single_boxes(kind):
+    """Boxes of uneven sizes stepped as one ensemble == each box alone, bit for
+    bit: the fluctuating-hydro box (stochastic stress, per-box Philox key) and
+    an FP64 nbasis-10 box, whose face traces go through the grid-wide trace
+    buffer (cells of every box in one array)."""
     import torch
     from hermeshd_gb300.solver import Ensemble
-    base = config.fh_box(8, precision="fp64", seed=0)
-    dims = [(8, 8, 8), (6, 6, 6), (4, 5, 3)]
+    if kind == "fh_nb4":
+        base = config.fh_box(8, precision="fp64", seed=0)
+        dims = [(8, 8, 8), (6, 6, 6), (4, 5, 3)]
+    else:
+        base = config.Config(nx=6, ny=5, nz=2, nbasis=10, iquad=3, ivis=1, coll=2.0, colvis=1.0)
+        dims = [(6, 5, 2), (4, 4, 3), (5, 3, 1)]
     L = 10.0
     lengths = [(d[0] * L, d[1] * L, d[2] * L) for d in dims]
     seeds = [11, 22, 33]
