@@ -791,8 +791,6 @@ __device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T
     volatile T* ub = cx.ub;   // [2][NQ][2][CELL_CPB]
     const int lc = cx.lc;
     const bool act = cx.act;
-    // the stress thread (here ivis 2, 3) needs its own values at the points
-    const bool need_all = true;
     sfor_seq<XO::NCH>([&](auto cc) {
         constexpr int c = decltype(cc)::value;
         constexpr bool PAIR = XO::pair(c);
@@ -808,7 +806,7 @@ __device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T
                 constexpr int k = decltype(kk)::value;
                 sfor<NQ>([&](auto vv) {
                     constexpr int v = decltype(vv)::value;
-                    u[k][v] = (v <= MZ || need_all) ? T(ubc[(v * 2 + k) * CELL_CPB + lc]) : T(0);
+                    u[k][v] = T(ubc[(v * 2 + k) * CELL_CPB + lc]);
                 });
                 w[k] = primitives(ph, u[k]);
             });
@@ -884,9 +882,10 @@ __device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T
         }
     });
     if (!act) return;
-    // sources linear in the state: their projection is the same linear map of
-    // the coefficients (src_gram is the identity), sources.f90:37-43 and the
-    // body force (no reference counterpart)
+    // the body force (no reference counterpart) is linear in the state: its
+    // projection is the same linear map of the coefficients (src_gram is the
+    // identity); the stress group's linear source (ivis 0) is in
+    // cell_volume_linear_stress
     static_assert(src_gram_is_identity<TB>(), "source projection of a linear field is not the identity");
     if (GRP == 0 && ph.body_force != 0.0) {
         const T bf = T(ph.body_force);
@@ -894,15 +893,6 @@ __device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T
             constexpr int b = decltype(bb)::value;
             acc[MX][b] = fma(bf, T(qs[(b * NQ + RH) * CELL_CPB + lc]), acc[MX][b]);
             acc[EN][b] = fma(bf, T(qs[(b * NQ + MX) * CELL_CPB + lc]), acc[EN][b]);
-        });
-    } else if (GRP == 1 && ph.ivis == 0) {
-        const T mc = -T(ph.coll);
-        sfor<NB>([&](auto bb) {
-            constexpr int b = decltype(bb)::value;
-            sfor<6>([&](auto mm) {
-                constexpr int m = decltype(mm)::value;
-                acc[m][b] = fma(mc, T(qs[(b * NQ + PXX + m) * CELL_CPB + lc]), acc[m][b]);
-            });
         });
     }
 }
