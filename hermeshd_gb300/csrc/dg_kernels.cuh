@@ -364,9 +364,13 @@ struct FaceTraces {
 // ghosts): point fluxes of both sides (flux.f90:240), central flux or LLF
 // with the freezing speed (flux.f90:243-262), then HLLC (flux.f90:264-271) or
 // Roe (SEAN monolith) for rh..en.  Shared by k_face and the adjoint.
+// F comes out multiplied by sc (the face kernel's inverse spacing): the
+// central rows as (fL + fR) * (0.5 sc), the same rounding as 0.5 (fL + fR)
+// scaled afterwards, since 0.5 sc is exact; with HLLC the central values of
+// rh..en, which HLLC replaces, are not formed.
 template <class T, int DIR>
 __device__ __forceinline__ void face_flux_fn(const Phys& ph, const T qL[NQ], const T qR[NQ], const T SL[6], const T SR[6],
-                                             T rho_i_last, T F[NQ]) {
+                                             T rho_i_last, T F[NQ], T sc = T(1)) {
     T fL[NQ], fR[NQ];
     const Prim<T> wL = primitives(ph, qL);
     point_flux<T, DIR>(ph, qL, wL, SL, fL);
@@ -375,18 +379,23 @@ __device__ __forceinline__ void face_flux_fn(const Phys& ph, const T qL[NQ], con
     if (ph.ivis >= 2) {   // ivis 3: the Grad-closure code always applies LLF (ten_moment.f90:1131-1147)
         const T cfr = fmax(cfcal<T, DIR>(ph, qL), cfcal<T, DIR>(ph, qR));
 #pragma unroll
-        for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]) - T(0.5) * cfr * (qR[v] - qL[v]);
+        for (int v = 0; v < NQ; ++v) F[v] = (T(0.5) * (fL[v] + fR[v]) - T(0.5) * cfr * (qR[v] - qL[v])) * sc;
     } else {
+        const T h = T(0.5) * sc;
+        const bool hl = ph.ihllc == 1;
 #pragma unroll
-        for (int v = 0; v < NQ; ++v) F[v] = T(0.5) * (fL[v] + fR[v]);
+        for (int v = 0; v < NQ; ++v)
+            if (v >= PXX || !hl) F[v] = (fL[v] + fR[v]) * h;
     }
     if (ph.ihllc == 2) {
         T FR[NQ];
         if (roe<T, DIR>(ph, qL, qR, fL, fR, FR)) {
-            F[RH] = FR[RH]; F[MX] = FR[MX]; F[MY] = FR[MY]; F[MZ] = FR[MZ]; F[EN] = FR[EN];
+            F[RH] = FR[RH] * sc; F[MX] = FR[MX] * sc; F[MY] = FR[MY] * sc; F[MZ] = FR[MZ] * sc; F[EN] = FR[EN] * sc;
         }
     } else if (ph.ihllc == 1) {
         hllc<T, DIR>(ph, qL, qR, fL, fR, wL.dni, wR.dni, rho_i_last, F);
+#pragma unroll
+        for (int v = RH; v <= EN; ++v) F[v] = F[v] * sc;
     }
 }
 
@@ -511,13 +520,12 @@ __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restric
             rho_i_last = T(1) / rlast;
         }
     }
-    face_flux_fn<T, DIR>(ph, qL, qR, SL, SR, rho_i_last, F);
-    // store, scaled by the inverse spacing of this direction
-    const T sc = T(B.di[DIR]);
+    // scaled by the inverse spacing of this direction
+    face_flux_fn<T, DIR>(ph, qL, qR, SL, SR, rho_i_last, F, T(B.di[DIR]));
     const long long nfd = (long long)ex * ey * (DIR == 2 ? B.nfp[2] : n2);
     T* fb = flux + B.fbase[DIR];
 #pragma unroll
-    for (int v = 0; v < NQ; ++v) fb[(long long)(v * TB::NF + P) * nfd + lf] = F[v] * sc;
+    for (int v = 0; v < NQ; ++v) fb[(long long)(v * TB::NF + P) * nfd + lf] = F[v];
 }
 
 // resident blocks per SM the face kernel's register allocation must allow:
