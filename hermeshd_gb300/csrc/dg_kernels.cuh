@@ -393,7 +393,7 @@ __device__ __forceinline__ void face_flux_fn(const Phys& ph, const T qL[NQ], con
             F[RH] = FR[RH] * sc; F[MX] = FR[MX] * sc; F[MY] = FR[MY] * sc; F[MZ] = FR[MZ] * sc; F[EN] = FR[EN] * sc;
         }
     } else if (ph.ihllc == 1) {
-        hllc<T, DIR>(ph, qL, qR, fL, fR, wL.dni, wR.dni, rho_i_last, F);
+        hllc<T, DIR>(ph, qL, qR, fL, fR, wL, wR, rho_i_last, F);
 #pragma unroll
         for (int v = RH; v <= EN; ++v) F[v] = F[v] * sc;
     }

@@ -102,6 +102,7 @@ __device__ __forceinline__ void random_stress(const Phys& ph, unsigned long long
 template <class T>
 struct Prim {
     T dn, dni, vx, vy, vz, P, P_10;
+    T Pig;   // ideal-gas pressure before the Tait term and the floor (HLLC's p)
 };
 
 template <class T>
@@ -114,11 +115,17 @@ __device__ __forceinline__ Prim<T> primitives(const Phys& ph, const T q[NQ]) {
     w.vz = q[MZ] * w.dni;
     T smsq = q[MX] * q[MX] + q[MY] * q[MY] + q[MZ] * q[MZ];
     w.P = T(ph.aindm1) * (q[EN] - T(0.5) * w.dni * smsq);
-    w.P_10 = T(1.0 / 3.0) * (q[PXX] + q[PYY] + q[PZZ] - w.dni * smsq);
+    w.Pig = w.P;
     if (ph.ieos == 2) w.P = T(ph.P_1) * (pow(w.dn, T(7.2)) - T(1)) + T(ph.P_base) + w.P;
     const T Pf = T(ph.P_floor);
     if (w.P < Pf) w.P = Pf;
-    if (w.P_10 < Pf) w.P_10 = Pf;
+    // the 10-moment pressure enters only the ivis 2/3 fluxes (flux.f90:91-95)
+    if (ph.ivis >= 2) {
+        w.P_10 = T(1.0 / 3.0) * (q[PXX] + q[PYY] + q[PZZ] - w.dni * smsq);
+        if (w.P_10 < Pf) w.P_10 = Pf;
+    } else {
+        w.P_10 = T(0);
+    }
     return w;
 }
 
@@ -230,17 +237,21 @@ __device__ __forceinline__ T cfcal(const Phys& ph, const T q[NQ]) {
 // ---------------------------------------------------------------------------
 template <class T, int DIR>
 __device__ __forceinline__ void hllc(const Phys& ph, const T qL[NQ], const T qR[NQ], const T fL[NQ], const T fR[NQ],
-                                     T dniL, T dniR, T rho_i_last, T F[NQ]) {
-    // dniL, dniR: 1/rho of the two states, as computed by primitives()
+                                     const Prim<T>& PL, const Prim<T>& PR, T rho_i_last, T F[NQ]) {
+    // PL, PR: the primitives of the two states (primitives()).  The velocities
+    // are theirs; p is the unfloored ideal-gas pressure, which flux.f90:525
+    // forms as aindm1 (E - rho |v|^2 / 2): here aindm1 (E - |m|^2 / rho / 2),
+    // equal to rounding
     constexpr int IPAR = DIR == 0 ? MX : DIR == 1 ? MY : MZ;
     constexpr int IP1 = DIR == 0 ? MY : DIR == 1 ? MZ : MX;
     constexpr int IP2 = DIR == 0 ? MZ : DIR == 1 ? MX : MY;
-    const T aindex = T(ph.aindex), aindm1 = T(ph.aindm1);
+    const T aindex = T(ph.aindex);
+    const T dniL = PL.dni, dniR = PR.dni;
     const T rhoL = qL[RH], rhoR = qR[RH];
-    const T uL = qL[IPAR] * dniL, vL = qL[IP1] * dniL, wL = qL[IP2] * dniL;
-    const T uR = qR[IPAR] * dniR, vR = qR[IP1] * dniR, wR = qR[IP2] * dniR;
-    T pL = aindm1 * (qL[EN] - T(0.5) * rhoL * (uL * uL + vL * vL + wL * wL));
-    T pR = aindm1 * (qR[EN] - T(0.5) * rhoR * (uR * uR + vR * vR + wR * wR));
+    const T uL = DIR == 0 ? PL.vx : DIR == 1 ? PL.vy : PL.vz;
+    const T uR = DIR == 0 ? PR.vx : DIR == 1 ? PR.vy : PR.vz;
+    T pL = PL.Pig;
+    T pR = PR.Pig;
     T cL, cR;
     if (ph.ieos == 2) {
         pL = T(ph.P_1) * (pow(rhoL, T(7.2)) - T(1)) + T(ph.P_base) + pL;
