@@ -2,9 +2,10 @@
 // step, templated on the arithmetic type T and the basis (NB, NQD):
 //
 //   k_limit  positivity limiter, in place on the stage input (flux.f90:1077-1164)
-//   k_face   traces + point fluxes + central/LLF + HLLC at every face point of
-//            one direction (flux.f90:197-450,466-647; boundary ghosts of
-//            prepare_step.f90:20-179 and boundary.f90:40-338 synthesised in place)
+//   k_face   traces (evaluated here, or read from k_trace's buffer,
+//            dg_trace.cuh) + point fluxes + central/LLF + HLLC at every face
+//            point of one direction (flux.f90:197-450,466-647; boundary ghosts
+//            of prepare_step.f90:20-179 and boundary.f90:40-338 synthesised in place)
 //   k_cell   volume quadrature + surface assembly + sources + forward-Euler
 //            update + RK combination (flux.f90:751-1022, sources.f90:12-84,
 //            integrator.f90:62-252), one write of the stage output
@@ -13,6 +14,10 @@
 // Basis and quadrature tables are compile-time constants (dg_tables_gen.cuh)
 // and every zero entry is skipped at compile time: on GB300 the FP64 pipe is
 // the binding resource of the FP64 path, so each skipped term is time saved.
+// For the same reason the kernels use the tables' mirror symmetries (each
+// entry at a mirrored point is +- the entry at the point, asserted at compile
+// time): values at a mirror pair of points from one even and one odd sum, and
+// quadrature sums over a pair as one product with a sum or difference.
 #pragma once
 
 #include <cfloat>
@@ -550,13 +555,12 @@ __global__ void __launch_bounds__(FACE_TPB, (FaceMinBlocks<T>::value)) k_face(co
 // ===========================================================================
 // k_cell: two threads per cell.  In a block of 2*CELL_CPB threads, thread
 // c < CELL_CPB owns the hydro variables rh..en of cell c and thread
-// CELL_CPB + c owns the six stress variables of the same cell.  The cell's
-// coefficients are shared through one shared-memory column per cell; each
-// thread keeps the volume-quadrature accumulators of its own variables in
-// registers.  The stress thread re-evaluates rho and the momenta at the
-// quadrature points (its fluxes need the velocity), a few per cent of the
-// cell's FP64 work, in exchange for twice the threads and no accumulator
-// traffic through shared memory.
+// CELL_CPB + c owns the six stress variables of the same cell (each group
+// fills whole warps).  The cell's coefficients are shared through one
+// shared-memory column per cell; each thread evaluates its own variables at
+// the quadrature points and the pair swaps them through an exchange buffer,
+// one x-mirror orbit of points at a time; each thread keeps the
+// volume-quadrature accumulators of its own variables in registers.
 // ===========================================================================
 struct CellArgs {
     Geom G;
