@@ -103,7 +103,13 @@ class Hermeshd:
 
     def setup(self, q_io, t, dt, t1, t_start, dtout, nout, comm=0):
         """hermeshd.f90:67-114: initializer (tables, spacing, dt), initial
-        condition into q_io, integrator and boundary selection."""
+        condition into q_io, integrator and boundary selection.  As set_ic
+        does (initialcon.f90:29-32), ivis 0 zeroes coll and colvis."""
+        if self.cfg is not None and not self.iread and self.cfg.ivis == 0 and (self.cfg.coll or self.cfg.colvis):
+            self.cfg = self.cfg.replace(coll=0.0, colvis=0.0)
+            if self.solver is not None:
+                self.solver.close()
+                self.solver = None
         s = self._need()
         cfg = self.cfg
         _set0d(t, 0.0)
