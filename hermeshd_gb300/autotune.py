@@ -15,7 +15,11 @@ include/hermes_gb300.h):
 * ``face_traces``      face traces evaluated once per stage by their own
                        kernel and read by the face kernels (1) or evaluated
                        by the face kernels (0); tuned where the trace kernel
-                       exists (FP64, nbasis 8/10, no stochastic stress).
+                       exists (FP64, nbasis 8/10, no stochastic stress);
+* ``split_update``     the cell update as the volume kernel plus a surface and
+                       update kernel of one thread per (cell, variable) (1) or
+                       one kernel (0); tuned where it exists (FP64, ivis 0/1,
+                       no stochastic stress).
 
 The cell kernel keeps 32 cells per block: its hydro and stress thread groups
 must each fill whole warps, and its register cap is fixed at compile time.
@@ -40,6 +44,7 @@ KNOBS = {
     "steps_per_graph": (1, 2, 4, 8),
     "noise_inline": (0, 1),          # tuned only with the stochastic stress on
     "face_traces": (1, 0),           # tuned only where the context has the trace buffer
+    "split_update": (1, 0),          # tuned only where the context has the split-update buffer
 }
 
 
@@ -118,8 +123,10 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
     knobs = dict(knobs or KNOBS)
     if not solver.cfg.llns:
         knobs.pop("noise_inline", None)
-    if solver.get_launch()["face_traces"] == 0:
-        knobs.pop("face_traces", None)
+    cur = solver.get_launch()
+    for k in ("face_traces", "split_update"):
+        if cur[k] == 0:
+            knobs.pop(k, None)
     qt, q1t = q.clone(), q.clone()
     best = {k: v[0] for k, v in knobs.items()}
     solver.set_launch(**best)

@@ -572,6 +572,7 @@ struct CellArgs {
     int mode, comb;
     int split_source;   // Grad closure with RK2: the implicit source step after the update
     const void* noise;  // staged interior stochastic stress (k_noise_cell), or null: drawn here
+    void* accbuf;       // split update: k_cell stores the volume terms here, k_update finishes
 };
 
 // RK combination of integrator.f90:62-86
@@ -920,6 +921,81 @@ __device__ __forceinline__ void cell_store(const CellArgs& a, CellCtx<T>& cx, in
     cx.ob[(long long)(b * NQ + v) * cx.nc + cx.le] = o;
 }
 
+// the minus and plus face of local cell le in each direction and the face
+// count of each direction of box B (periodic directions wrap the plus face)
+__device__ __forceinline__ void cell_faces(const Box& B, long long le, long long (&fm)[3], long long (&fp)[3],
+                                           long long (&nfd)[3]) {
+    const int n0 = B.n[0], n1 = B.n[1];
+    const unsigned leu = (unsigned)le, t = leu / (unsigned)n0;   // fewer than 2^31 cells per box
+    const int c[3] = {(int)(leu - t * (unsigned)n0), (int)(t % (unsigned)n1), (int)(t / (unsigned)n1)};
+    for (int d = 0; d < 3; ++d) {
+        const int e0 = d == 0 ? B.nfp[0] : B.n[0], e1 = d == 1 ? B.nfp[1] : B.n[1], e2 = d == 2 ? B.nfp[2] : B.n[2];
+        nfd[d] = (long long)e0 * e1 * e2;
+        int hi = c[d] + 1;
+        if (B.nfp[d] == B.n[d] && hi == B.n[d]) hi = 0;
+        int a0 = d == 0 ? c[d] : c[0], a1 = d == 1 ? c[d] : c[1], a2 = d == 2 ? c[d] : c[2];
+        fm[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
+        a0 = d == 0 ? hi : c[0]; a1 = d == 1 ? hi : c[1]; a2 = d == 2 ? hi : c[2];
+        fp[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
+    }
+}
+
+// the surface sums of variable v of one cell (flux.f90:958-978) added to
+// r[b]: the fluxes of its plus and minus face of each direction
+template <class T, class TB>
+__device__ __forceinline__ void surface_add(const T* __restrict__ flux, const Box& B, const long long (&fm)[3],
+                                            const long long (&fp)[3], const long long (&nfd)[3], int v,
+                                            T (&r)[TB::NB]) {
+    constexpr int NB = TB::NB, NF = TB::NF;
+    sfor<3>([&](auto dd) {
+        constexpr int d = decltype(dd)::value;
+        using FO = FOrbit<TB>;
+        static_assert(face_tables_symmetric<TB, d, true>(), "surface tables not mirror-symmetric");
+        const T* fb = flux + B.fbase[d] + (long long)v * NF * nfd[d];
+        if constexpr (!std::is_same<T, double>::value) {
+            // FP32 (not bound by its arithmetic): the two faces of a point
+            // only, which keeps the register footprint of the FP32 kernels
+            sfor<NF>([&](auto pp) {
+                constexpr int p = decltype(pp)::value;
+                const T Fp = __ldg(fb + (long long)p * nfd[d] + fp[d]);
+                const T Fm = __ldg(fb + (long long)p * nfd[d] + fm[d]);
+                const T Fs = Fp + Fm, Fd = Fp - Fm;
+                sfor<NB>([&](auto bb) {
+                    constexpr int b = decltype(bb)::value;
+                    constexpr double cp = stab<TB, d, 1>(p, b), cm = stab<TB, d, 0>(p, b);
+                    if constexpr (cp != 0.0) r[b] = fma(T(cp), cm == cp ? Fs : Fd, r[b]);
+                });
+            });
+            return;
+        }
+        // the weights of the plus and minus faces at a tangential mirror pair
+        // of points are +-one value (the parity of the function along d and
+        // along the mirror): one product per chunk with a signed sum of the
+        // four fluxes
+        sfor<FO::NCH>([&](auto cc) {
+            constexpr int c = decltype(cc)::value;
+            constexpr int pA = FO::pA(c), pB = FO::pB(c);
+            const T FpA = __ldg(fb + (long long)pA * nfd[d] + fp[d]);
+            const T FmA = __ldg(fb + (long long)pA * nfd[d] + fm[d]);
+            const T XsA = FpA + FmA, XdA = FpA - FmA;
+            T X[4];
+            if constexpr (FO::pair(c)) {
+                const T FpB = __ldg(fb + (long long)pB * nfd[d] + fp[d]);
+                const T FmB = __ldg(fb + (long long)pB * nfd[d] + fm[d]);
+                const T XsB = FpB + FmB, XdB = FpB - FmB;
+                X[0] = XsA + XsB; X[1] = XdA + XdB; X[2] = XsA - XsB; X[3] = XdA - XdB;
+            } else {
+                X[0] = XsA; X[1] = XdA; X[2] = T(0); X[3] = T(0);
+            }
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                constexpr int k = face_class<TB, d, true>(c, b);
+                if constexpr (k >= 0) r[b] = fma(T(stab<TB, d, 1>(pA, b)), X[k], r[b]);
+            });
+        });
+    });
+}
+
 // phase 2: surface assembly (flux.f90:958-978), update and RK combination,
 // one variable at a time
 template <class T, class TB, int GRP>
@@ -937,53 +1013,7 @@ __device__ __forceinline__ void cell_surface_update(const CellArgs& a, CellCtx<T
         constexpr int v = GV0 + m;
         T r[NB];
         sfor<NB>([&](auto bb) { r[decltype(bb)::value] = -acc[m][decltype(bb)::value]; });
-        sfor<3>([&](auto dd) {
-            constexpr int d = decltype(dd)::value;
-            using FO = FOrbit<TB>;
-            static_assert(face_tables_symmetric<TB, d, true>(), "surface tables not mirror-symmetric");
-            const T* fb = flux + cx.B->fbase[d] + (long long)v * NF * cx.nfd[d];
-            if constexpr (!std::is_same<T, double>::value) {
-                // FP32 (not bound by its arithmetic): the two faces of a point
-                // only, which keeps the register footprint of the FP32 kernels
-                sfor<NF>([&](auto pp) {
-                    constexpr int p = decltype(pp)::value;
-                    const T Fp = __ldg(fb + (long long)p * cx.nfd[d] + cx.fp[d]);
-                    const T Fm = __ldg(fb + (long long)p * cx.nfd[d] + cx.fm[d]);
-                    const T Fs = Fp + Fm, Fd = Fp - Fm;
-                    sfor<NB>([&](auto bb) {
-                        constexpr int b = decltype(bb)::value;
-                        constexpr double cp = stab<TB, d, 1>(p, b), cm = stab<TB, d, 0>(p, b);
-                        if constexpr (cp != 0.0) r[b] = fma(T(cp), cm == cp ? Fs : Fd, r[b]);
-                    });
-                });
-                return;
-            }
-            // the weights of the plus and minus faces at a tangential mirror pair
-            // of points are +-one value (the parity of the function along d and
-            // along the mirror): one product per chunk with a signed sum of the
-            // four fluxes
-            sfor<FO::NCH>([&](auto cc) {
-                constexpr int c = decltype(cc)::value;
-                constexpr int pA = FO::pA(c), pB = FO::pB(c);
-                const T FpA = __ldg(fb + (long long)pA * cx.nfd[d] + cx.fp[d]);
-                const T FmA = __ldg(fb + (long long)pA * cx.nfd[d] + cx.fm[d]);
-                const T XsA = FpA + FmA, XdA = FpA - FmA;
-                T X[4];
-                if constexpr (FO::pair(c)) {
-                    const T FpB = __ldg(fb + (long long)pB * cx.nfd[d] + cx.fp[d]);
-                    const T FmB = __ldg(fb + (long long)pB * cx.nfd[d] + cx.fm[d]);
-                    const T XsB = FpB + FmB, XdB = FpB - FmB;
-                    X[0] = XsA + XsB; X[1] = XdA + XdB; X[2] = XsA - XsB; X[3] = XdA - XdB;
-                } else {
-                    X[0] = XsA; X[1] = XdA; X[2] = T(0); X[3] = T(0);
-                }
-                sfor<NB>([&](auto bb) {
-                    constexpr int b = decltype(bb)::value;
-                    constexpr int k = face_class<TB, d, true>(c, b);
-                    if constexpr (k >= 0) r[b] = fma(T(stab<TB, d, 1>(pA, b)), X[k], r[b]);
-                });
-            });
-        });
+        surface_add<T, TB>(flux, *cx.B, cx.fm, cx.fp, cx.nfd, v, r);
         // r[b] = glflux - source of variable v
         if (a.mode == MODE_RHS) {
             sfor<NB>([&](auto bb) {
@@ -1098,7 +1128,11 @@ struct CellMinBlocks {
                                                                : (NB <= 4 ? 6 : NB <= 8 ? 5 : 4);
 };
 
-template <class T, class TB, bool NOISE>
+// SPLIT: the volume phase only; the volume terms go to a.accbuf and
+// k_update adds the surface sums and does the update, one thread per
+// (cell, variable), so the surface phase runs at full occupancy (ivis 0/1,
+// FP64; the same operations in the same order, so the same bits)
+template <class T, class TB, bool NOISE, bool SPLIT>
 __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value))
     k_cell(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux, CellArgs a) {
     // Qin, Q0 and out may alias (the RK stages write in place); every element
@@ -1138,21 +1172,7 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
     cx.q0b = Q0 ? Q0 + B.q0 : nullptr;
     cx.bad = false;
     for (int d = 0; d < 3; ++d) { cx.fm[d] = 0; cx.fp[d] = 0; cx.nfd[d] = 1; }
-    if (cx.act) {
-        const int n0 = B.n[0], n1 = B.n[1];
-        const unsigned leu = (unsigned)cx.le, t = leu / (unsigned)n0;   // fewer than 2^31 cells per box
-        const int c[3] = {(int)(leu - t * (unsigned)n0), (int)(t % (unsigned)n1), (int)(t / (unsigned)n1)};
-        for (int d = 0; d < 3; ++d) {
-            const int e0 = d == 0 ? B.nfp[0] : B.n[0], e1 = d == 1 ? B.nfp[1] : B.n[1], e2 = d == 2 ? B.nfp[2] : B.n[2];
-            cx.nfd[d] = (long long)e0 * e1 * e2;
-            int hi = c[d] + 1;
-            if (B.nfp[d] == B.n[d] && hi == B.n[d]) hi = 0;
-            int a0 = d == 0 ? c[d] : c[0], a1 = d == 1 ? c[d] : c[1], a2 = d == 2 ? c[d] : c[2];
-            cx.fm[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
-            a0 = d == 0 ? hi : c[0]; a1 = d == 1 ? hi : c[1]; a2 = d == 2 ? hi : c[2];
-            cx.fp[d] = (long long)a0 + (long long)e0 * (a1 + (long long)e1 * a2);
-        }
-    }
+    if (cx.act) cell_faces(B, cx.le, cx.fm, cx.fp, cx.nfd);
     __syncthreads();
 
     T acc[6][NB];
@@ -1163,6 +1183,21 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
     // every thread runs the volume phase: it holds one block barrier per orbit
     if (grp == 0) cell_volume<T, TB, 0, NOISE>(a, cx, acc);
     else cell_volume<T, TB, 1, NOISE>(a, cx, acc);
+    if constexpr (SPLIT) {
+        // [variable][basis][cell of the grid]
+        if (cx.act) {
+            T* ab = static_cast<T*>(a.accbuf);
+            const long long ncl = a.G.ncell;
+            const int v0 = grp == 0 ? 0 : PXX, nv = grp == 0 ? 5 : 6;
+#pragma unroll
+            for (int m = 0; m < 6; ++m)
+                if (m < nv) {
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) ab[((long long)(v0 + m) * NB + b) * ncl + gc] = acc[m][b];
+                }
+        }
+        return;
+    }
     __syncthreads();   // every read of the other group's coefficients is done
     if (cx.act) {
         if (grp == 0) cell_surface_update<T, TB, 0>(a, cx, flux, acc);
@@ -1173,6 +1208,52 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
         if (grp == 1 && cx.act) cell_split_source<T, TB>(a, cx);
     }
     if (cx.bad) a.flags[0] |= FLAG_NONFINITE;   // integrator.f90:234-250 (the reference exits)
+}
+
+// k_update: the second half of a split k_cell (ivis 0/1): thread per (cell,
+// variable), blockIdx.y = variable.  r = surface sums - volume terms, then the
+// forward-Euler update (integrator.f90:147-149,171-174), the RK combination and
+// the NaN check of the cell average, as cell_surface_update does.
+constexpr int UPD_TPB = 128;
+template <class T, class TB>
+__global__ void __launch_bounds__(UPD_TPB) k_update(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux,
+                                                   CellArgs a) {
+    constexpr int NB = TB::NB;
+    const long long gc = (long long)blockIdx.x * UPD_TPB + threadIdx.x;
+    if (gc >= a.G.ncell) return;
+    const int v = blockIdx.y;
+    const int bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
+    const Box& B = a.G.boxes[bx];
+    const long long le = gc - B.cell0, nc = B.ncell, ncl = a.G.ncell;
+    long long fm[3], fp[3], nfd[3];
+    cell_faces(B, le, fm, fp, nfd);
+    const T* ab = static_cast<const T*>(a.accbuf);
+    T r[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) r[b] = -ab[((long long)v * NB + b) * ncl + gc];
+    surface_add<T, TB>(flux, B, fm, fp, nfd, v, r);
+    T* ob = out + B.q0;
+    if (a.mode == MODE_RHS) {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) ob[(long long)(b * NQ + v) * nc + le] = r[b];
+        return;
+    }
+    const T dt = T(a.st[bx].dt), faci = T(1) / (T(1) + dt * T(a.ph.coll));
+    const T* qb = Qin + B.q0;
+    const T* q0b = Q0 ? Q0 + B.q0 : nullptr;
+    const bool stress_faci = v >= PXX && a.ph.ivis == 1;
+    bool bad = false;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const long long ix = (long long)(b * NQ + v) * nc + le;
+        T e = qb[ix] - dt * r[b];
+        if (stress_faci) e = faci * e;
+        T o = e;
+        if (a.comb != COMB_NONE) o = rk_combine(a.comb, q0b[ix], o);
+        if (b == 0 && o != o) bad = true;
+        ob[ix] = o;
+    }
+    if (bad) a.flags[0] |= FLAG_NONFINITE;
 }
 
 // ===========================================================================

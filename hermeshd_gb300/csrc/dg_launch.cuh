@@ -31,9 +31,19 @@ template <class T, int NB, int NQD>
 struct Launch {
     using TB = hermes_tab::Tab<NB, NQD>;
     static size_t cell_smem() { return (size_t)(NB * NQ + 4 * NQ) * CELL_CPB * sizeof(T); }
+    // the split update (k_cell volume phase + k_update) exists for FP64
+    // without the stochastic stress
+    static constexpr bool HAS_SPLIT = std::is_same<T, double>::value;
     template <bool NOISE>
     static cudaError_t prepare_cell() {
-        return cudaFuncSetAttribute(k_cell<T, TB, NOISE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cell_smem());
+        cudaError_t e = cudaFuncSetAttribute(k_cell<T, TB, NOISE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)cell_smem());
+        if constexpr (HAS_SPLIT && !NOISE) {
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_cell<T, TB, NOISE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)cell_smem());
+        }
+        return e;
     }
     static void limit(void* Q, const Geom& G, const Phys& ph, cudaStream_t s) {
         if (G.ncell <= 0) return;
@@ -75,8 +85,19 @@ struct Launch {
     static void cell(const void* Qin, const void* Q0, void* out, const void* flux, const CellArgs& a, cudaStream_t s) {
         if (a.G.ncell <= 0) return;
         const unsigned nb = (unsigned)((a.G.ncell + CELL_CPB - 1) / CELL_CPB);
-        k_cell<T, TB, NOISE><<<nb, 2 * CELL_CPB, cell_smem(), s>>>(static_cast<const T*>(Qin), static_cast<const T*>(Q0),
-                                                                 static_cast<T*>(out), static_cast<const T*>(flux), a);
+        const T* qi = static_cast<const T*>(Qin);
+        const T* q0 = static_cast<const T*>(Q0);
+        T* o = static_cast<T*>(out);
+        const T* f = static_cast<const T*>(flux);
+        if constexpr (HAS_SPLIT && !NOISE) {
+            if (a.accbuf && a.ph.ivis < 2 && !a.split_source) {
+                k_cell<T, TB, NOISE, true><<<nb, 2 * CELL_CPB, cell_smem(), s>>>(qi, q0, o, f, a);
+                const dim3 grid((unsigned)((a.G.ncell + UPD_TPB - 1) / UPD_TPB), NQ);
+                k_update<T, TB><<<grid, UPD_TPB, 0, s>>>(qi, q0, o, f, a);
+                return;
+            }
+        }
+        k_cell<T, TB, NOISE, false><<<nb, 2 * CELL_CPB, cell_smem(), s>>>(qi, q0, o, f, a);
     }
     static void mindt(const void* Q, const DtArgs& a, cudaStream_t s) {
         if (a.G.ncell <= 0) return;

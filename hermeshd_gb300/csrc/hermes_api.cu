@@ -153,6 +153,9 @@ struct hermes_ctx {
     // face traces evaluated once per stage (dg_trace.cuh)
     void* d_traces = nullptr;
     bool face_traces = false;
+    // split cell update: volume terms of k_cell for k_update
+    void* d_accbuf = nullptr;
+    bool split_update = false;
     // adjoint scratch, allocated on first use
     AdjFn adj = nullptr;
     double* d_tadj = nullptr;   // trace adjoints: 2 x the face-flux size
@@ -331,7 +334,7 @@ void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
 void enq_cell(hermes_ctx* c, const void* qin, const void* q0, void* out, int mode, int comb, unsigned stage) {
     const int split = (mode == MODE_STAGE && c->cfg.ivis == 3 && c->cfg.iorder == 2) ? 1 : 0;
     CellArgs a{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb, split,
-               c->noise_staged ? c->d_noise_cell : nullptr};
+               c->noise_staged ? c->d_noise_cell : nullptr, c->split_update ? c->d_accbuf : nullptr};
     ProfScope ps(c, 5);
     c->K.cell(qin, q0, out, c->d_flux, a, c->stream);
 }
@@ -495,6 +498,11 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
             c->d_noise_cell = c->d_noise_face = nullptr;
         }
     }
+    if (c->K.elem_size == (int)sizeof(double) && !cfg->llns && cfg->ivis < 2) {
+        // split cell update: NQ x nbasis volume terms per cell
+        if (cudaMalloc(&c->d_accbuf, (size_t)ncell * NQ * c->K.nb * sizeof(double)) == cudaSuccess) c->split_update = true;
+        else { cudaGetLastError(); c->d_accbuf = nullptr; }   // no room: one kernel
+    }
     if (c->K.trace) {
         // face traces: 2 sides x 3 directions x NQ x NF values per cell
         const size_t bytes = (size_t)ncell * 6 * NQ * c->K.nf * c->K.elem_size;
@@ -584,6 +592,7 @@ int hermes_destroy(hermes_ctx* c) {
     cudaFree(c->d_noise_cell);
     cudaFree(c->d_noise_face);
     cudaFree(c->d_traces);
+    cudaFree(c->d_accbuf);
     delete c;
     return HERMES_OK;
 }
@@ -795,7 +804,12 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     if (l->face_traces == 1 && !c->d_traces)
         return fail(c, HERMES_ERR_ARG, "face traces need FP64, nbasis 8 or 10, no stochastic stress and room for the buffer");
     const bool traces = l->face_traces == 1;
-    if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged || traces != c->face_traces) {
+    if (l->split_update != 0 && l->split_update != 1) return fail(c, HERMES_ERR_ARG, "split_update must be 0 or 1");
+    if (l->split_update == 1 && !c->d_accbuf)
+        return fail(c, HERMES_ERR_ARG, "the split update needs FP64, ivis 0/1, no stochastic stress and room for the buffer");
+    const bool split = l->split_update == 1;
+    if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged || traces != c->face_traces ||
+        split != c->split_update) {
         // captured graphs hold the old launch shape
         HCK(c, cudaSetDevice(c->device));
         HCK(c, cudaStreamSynchronize(c->stream));
@@ -806,6 +820,7 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     c->graph_steps = g > 0 ? g : 1;
     c->noise_staged = staged;
     c->face_traces = traces;
+    c->split_update = split;
     return HERMES_OK;
 }
 
@@ -816,6 +831,7 @@ int hermes_get_launch(hermes_ctx* c, hermes_launch* l) {
     l->steps_per_graph = c->graph_steps;
     l->noise_inline = (c->cfg.llns && !c->noise_staged) ? 1 : 0;
     l->face_traces = c->face_traces ? 1 : 0;
+    l->split_update = c->split_update ? 1 : 0;
     return HERMES_OK;
 }
 

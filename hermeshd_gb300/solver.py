@@ -175,15 +175,21 @@ class Solver:
         l = _lib.HermesLaunch()
         check(lib().hermes_get_launch(self.ctx, C.byref(l)), self.ctx)
         return {"face_tpb": l.face_tpb, "dt_tpb": l.dt_tpb, "steps_per_graph": l.steps_per_graph,
-                "noise_inline": l.noise_inline, "face_traces": l.face_traces}
+                "noise_inline": l.noise_inline, "face_traces": l.face_traces, "split_update": l.split_update}
 
     def set_launch(self, face_tpb: int = 0, dt_tpb: int = 0, steps_per_graph: int = 1, noise_inline: int = 0,
-                   face_traces=None):
-        """face_traces None keeps the context's current choice (on by default
-        where the trace kernel exists: FP64, nbasis 8/10, no stochastic stress)."""
+                   face_traces=None, split_update=None):
+        """face_traces / split_update None keep the context's current choice
+        (on by default where they exist: the trace kernel for FP64, nbasis
+        8/10, no stochastic stress; the split update for FP64, ivis 0/1, no
+        stochastic stress)."""
+        cur = self.get_launch()
         if face_traces is None:
-            face_traces = self.get_launch()["face_traces"]
-        l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), int(noise_inline), int(face_traces))
+            face_traces = cur["face_traces"]
+        if split_update is None:
+            split_update = cur["split_update"]
+        l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), int(noise_inline), int(face_traces),
+                              int(split_update))
         check(lib().hermes_set_launch(self.ctx, C.byref(l)), self.ctx)
 
     def set_noise_step(self, step: int):

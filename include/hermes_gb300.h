@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define HERMES_ABI_VERSION 4
+#define HERMES_ABI_VERSION 5
 
 typedef enum hermes_status {
     HERMES_OK = 0,
@@ -218,6 +218,10 @@ typedef struct hermes_launch {
                                 kernel of their own and read by the face kernels (FP64, nbasis 8/10,
                                 no stochastic stress; the default there, the buffer is allocated at
                                 creation); 0: the face kernels evaluate them.  Equal to rounding. */
+    int32_t split_update;    /* 1: the cell update in two kernels, the volume terms (k_cell) and the
+                                surface sums + update (k_update, one thread per cell and variable);
+                                FP64 with ivis 0/1 and no stochastic stress, the default there (the
+                                buffer is allocated at creation); 0: one kernel.  Bit-identical. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
 int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);

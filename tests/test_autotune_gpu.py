@@ -19,13 +19,13 @@ def test_launch_defaults_and_validation():
     from hermeshd_gb300.solver import Solver
     s = Solver(config.sod_1d(nx=64))
     assert s.get_launch() == {"face_tpb": 128, "dt_tpb": 256, "steps_per_graph": 1, "noise_inline": 0,
-                              "face_traces": 0}
+                              "face_traces": 0, "split_update": 1}
     for bad in ({"face_tpb": 96}, {"face_tpb": 256}, {"dt_tpb": 48}, {"dt_tpb": 512}, {"steps_per_graph": 65}):
         with pytest.raises(HermesError):
             s.set_launch(**bad)
     s.set_launch(face_tpb=32, dt_tpb=64, steps_per_graph=4)
     assert s.get_launch() == {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 4, "noise_inline": 0,
-                              "face_traces": 0}
+                              "face_traces": 0, "split_update": 1}
     with pytest.raises(HermesError):   # no trace kernel for nbasis 4
         s.set_launch(face_traces=1)
 
@@ -39,6 +39,8 @@ def test_every_launch_shape_is_bit_identical(mk):
     ref = None
     shapes = [{}, {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 3},
               {"face_tpb": 64, "dt_tpb": 128, "steps_per_graph": 2}]
+    if cfg.precision == "fp64" and not cfg.llns:   # the cell update in one kernel instead of two
+        shapes.append({"split_update": 0})
     if cfg.llns:   # the stochastic stress drawn inside the face and cell kernels instead of staged
         shapes.append({"noise_inline": 1})
     for shape in shapes:
@@ -92,7 +94,8 @@ def test_autotune_resets_state_and_caches(tmp_path, monkeypatch):
         v[0, 4].fill_(1.0 / (base.aindex - 1.0))
     r = autotune.autotune(ens, q, steps=2, repeats=2)
     assert not r["cached"] and r["ms_per_step"] <= r["default_ms_per_step"]
-    assert set(r["launch"]) == {"face_tpb", "dt_tpb", "steps_per_graph", "noise_inline", "face_traces"}
+    assert set(r["launch"]) == {"face_tpb", "dt_tpb", "steps_per_graph", "noise_inline", "face_traces",
+                                "split_update"}
     assert ens.get_launch() == r["launch"]
     # tuning stepped copies of q; the context's time and noise counter are reset
     qa, qa1 = q.clone(), ens.new_state()
