@@ -8,7 +8,10 @@
 //            of prepare_step.f90:20-179 and boundary.f90:40-338 synthesised in place)
 //   k_cell   volume quadrature + surface assembly + sources + forward-Euler
 //            update + RK combination (flux.f90:751-1022, sources.f90:12-84,
-//            integrator.f90:62-252), one write of the stage output
+//            integrator.f90:62-252), one write of the stage output; or, split
+//            (FP64, ivis 0/1), the volume quadrature only, with
+//   k_update the surface assembly, update and RK combination at one thread
+//            per (cell, variable)
 //   k_mindt  CFL time step (hermeshd.f90:145-199), FP64 in every precision
 //
 // Basis and quadrature tables are compile-time constants (dg_tables_gen.cuh)

@@ -21,6 +21,30 @@ def test_header_and_binding_agree():
     assert header_functions() == set(_lib.EXPORTS)
 
 
+def _header_struct_fields(name):
+    src = open(os.path.join(ROOT, "include", "hermes_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"typedef struct " + name + r"\s*\{(.*?)\}\s*" + name + ";", src, flags=re.S).group(1)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if decl:
+            typ, names = decl.split(None, 1)
+            fields += [(n.strip(), typ) for n in names.split(",")]
+    return fields
+
+
+@pytest.mark.parametrize("cname,pycls", [("hermes_launch", "HermesLaunch"), ("hermes_output_units", "HermesOutputUnits")])
+def test_small_structs_match_header(cname, pycls):
+    """Field names and order of the ctypes mirrors of the header's small
+    structs (their sizes are not reported by the library)."""
+    fields = _header_struct_fields(cname)
+    py = getattr(_lib, pycls)._fields_
+    assert [f for f, _ in fields] == [f for f, _ in py]
+    ctype = {"int32_t": C.c_int32, "double": C.c_double}
+    assert [ctype[t] for _, t in fields] == [t for _, t in py]
+
+
 def test_library_exports_every_symbol(hermes_lib):
     for name in _lib.EXPORTS:
         assert hasattr(hermes_lib, name), name
