@@ -18,8 +18,8 @@ include/hermes_gb300.h):
                        exists (FP64, nbasis 8/10, no stochastic stress);
 * ``split_update``     the cell update as the volume kernel plus a surface and
                        update kernel of one thread per (cell, variable) (1) or
-                       one kernel (0); tuned where it exists (FP64, ivis 0/1,
-                       no stochastic stress).
+                       one kernel (0); tuned where it exists (ivis 0/1, no
+                       stochastic stress).
 
 The cell kernel keeps 32 cells per block: its hydro and stress thread groups
 must each fill whole warps, and its register cap is fixed at compile time.

@@ -9,7 +9,7 @@
 //   k_cell   volume quadrature + surface assembly + sources + forward-Euler
 //            update + RK combination (flux.f90:751-1022, sources.f90:12-84,
 //            integrator.f90:62-252), one write of the stage output; or, split
-//            (FP64, ivis 0/1), the volume quadrature only, with
+//            (ivis 0/1, no stochastic stress), the volume quadrature only, with
 //   k_update the surface assembly, update and RK combination at one thread
 //            per (cell, variable)
 //   k_mindt  CFL time step (hermeshd.f90:145-199), FP64 in every precision
@@ -1133,8 +1133,8 @@ struct CellMinBlocks {
 
 // SPLIT: the volume phase only; the volume terms go to a.accbuf and
 // k_update adds the surface sums and does the update, one thread per
-// (cell, variable), so the surface phase runs at full occupancy (ivis 0/1,
-// FP64; the same operations in the same order, so the same bits)
+// (cell, variable), so the surface phase runs at full occupancy (ivis 0/1;
+// the same operations in the same order, so the same bits)
 template <class T, class TB, bool NOISE, bool SPLIT>
 __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value))
     k_cell(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux, CellArgs a) {

@@ -31,9 +31,9 @@ template <class T, int NB, int NQD>
 struct Launch {
     using TB = hermes_tab::Tab<NB, NQD>;
     static size_t cell_smem() { return (size_t)(NB * NQ + 4 * NQ) * CELL_CPB * sizeof(T); }
-    // the split update (k_cell volume phase + k_update) exists for FP64
-    // without the stochastic stress
-    static constexpr bool HAS_SPLIT = std::is_same<T, double>::value;
+    // the split update (k_cell volume phase + k_update) exists without the
+    // stochastic stress
+    static constexpr bool HAS_SPLIT = true;
     template <bool NOISE>
     static cudaError_t prepare_cell() {
         cudaError_t e = cudaFuncSetAttribute(k_cell<T, TB, NOISE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -181,7 +181,7 @@ class Solver:
                    face_traces=None, split_update=None):
         """face_traces / split_update None keep the context's current choice
         (on by default where they exist: the trace kernel for FP64, nbasis
-        8/10, no stochastic stress; the split update for FP64, ivis 0/1, no
+        8/10, no stochastic stress; the split update for ivis 0/1, no
         stochastic stress)."""
         cur = self.get_launch()
         if face_traces is None:
