@@ -402,6 +402,24 @@ __global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__
         }
 }
 
+// the cell pass of one basis; the reverse-sweep and the dual-number (check
+// path) variants are compiled in units of their own (adj_f64_nb*_cell.cu,
+// adj_f64_nb*_dual.cu), the cell kernels being the slowest to compile
+template <int NB, int NQD, bool REV>
+cudaError_t cell_adj_launch(const double* Q, const double* mu, const double* tadj, double* out, const AdjArgs& a,
+                            cudaStream_t s) {
+    using TB = hermes_tab::Tab<NB, NQD>;
+    if (a.G.ncell > 0) {
+        const unsigned nblk = (unsigned)((a.G.ncell + ADJ_TPB - 1) / ADJ_TPB);
+        k_cell_adj<TB, REV><<<nblk, ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);
+    }
+    return cudaGetLastError();
+}
+cudaError_t cell_adj_dual(int nb, const double* Q, const double* mu, const double* tadj, double* out,
+                          const AdjArgs& a, cudaStream_t s);
+cudaError_t cell_adj_rev(int nb, const double* Q, const double* mu, const double* tadj, double* out,
+                         const AdjArgs& a, cudaStream_t s);
+
 // launcher of one basis: the three face-adjoint passes, then the cell pass
 template <int NB, int NQD>
 cudaError_t adj_launch(const double* Q, const double* mu, double* tadj, double* out, const AdjArgs& a, cudaStream_t s) {
@@ -420,12 +438,10 @@ cudaError_t adj_launch(const double* Q, const double* mu, double* tadj, double* 
             else k_face_adj<TB, 2, true><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
         }
     }
-    if (a.G.ncell > 0) {
-        const unsigned nblk = (unsigned)((a.G.ncell + ADJ_TPB - 1) / ADJ_TPB);
-        if (a.dual) k_cell_adj<TB, false><<<nblk, ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);
-        else k_cell_adj<TB, true><<<nblk, ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);
-    }
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (a.dual) return cell_adj_dual(NB, Q, mu, tadj, out, a, s);
+    return cell_adj_rev(NB, Q, mu, tadj, out, a, s);
 }
 
 }  // namespace hermes

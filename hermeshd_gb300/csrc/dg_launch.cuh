@@ -31,13 +31,16 @@ template <class T, int NB, int NQD>
 struct Launch {
     using TB = hermes_tab::Tab<NB, NQD>;
     static size_t cell_smem() { return (size_t)(NB * NQ + 4 * NQ) * CELL_CPB * sizeof(T); }
-    // the split update: k_cell's volume phase + k_update
-    static constexpr bool HAS_SPLIT = true;
+    // the split update (k_cell's volume phase + k_update); with the
+    // stochastic stress only in FP32 (the batched ensemble), which keeps the
+    // FP64 stochastic-stress units' compile time down
+    template <bool NOISE>
+    static constexpr bool has_split() { return !NOISE || std::is_same<T, float>::value; }
     template <bool NOISE>
     static cudaError_t prepare_cell() {
         cudaError_t e = cudaFuncSetAttribute(k_cell<T, TB, NOISE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)cell_smem());
-        if constexpr (HAS_SPLIT) {
+        if constexpr (has_split<NOISE>()) {
             if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(k_cell<T, TB, NOISE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)cell_smem());
@@ -88,7 +91,7 @@ struct Launch {
         const T* q0 = static_cast<const T*>(Q0);
         T* o = static_cast<T*>(out);
         const T* f = static_cast<const T*>(flux);
-        if constexpr (HAS_SPLIT) {
+        if constexpr (has_split<NOISE>()) {
             if (a.accbuf && a.ph.ivis < 2 && !a.split_source) {
                 k_cell<T, TB, NOISE, true><<<nb, 2 * CELL_CPB, cell_smem(), s>>>(qi, q0, o, f, a);
                 const dim3 grid((unsigned)((a.G.ncell + UPD_TPB - 1) / UPD_TPB), NQ);

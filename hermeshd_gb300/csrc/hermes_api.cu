@@ -498,7 +498,7 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
             c->d_noise_cell = c->d_noise_face = nullptr;
         }
     }
-    if (cfg->ivis < 2) {
+    if (cfg->ivis < 2 && (!cfg->llns || c->K.elem_size == (int)sizeof(float))) {
         // split cell update: NQ x nbasis volume terms per cell
         if (cudaMalloc(&c->d_accbuf, (size_t)ncell * NQ * c->K.nb * c->K.elem_size) == cudaSuccess) c->split_update = true;
         else { cudaGetLastError(); c->d_accbuf = nullptr; }   // no room: one kernel

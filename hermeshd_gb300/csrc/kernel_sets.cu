@@ -126,6 +126,28 @@ cudaError_t adj_f64_nb4(const double*, const double*, double*, double*, const Ad
 cudaError_t adj_f64_nb8(const double*, const double*, double*, double*, const AdjArgs&, cudaStream_t);
 cudaError_t adj_f64_nb10(const double*, const double*, double*, double*, const AdjArgs&, cudaStream_t);
 
+cudaError_t cell_adj_dual_nb4(const double*, const double*, const double*, double*, const AdjArgs&, cudaStream_t);
+cudaError_t cell_adj_dual_nb8(const double*, const double*, const double*, double*, const AdjArgs&, cudaStream_t);
+cudaError_t cell_adj_dual_nb10(const double*, const double*, const double*, double*, const AdjArgs&, cudaStream_t);
+
+cudaError_t cell_adj_rev_nb4(const double*, const double*, const double*, double*, const AdjArgs&, cudaStream_t);
+cudaError_t cell_adj_rev_nb8(const double*, const double*, const double*, double*, const AdjArgs&, cudaStream_t);
+cudaError_t cell_adj_rev_nb10(const double*, const double*, const double*, double*, const AdjArgs&, cudaStream_t);
+
+cudaError_t cell_adj_rev(int nb, const double* Q, const double* mu, const double* tadj, double* out,
+                         const AdjArgs& a, cudaStream_t s) {
+    if (nb == 4) return cell_adj_rev_nb4(Q, mu, tadj, out, a, s);
+    if (nb == 8) return cell_adj_rev_nb8(Q, mu, tadj, out, a, s);
+    return cell_adj_rev_nb10(Q, mu, tadj, out, a, s);
+}
+
+cudaError_t cell_adj_dual(int nb, const double* Q, const double* mu, const double* tadj, double* out,
+                          const AdjArgs& a, cudaStream_t s) {
+    if (nb == 4) return cell_adj_dual_nb4(Q, mu, tadj, out, a, s);
+    if (nb == 8) return cell_adj_dual_nb8(Q, mu, tadj, out, a, s);
+    return cell_adj_dual_nb10(Q, mu, tadj, out, a, s);
+}
+
 bool adjoint_launcher(int nb, AdjFn* out) {
     if (nb == 4) *out = &adj_f64_nb4;
     else if (nb == 8) *out = &adj_f64_nb8;
