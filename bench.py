@@ -275,15 +275,18 @@ def run_ours(args, rank, ws):
     per_launch = {"cell": cfg.dof * sbytes, "face_x": cfg.dof * 8.0, "face_y": cfg.dof * 8.0,
                   "face_z": cfg.dof * 8.0, "limiter": cfg.dof * 8.0 * 5 / 11, "cfl_dt": cfg.ncells * 5 * 8.0}
     ach = per_launch[top] / (kern[top]["ms_avg"] * 1e-3) / 1e9
-    # DRAM bytes of one k_cell launch from ncu (256x256: 285 MB read + 95 MB written,
-    # profiles/k_cell_vortex256_f64.txt), scaled by the cell count to this grid;
-    # the excess over the algorithmic bytes is the face-flux intermediate the
-    # cell kernel reads (each face's 9 x 11 fluxes by both its cells) and spills
-    traffic = 380e6 * cfg.ncells / (256 * 256) if top == "cell" else None
+    # DRAM bytes of one one-kernel cell update from ncu (256x256: 285 MB read +
+    # 95 MB written, profiles/k_cell_vortex256_f64.txt), scaled by the cell
+    # count to this grid; the excess over the algorithmic bytes is the face-flux
+    # intermediate the cell kernel reads (each face's 9 x 11 fluxes by both its
+    # cells) and spills.  The split update (the default here) adds the round trip
+    # of the volume terms, nQ x nbasis values per cell written and read once.
+    traffic = (380e6 * cfg.ncells / (256 * 256) + 2.0 * 11 * 10 * 8 * cfg.ncells) if top == "cell" else None
     out["roofline"] = {"bound": "hbm", "kernel": top, "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                        "frac": ach / pk["hbm_gbs"], "peak_source": pk["source"], "traffic": traffic,
-                       "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_cell launch at "
-                                         "256x256, scaled by cells" if traffic else None,
+                       "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one one-kernel cell "
+                                         "update at 256x256, scaled by cells, plus the split update's volume-term "
+                                         "buffer (2 x 11 x 10 x 8 B per cell, counted)" if traffic else None,
                        "algorithmic_bytes_per_launch": per_launch[top], "kernels": kern}
     fl = perfmodel.flops_per_cell_stage(cfg)
     try:
