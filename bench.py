@@ -281,7 +281,7 @@ def run_ours(args, rank, ws):
     # intermediate the cell kernel reads (each face's 9 x 11 fluxes by both its
     # cells) and spills.  The split update (the default here) adds the round trip
     # of the volume terms, nQ x nbasis values per cell written and read once.
-    traffic = (380e6 * cfg.ncells / (256 * 256) + 2.0 * 11 * 10 * 8 * cfg.ncells) if top == "cell" else None
+    traffic = (380e6 * cfg.ncells / (256 * 256) + 2.0 * 11 * cfg.nbasis * 8 * cfg.ncells) if top == "cell" else None
     out["roofline"] = {"bound": "hbm", "kernel": top, "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                        "frac": ach / pk["hbm_gbs"], "peak_source": pk["source"], "traffic": traffic,
                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one one-kernel cell "
