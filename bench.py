@@ -80,13 +80,23 @@ def barrier(ws):
 
 
 def max_over_ranks(x, ws):
+    """The largest of every rank's x (the slowest replica's time): the only
+    collective of a replica run, outside the timed region."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(units_per_rank, elapsed_local, ws):
+    """Whole-job throughput of ws independent replicas: every rank processes
+    units_per_rank units; the job takes as long as its slowest rank."""
+    elapsed = max_over_ranks(elapsed_local, ws)
+    return ws * units_per_rank / elapsed, elapsed
 
 
 class ClockSampler:
@@ -184,6 +194,38 @@ def alu_peaks():
     return out
 
 
+def bench_config(cfg, ws):
+    """The workload description both arms (--impl ours and --impl reference)
+    print, key for key."""
+    return {"workload": WORKLOAD.format(n=cfg.nx), "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "nQ": 11,
+            "nbasis": cfg.nbasis, "dof": cfg.dof, "rk_stages": cfg.stages,
+            "l2": "GPU arm: 256 MiB written to flush L2 before every timed step",
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the one-kernel cell update from an ncu capture: the configuration it was
+# captured on and the bytes (profiles/k_cell_vortex256_f64.txt)
+CELL_CAPTURE = {"nbasis": 10, "precision": "fp64", "cells": 256 * 256, "bytes": 380e6}
+
+
+def cell_traffic(cfg):
+    """DRAM bytes per launch of the cell update: the ncu capture scaled by
+    cells, plus the split update's volume-term round trip (nQ x nbasis values
+    per cell written and read once, counted).  None for a configuration the
+    capture does not describe."""
+    c = CELL_CAPTURE
+    if cfg.nbasis != c["nbasis"] or cfg.precision != c["precision"]:
+        return None, None
+    es = 8 if cfg.precision == "fp64" else 4
+    vol = 2.0 * 11 * cfg.nbasis * es
+    t = c["bytes"] * cfg.ncells / c["cells"] + vol * cfg.ncells
+    return t, (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one one-kernel cell update "
+               f"({c['bytes'] / 1e6:.0f} MB at {c['cells']} cells, nbasis {c['nbasis']}, {c['precision']}), "
+               f"scaled by cells, plus the split update's volume-term buffer "
+               f"(2 x 11 x {cfg.nbasis} x {es} B per cell, counted)")
+
+
 # ---------------------------------------------------------------------------
 def time_steps(solver, q, q1, steps, flush):
     """Per-step device time (s) with CUDA events on the kernels' own stream,
@@ -222,19 +264,16 @@ def run_ours(args, rank, ws):
     barrier(ws)
     with ClockSampler(torch.cuda.current_device()) as clk:
         times = time_steps(s, q, q1, K, flush)
-    elapsed = max_over_ranks(sum(times), ws)
     clocks = clk.summary()
     qg64 = q.clone()          # FP64 state after W + K steps, the reference for the FP32 error
     dof_stage = cfg.dof * cfg.stages
-    value = ws * dof_stage * K / elapsed
+    value, elapsed = replica_throughput(dof_stage * K, sum(times), ws)
     ms_per_step = 1e3 * elapsed / K
     launches_per_step = 2 + 5 * cfg.stages
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD.format(n=cfg.nx), "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "nQ": 11, "nbasis": 10,
-                      "dof": cfg.dof, "rk_stages": cfg.stages, "l2": "flushed: 256 MiB write before every timed step",
-                      "parallelism": "replicas" if ws > 1 else "single GPU", "timing": "CUDA events per step on the kernels' stream"},
+           "config": bench_config(cfg, ws), "timing": "CUDA events per step on the kernels' stream",
            "clocks": clocks, "gpu_launches": launches_per_step * K,
            "autotune": {"launch": tune["launch"], "tuned_ms_per_step": tune["ms_per_step"],
                         "default_ms_per_step": tune["default_ms_per_step"], "trials": len(tune["trials"])}}
@@ -275,18 +314,10 @@ def run_ours(args, rank, ws):
     per_launch = {"cell": cfg.dof * sbytes, "face_x": cfg.dof * 8.0, "face_y": cfg.dof * 8.0,
                   "face_z": cfg.dof * 8.0, "limiter": cfg.dof * 8.0 * 5 / 11, "cfl_dt": cfg.ncells * 5 * 8.0}
     ach = per_launch[top] / (kern[top]["ms_avg"] * 1e-3) / 1e9
-    # DRAM bytes of one one-kernel cell update from ncu (256x256: 285 MB read +
-    # 95 MB written, profiles/k_cell_vortex256_f64.txt), scaled by the cell
-    # count to this grid; the excess over the algorithmic bytes is the face-flux
-    # intermediate the cell kernel reads (each face's 9 x 11 fluxes by both its
-    # cells) and spills.  The split update (the default here) adds the round trip
-    # of the volume terms, nQ x nbasis values per cell written and read once.
-    traffic = (380e6 * cfg.ncells / (256 * 256) + 2.0 * 11 * cfg.nbasis * 8 * cfg.ncells) if top == "cell" else None
+    traffic, traffic_source = cell_traffic(cfg) if top == "cell" else (None, None)
     out["roofline"] = {"bound": "hbm", "kernel": top, "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                        "frac": ach / pk["hbm_gbs"], "peak_source": pk["source"], "traffic": traffic,
-                       "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one one-kernel cell "
-                                         "update at 256x256, scaled by cells, plus the split update's volume-term "
-                                         "buffer (2 x 11 x 10 x 8 B per cell, counted)" if traffic else None,
+                       "traffic_source": traffic_source,
                        "algorithmic_bytes_per_launch": per_launch[top], "kernels": kern}
     fl = perfmodel.flops_per_cell_stage(cfg)
     try:
@@ -666,43 +697,52 @@ def ensemble_accuracy(base, nbox=32, steps=20):
             "density_S_k_fp64": {int(k): v for k, v in sf.result().items()}}
 
 
-def cpu_baseline(cfg, Q0, steps):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+def _time_oracle(cfg, Q0, steps, warmup, timing):
     import oracle as O
     O.set_num_threads(os.cpu_count() or 1)
-    o = O.Oracle(cfg)
+    o = O.Oracle(cfg, timing=timing)
     Q = Q0.copy(order="F")
-    o.advance(Q, 1)
+    o.advance(Q, warmup)
     t0 = time.perf_counter()
     o.advance(Q, steps)
-    el = time.perf_counter() - t0
-    return {"value": cfg.dof * cfg.stages * steps / el, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
-            "sample": f"{steps} SSP-RK3 steps of the same 128x128 vortex, FP64, OpenMP over the oracle's (k,j) loops"}
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(cfg, Q0, steps):
+    """The oracle (the reference's step restated in C, OpenMP over its (k, j)
+    loops) on all host cores: the timing build (host-tuned, FMA contraction),
+    with the parity build's figure beside it."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    el = _time_oracle(cfg, Q0, steps, 1, timing=True)
+    el_parity = _time_oracle(cfg, Q0, steps, 1, timing=False)
+    v = cfg.dof * cfg.stages * steps / el
+    return {"value": v, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": f"{steps} SSP-RK3 steps of the same 128x128 vortex, FP64, OpenMP over the oracle's (k,j) loops",
+            "build": "gcc " + O.timing_flags(),
+            "parity_build": {"value": cfg.dof * cfg.stages * steps / el_parity,
+                             "flags": "gcc -O3 -fopenmp -ffp-contract=off (the checker's build)"}}
 
 
 def run_reference(args, rank, ws):
     """The reference algorithm's CPU implementation (the C restatement of the
     Fortran step; the Fortran itself needs ifort/gfortran, MPI and MKL, none of
-    which exist here) on all host threads, same workload and metric."""
+    which exist here or on the GPU host) on all host threads, same workload
+    and metric, timing build (host-tuned, FMA contraction)."""
     from hermeshd_gb300 import config, ic
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     cfg = config.isentropic_vortex_2d(n=args.n)
     nthreads = os.cpu_count() or 1
-    O.set_num_threads(nthreads)
-    o = O.Oracle(cfg)
-    Q = ic.isentropic_vortex(cfg)
-    o.advance(Q, args.warmup)
-    t0 = time.perf_counter()
-    o.advance(Q, args.steps)
-    el = time.perf_counter() - t0
+    el = _time_oracle(cfg, ic.isentropic_vortex(cfg), args.steps, args.warmup, timing=True)
     v = cfg.dof * cfg.stages * args.steps / el
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD.format(n=cfg.nx), "nx": cfg.nx, "ny": cfg.ny, "nz": cfg.nz, "dof": cfg.dof},
+            "config": bench_config(cfg, ws), "timing": "wall clock around the oracle's advance on the host",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": f"{args.steps} full SSP-RK3 steps after {args.warmup} warm-up steps"},
+                             "sample": f"{args.steps} full SSP-RK3 steps after {args.warmup} warm-up steps",
+                             "build": "gcc " + O.timing_flags()},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

@@ -5,9 +5,10 @@ The values are computed with the same double-precision operations, in the
 same order, as the reference's table setup (basis_funcs.f90:265-627,
 initialize.f90:126-220,350-389), so the face, interior and limiter tables are
 bit-identical to the ones the oracle builds at run time
-(tests/test_tables.py checks this).  Combined tables (volume, surface and
-source quadrature weights) fold the constant factors 0.25*cbasis*w, and are
-used by the kernels with every zero entry skipped at compile time.
+(tests/test_oracle_kat.py::test_generated_tables_bit_identical checks
+this).  Combined tables (volume, surface and source quadrature weights) fold
+the constant factors 0.25*cbasis*w, and are used by the kernels with every
+zero entry skipped at compile time.
 
 Run:  python gen_tables.py  (writes dg_tables_gen.cuh next to this file)
 """

@@ -17,8 +17,16 @@
 // GPU (two streams at once, or two host threads) race; serialise them on one
 // stream.  Every face flux the cell kernel reads is written by the face
 // kernels of the same call, so nothing of the previous call is read; the
-// small records (grid descriptor, error flag, noise counter) are rewritten on
-// every call.
+// small records (grid descriptor, time-step record, error flag, noise
+// counter) are rewritten on every call by k_noalloc_records, a one-thread
+// kernel that receives the grid descriptor as a kernel parameter (by value),
+// so no host memory has to outlive the call.
+//
+// The right-hand side is returned as computed: the reference's NaN check
+// belongs to the update (integrator.f90:234-250), not to the right-hand side,
+// so a non-finite value is not flagged (check the output if needed).  With the
+// stochastic stress on, every call draws the realisation of step 0, stage 0
+// (the Philox counters a fresh context's hermes_rhs uses).
 //
 // Device addresses: in host code g_scratch names a host-side stand-in, not a
 // device address.  The first call on a device, with that device current,
@@ -43,6 +51,17 @@ static __device__ __align__(256) Box g_box;
 static __device__ __align__(16) BoxState g_state;
 static __device__ __align__(16) unsigned long long g_step[2];
 static __device__ __align__(16) int g_flags;
+
+// the per-call records: the grid descriptor (a kernel parameter, so nothing
+// of the host's stack is read after the call returns), a zeroed time-step
+// record and error flag, and the noise counter of step 0
+__global__ void k_noalloc_records(Box b) {
+    g_box = b;
+    g_state = BoxState{0.0, 0.0, 0ull, 0.0};
+    g_step[0] = 0ull;
+    g_step[1] = 0ull;
+    g_flags = 0;
+}
 
 struct DevAddrs {
     bool ready = false;
@@ -159,11 +178,8 @@ extern "C" int hermes_rhs_noalloc(const hermes_config* cfg, void* q, void* rhs, 
     if (e != cudaSuccess) { set_err(err, errlen, cudaGetErrorString(e)); return HERMES_ERR_CUDA; }
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const unsigned long long step0[2] = {0ull, 0ull};
-    e = cudaMemcpyAsync(A->box, &b, sizeof(Box), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(A->step, step0, sizeof(step0), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(A->state, 0, sizeof(BoxState), s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(A->flags, 0, sizeof(int), s);
+    k_noalloc_records<<<1, 1, 0, s>>>(b);
+    e = cudaGetLastError();
     if (e != cudaSuccess) { set_err(err, errlen, cudaGetErrorString(e)); return HERMES_ERR_CUDA; }
 
     Phys ph{};

@@ -17,9 +17,15 @@ Usage mirrors src/test_hermeshd.py:37-83::
 
 Arrays may be numpy Fortran-ordered host arrays (copied to the device and
 back around each call, as the f2py extension works on host memory) or torch
-CUDA tensors of shape (nbasis, nQ, nz, ny, nx) (no copies).  Scalars are 0-d
-numpy arrays mutated in place, as in the reference, and are also returned.
-``comm`` is accepted and ignored (one GPU, no MPI).
+CUDA tensors of shape (nbasis, nQ, nz, ny, nx) (no copies).  As with the
+f2py extension's intent(inout) arguments, nothing is converted: a host array
+must be Fortran-contiguous with the configuration's shape (nx, ny, nz, nQ,
+nbasis) and its element type (float64 for precision 'fp64', float32 for
+'fp32' -- the reference driver's float32 arrays, src/test_hermeshd.py:48-50,
+run on the FP32 path); anything else raises HermesError with
+HERMES_ERR_SHAPE or HERMES_ERR_DTYPE before any work is done.  Scalars are
+0-d numpy arrays mutated in place, as in the reference, and are also
+returned.  ``comm`` is accepted and ignored (one GPU, no MPI).
 """
 from __future__ import annotations
 
@@ -31,8 +37,11 @@ import numpy as np
 from . import checkpoint as _ckpt
 from . import ic as _ic
 from . import output as _out
+from ._lib import HermesError
 from .config import Config
 from .solver import Solver
+
+_ERR_SHAPE, _ERR_DTYPE = 2, 3   # HERMES_ERR_SHAPE, HERMES_ERR_DTYPE (include/hermes_gb300.h)
 
 
 def _set0d(a, v):
@@ -79,6 +88,25 @@ class Hermeshd:
             self.solver.close()
             self.solver = None
 
+    def _check(self, a, name):
+        """The f2py contract of an intent(inout) field array: a host array is
+        used as given or rejected, never converted.  Device tensors are
+        checked by the Solver (dtype, shape, contiguity, device)."""
+        if a is None or not isinstance(a, np.ndarray):
+            return
+        cfg = self.cfg
+        want = self._host_dtype()
+        if a.dtype != want:
+            raise HermesError(_ERR_DTYPE, f"{name}: dtype {a.dtype} does not match precision {cfg.precision} "
+                                          f"(expected {np.dtype(want).name})")
+        if tuple(a.shape) != tuple(cfg.shape_f):
+            raise HermesError(_ERR_SHAPE, f"{name}: shape {tuple(a.shape)}, expected {tuple(cfg.shape_f)}")
+        if not a.flags.f_contiguous:
+            raise HermesError(_ERR_SHAPE, f"{name}: not Fortran-contiguous")
+
+    def _host_dtype(self):
+        return np.float64 if self.cfg.precision == "fp64" else np.float32
+
     def _need(self):
         if self.cfg is None:
             raise RuntimeError("hermeshd: configure(cfg) before setup (the reference fixes it at compile time)")
@@ -90,7 +118,7 @@ class Hermeshd:
     def main(self, comm=0):
         """hermeshd.f90:26-48: setup; while t < tf: step, generate_output; cleanup."""
         cfg = self.cfg
-        Q = np.zeros(cfg.shape_f, order="F", dtype=np.float64)
+        Q = np.zeros(cfg.shape_f, order="F", dtype=self._host_dtype())
         Q1, Q2 = np.zeros_like(Q), np.zeros_like(Q)
         t, dt, t1, t_start, dtout, nout = (np.array(0.0), np.array(0.0), np.array(0.0), np.array(0.0),
                                             np.array(0.0), np.array(0))
@@ -105,6 +133,8 @@ class Hermeshd:
         """hermeshd.f90:67-114: initializer (tables, spacing, dt), initial
         condition into q_io, integrator and boundary selection.  As set_ic
         does (initialcon.f90:29-32), ivis 0 zeroes coll and colvis."""
+        if self.cfg is not None:
+            self._check(q_io, "q_io")
         if self.cfg is not None and not self.iread and self.cfg.ivis == 0 and (self.cfg.coll or self.cfg.colvis):
             self.cfg = self.cfg.replace(coll=0.0, colvis=0.0)
             if self.solver is not None:
@@ -146,13 +176,17 @@ class Hermeshd:
 
     def step(self, q_io, q_1, q_2, t, dt):
         """hermeshd.f90:53-62: dt = get_min_dt(Q); update(Q, Q1, Q2, dt); t += dt."""
+        if self.cfg is not None:
+            for a, name in ((q_io, "q_io"), (q_1, "q_1"), (q_2, "q_2")):
+                self._check(a, name)
         s = self._need()
         if isinstance(q_io, np.ndarray):
-            # host arrays: copy in, step, copy back (Q_1 returned as well)
+            # host arrays: copy in, step, copy back (Q_1 returned as well),
+            # in the arrays' own element type
             dq, d1 = s.from_numpy(q_io), s.from_numpy(q_1)
             tn, dtn = s.step(dq, d1, None, _get0d(t))
-            q_io[...] = s.to_numpy(dq)
-            q_1[...] = s.to_numpy(d1)
+            q_io[...] = dq.cpu().numpy().T
+            q_1[...] = d1.cpu().numpy().T
         else:
             tn, dtn = s.step(q_io, q_1, q_2, _get0d(t))
         _set0d(t, tn)
@@ -164,6 +198,8 @@ class Hermeshd:
         nout, write the VTK derived fields (output_vtk) when vtk is set and,
         with iwrite, the checkpoint with the odd/even dump id
         (hermeshd.f90:248-252)."""
+        if self.cfg is not None:
+            self._check(q_r, "q_r")
         if _get0d(t) > _get0d(nout) * _get0d(dtout):
             n = int(_get0d(nout)) + 1
             _set0d(nout, n)

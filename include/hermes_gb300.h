@@ -265,7 +265,12 @@ int hermes_check(hermes_ctx *ctx);
  * HERMES_ERR_SHAPE.  All calls share that array: calls that overlap on the GPU
  * race.  The first call on a device looks up the array's device address and
  * should come before any stream capture.  err (errlen bytes, may be NULL)
- * receives a message on failure. */
+ * receives a message on failure.  The right-hand side is returned as
+ * computed: a non-finite value in it is not reported (the reference checks
+ * for NaN in the update, integrator.f90:234-250, not in the right-hand side).
+ * With the stochastic stress on (cfg->llns), every call draws the same
+ * realisation, the one of step 0, stage 0 (what hermes_rhs draws on a fresh
+ * context). */
 #define HERMES_NOALLOC_SCRATCH_BYTES (64ull << 20)
 int hermes_rhs_noalloc(const hermes_config *cfg, void *q, void *rhs, int apply_limiter, void *stream, char *err,
                        size_t errlen);

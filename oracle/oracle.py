@@ -19,6 +19,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "build", "libhermes_oracle.so")
+# the same source built for timing only (host-tuned, FMA contraction on):
+# the CPU baseline's clock, never the checker (its roundings differ)
+LIB_TIMING = os.path.join(HERE, "build", "libhermes_oracle_timing.so")
 
 
 class OrcParams(C.Structure):
@@ -39,21 +42,29 @@ class OrcParams(C.Structure):
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (gcc, OpenMP)."""
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
-            os.path.getmtime(os.path.join(HERE, f)) for f in ("hermes_oracle.c", "hermes_oracle.h", "philox_ref.h")):
-        subprocess.check_call(["make", "-s", "-C", HERE])
+    """Compile the oracle's parity and timing builds with its Makefile (gcc, OpenMP)."""
+    src = max(os.path.getmtime(os.path.join(HERE, f)) for f in ("hermes_oracle.c", "hermes_oracle.h", "philox_ref.h",
+                                                                  "Makefile"))
+    if force or any(not os.path.exists(p) or os.path.getmtime(p) < src for p in (LIB, LIB_TIMING)):
+        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
     return LIB
 
 
-_lib = None
+def timing_flags() -> str:
+    """The compiler flags of the timing build on this host."""
+    return subprocess.run(["make", "-s", "-C", HERE, "timing_flags"], capture_output=True, text=True).stdout.strip()
 
 
-def lib():
-    global _lib
-    if _lib is None:
+_libs = {}
+
+
+def lib(timing: bool = False):
+    """The parity build (the checker), or with timing=True the host-tuned
+    build that bench.py times as the CPU baseline."""
+    L = _libs.get(timing)
+    if L is None:
         build()
-        L = C.CDLL(LIB)
+        L = C.CDLL(LIB_TIMING if timing else LIB)
         dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="F_CONTIGUOUS")
         L.orc_create.restype = C.c_void_p
         L.orc_create.argtypes = [C.POINTER(OrcParams)]
@@ -88,8 +99,8 @@ def lib():
         L.orc_philox4x32_10.argtypes = [u32p, C.c_uint32, C.c_uint32, u32p]
         L.orc_test_basis.restype = C.c_double
         L.orc_test_basis.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
-        _lib = L
-    return _lib
+        _libs[timing] = L
+    return L
 
 
 def params_from_config(cfg) -> OrcParams:
@@ -111,12 +122,13 @@ def params_from_config(cfg) -> OrcParams:
 
 
 class Oracle:
-    """One oracle context for one Config."""
+    """One oracle context for one Config (timing=True: the host-tuned build,
+    for the CPU baseline's clock only)."""
 
-    def __init__(self, cfg):
+    def __init__(self, cfg, timing: bool = False):
         cfg.validate(oracle=True)
         self.cfg = cfg
-        self.L = lib()
+        self.L = lib(timing)
         self._p = params_from_config(cfg)
         self.h = self.L.orc_create(C.byref(self._p))
         if not self.h:
