@@ -370,64 +370,54 @@ def variants(args, cfg64, Q0, qg64, flush, dev, ws, value64):
                    "hbm": hbm_share(v32, "fp32", c32.iorder)}
     s.close()
 
-    # FP32 batched ensemble vs the plain FP64 path on one box of the same physics
-    rng = np.random.default_rng(0)
-    sizes = rng.choice([16, 24, 32, 48], size=256)
-    dims = [(int(n), int(n), int(n)) for n in sizes]
-    base = config.fh_box(48, precision="fp32", seed=0)
-    dx = base.lx / 48
-    lengths = [(n * dx, n * dx, n * dx) for (n, _, _) in dims]
-    ens = Ensemble(base, dims, lengths, seeds=list(range(256)))
-    qe, qe1 = ens.new_state(), ens.new_state()
-    # equilibrium rho = 1, T = 1, v = 0 in every box, set on the device
-    for i in range(ens.nbox):
-        v = ens.box_view(qe, i)
-        v.zero_()
-        v[0, 0].fill_(1.0)
-        v[0, 4].fill_(1.0 / (base.aindex - 1.0))
-    ens.advance(qe, qe1, 2)
-    etune = autotune.autotune(ens, qe, steps=1, repeats=2, use_cache=False)
-    Ke = max(2, K // 5)
-    times = time_steps(ens, qe, qe1, Ke, flush)
-    el = max_over_ranks(sum(times), ws)
-    dof = ens.dof
-    vens = ws * dof * base.stages * Ke / el
-    res["fp32_batched_ensemble"] = {
-        "value": vens, "unit": UNIT, "ms_per_step": 1e3 * el / Ke, "steps": Ke, "dtype": "f32",
-        "config": {"boxes": 256, "sizes": "uniform from {16,24,32,48}^3, seed 0", "cells": ens.ncells, "dof": dof,
-                   "nbasis": 4, "ivis": 1, "stochastic_stress": True, "rk": "SSP-RK2", "riemann": "Roe (ihllc 2)",
-                   "noise": "kT/(rho dV) = 1e-3, eta = 1, Philox key = realisation id"},
-        "autotune": {"launch": etune["launch"], "tuned_ms_per_step": etune["ms_per_step"],
-                     "default_ms_per_step": etune["default_ms_per_step"]}}
-    ens.close()
-    del qe, qe1
-    torch.cuda.empty_cache()
-    # plain FP64 on one 48^3 box of the same physics
-    c64 = config.fh_box(48, precision="fp64", seed=0)
-    s = Solver(c64)
-    q = s.from_numpy(ic.equilibrium(c64))
-    q1 = s.new_state()
-    s.advance(q, q1, 2)
-    times = time_steps(s, q, q1, Ke, flush)
-    el = max_over_ranks(sum(times), ws)
-    v64 = ws * c64.dof * c64.stages * Ke / el
-    res["fp64_plain_fh_box48"] = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * el / Ke, "dtype": "f64",
-                                  "hbm": hbm_share(v64, "fp64", c64.iorder)}
-    res["fp32_batched_ensemble"]["speedup_vs_fp64_plain"] = vens / v64
-    res["fp32_batched_ensemble"]["hbm"] = hbm_share(vens, "fp32", base.iorder)
-    s.close()
-    res["fp32_batched_ensemble"]["accuracy"] = ensemble_accuracy(base)
-    hl = ensemble_accuracy(base.replace(ihllc=1), nbox=16, steps=20)
-    res["fp32_batched_ensemble"]["accuracy_with_hllc"] = {
-        "max_rel_l2": hl["max_rel_l2"],
-        "note": "HLLC with the stress-augmented point flux is discontinuous at S_M = 0, where an equilibrium "
-                "fluctuating state sits at every face; FP32 and FP64 then pick branches by rounding"}
+    # FP32 batched ensemble against the FP64 batched ensemble of the same 256
+    # boxes (and the plain FP64 path on one 48^3 box), with and without the
+    # stochastic stress; its accuracy on the same draw, Roe and HLLC
+    res.update(ensembles(args, flush, ws))
+    res["vortex_one_period"] = vortex_one_period(cfg64)
     res["adjoint_poiseuille"] = adjoint_poiseuille()
     res["tgv64"] = tgv64()
     res["sod256"] = sod256()
     res["derived_fields"] = derived_fields(cfg64, Q0, flush)
     res["checkpoint_io"] = checkpoint_io(cfg64, Q0)
     return res
+
+
+def vortex_one_period(cfg, T=10.0):
+    """The headline vortex advected for one period (t >= 10, the mean flow
+    (1, 1) crosses the 10 x 10 box once), FP64 and FP32: the relative L2 and
+    largest error of the cell-average density against the exactly advected
+    solution averaged over each cell (5 x 5 Gauss points,
+    initialcon.f90:158-177), beside the same error of the initial state (the
+    reference's initial condition samples the cell centres, so its own
+    deviation from the exact averages is the floor)."""
+    import numpy as np
+
+    from hermeshd_gb300 import ic
+    from hermeshd_gb300.solver import Solver
+
+    Q0 = ic.isentropic_vortex(cfg)
+    ex0 = ic.isentropic_vortex_exact(cfg, 0.0, quad=5)[:, :, 0]
+    r0 = Q0[:, :, 0, 0, 0]
+    out = {"t_target": T, "initial_state": {"rel_l2": float(np.linalg.norm(r0 - ex0) / np.linalg.norm(ex0)),
+                                            "max_abs": float(np.abs(r0 - ex0).max())}}
+    for prec in ("fp64", "fp32"):
+        c = cfg.replace(precision=prec)
+        s = Solver(c)
+        q, q1 = s.from_numpy(Q0), s.new_state()
+        t, n = 0.0, 0
+        while t < T:
+            k = 100 if t < T - 0.5 else 1
+            t, _ = s.advance(q, q1, k, t=t)
+            n += k
+        rho = s.to_numpy(q)[:, :, 0, 0, 0]
+        s.close()
+        ex = ic.isentropic_vortex_exact(cfg, t, quad=5)[:, :, 0]
+        out[prec] = {"steps": n, "t_end": t, "rel_l2": float(np.linalg.norm(rho - ex) / np.linalg.norm(ex)),
+                     "max_abs": float(np.abs(rho - ex).max())}
+    out["definition"] = ("cell-average density (coefficient 1 of rho) against the exact solution at t_end "
+                         "averaged over each cell; relative L2 over the grid")
+    return out
 
 
 def adjoint_poiseuille(nsteps=200, every=20):
@@ -487,7 +477,7 @@ def adjoint_poiseuille(nsteps=200, every=20):
             "limiter_events": roll.limiter_events}
 
 
-def tgv64(nsteps=200):
+def tgv64(nsteps=200, oracle_steps=20):
     """The 3-D Taylor-Green vortex, 10-moment ivis 1, 64^3, nb 4, RK3, Mach
     0.1, Re 400 (symmetry broken by 1e-3, seed 1): 200 steps in FP64 and in
     FP32 (FP64 CFL, limiter fixes and conservation sums), device time of the
@@ -527,7 +517,38 @@ def tgv64(nsteps=200):
     out["fp32"]["rel_l2_vs_fp64"] = float((states["fp32"] - states["fp64"]).norm() / states["fp64"].norm())
     out["fp32"]["speedup_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
     out["config"] = {"grid": "64^3", "nbasis": 4, "ivis": 1, "riemann": "HLLC", "rk": "SSP-RK3", "steps": nsteps}
+    out["vs_fp64_oracle"] = tgv_vs_oracle(oracle_steps)
     return out
+
+
+def tgv_vs_oracle(steps):
+    """FP64 and FP32 Taylor-Green 64^3 states after `steps` steps against the
+    FP64 oracle's (all host cores) from the same initial state."""
+    import numpy as np
+
+    from hermeshd_gb300 import config, ic
+    from hermeshd_gb300.solver import Solver
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cfg = config.taylor_green_3d(n=64, precision="fp64")
+    Q0 = ic.taylor_green(cfg, perturb=1e-3, seed=1)
+    O.set_num_threads(os.cpu_count() or 1)
+    Qo = Q0.copy(order="F")
+    t0 = time.perf_counter()
+    to, _ = O.Oracle(cfg).advance(Qo, steps)
+    oracle_s = time.perf_counter() - t0
+    res = {"steps": steps, "oracle_wall_s": oracle_s}
+    for prec in ("fp64", "fp32"):
+        s = Solver(cfg.replace(precision=prec))
+        q, q1 = s.from_numpy(Q0), s.new_state()
+        t, _ = s.advance(q, q1, steps)
+        g = s.to_numpy(q)
+        s.close()
+        res[prec] = {"rel_l2": float(np.linalg.norm(g - Qo) / np.linalg.norm(Qo)), "t_rel_diff": abs(t - to) / to}
+    res["note"] = (f"the oracle's {steps} steps of 64^3 take about {oracle_s:.0f} s on the host cores; its 200 "
+                   "are left to the FP64 GPU state, which holds the oracle to rounding")
+    return res
 
 
 def sod256():
@@ -654,34 +675,72 @@ def checkpoint_io(cfg, Q0, reps=3):
             "round_trip_bit_exact": exact, "host_threads": os.cpu_count()}
 
 
-def ensemble_accuracy(base, nbox=32, steps=20):
-    """Relative L2 error of the ensemble-averaged density field of the FP32
-    batched run against the same ensemble in FP64 (same seeds, same steps),
-    per box size, and the density S(k) of the FP64 run."""
+ENS_BOXES, ENS_SIZES = 256, (16, 24, 32, 48)
+
+
+def ensemble_draw(nbox=ENS_BOXES, seed=0):
+    """Box extents of the fluctuating-hydro ensemble: nbox cubes with edges
+    drawn uniformly from {16, 24, 32, 48} (numpy default_rng(seed)), all with
+    the 48^3 box's cell size; Philox key = realisation id."""
     import numpy as np
-    import torch
+    sizes = np.random.default_rng(seed).choice(ENS_SIZES, size=nbox)
+    return [(int(n),) * 3 for n in sizes]
 
-    from hermeshd_gb300.analysis import StructureFactor
+
+def make_ensemble(base, dims):
     from hermeshd_gb300.solver import Ensemble
-
-    rng = np.random.default_rng(1)
-    sizes = rng.choice([16, 24, 32, 48], size=nbox)
-    dims = [(int(n), int(n), int(n)) for n in sizes]
     dx = base.lx / 48
-    lengths = [(n * dx, n * dx, n * dx) for (n, _, _) in dims]
+    ens = Ensemble(base, dims, [(d[0] * dx, d[1] * dx, d[2] * dx) for d in dims], seeds=list(range(len(dims))))
+    q, q1 = ens.new_state(), ens.new_state()
+    equilibrate(ens, q)
+    return ens, q, q1
+
+
+def equilibrate(ens, q):
+    """rho = 1, T = 1 (p = 1), v = 0 in every box; time and noise counter 0."""
+    for i in range(ens.nbox):
+        v = ens.box_view(q, i)
+        v.zero_()
+        v[0, 0].fill_(1.0)
+        v[0, 4].fill_(1.0 / (ens.cfg.aindex - 1.0))
+    ens.set_time(0.0)
+    ens.set_noise_step(0)
+
+
+def time_ensemble(base, dims, K, flush, ws, tune=True):
+    """Device time of K steps of the batched ensemble (after 2 warm-up steps
+    and, with tune, the autotuner), CUDA events per step, L2 flushed."""
+    from hermeshd_gb300 import autotune
+    ens, q, q1 = make_ensemble(base, dims)
+    ens.advance(q, q1, 2)
+    tune_res = autotune.autotune(ens, q, steps=1, repeats=2, use_cache=False) if tune else None
+    times = time_steps(ens, q, q1, K, flush)
+    v, el = replica_throughput(ens.dof * base.stages * K, sum(times), ws)
+    out = {"value": v, "unit": UNIT, "ms_per_step": 1e3 * el / K, "steps": K,
+           "dtype": "f32" if base.precision == "fp32" else "f64",
+           "hbm": hbm_share(v, base.precision, base.iorder)}
+    if tune_res:
+        out["autotune"] = {"launch": tune_res["launch"], "tuned_ms_per_step": tune_res["ms_per_step"],
+                           "default_ms_per_step": tune_res["default_ms_per_step"]}
+    cells, dof = ens.ncells, ens.dof
+    ens.close()
+    return out, cells, dof
+
+
+def ensemble_accuracy(base, dims, steps):
+    """Relative L2 error of the ensemble-averaged density field of the FP32
+    batched run against the same ensemble in FP64 (same draw, seeds and
+    steps from the same equilibrium), per box size; and the density S(k) of
+    the FP64 run."""
+    import torch
+    from hermeshd_gb300.analysis import StructureFactor
     states = {}
     for prec in ("fp32", "fp64"):
-        ens = Ensemble(base.replace(precision=prec), dims, lengths, seeds=list(range(nbox)))
-        q, q1 = ens.new_state(), ens.new_state()
-        for i in range(nbox):
-            v = ens.box_view(q, i)
-            v.zero_()
-            v[0, 0].fill_(1.0)
-            v[0, 4].fill_(1.0 / (base.aindex - 1.0))
+        ens, q, q1 = make_ensemble(base.replace(precision=prec), dims)
         ens.advance(q, q1, steps)
         states[prec] = (ens, q)
     err = {}
-    sf = StructureFactor(kmax=8)
+    sizes = [d[0] for d in dims]
     e32, q32 = states["fp32"]
     e64, q64 = states["fp64"]
     for n in sorted(set(sizes)):
@@ -689,12 +748,61 @@ def ensemble_accuracy(base, nbox=32, steps=20):
         a32 = torch.stack([e32.box_view(q32, i)[0, 0].double() for i in idx]).mean(0)
         a64 = torch.stack([e64.box_view(q64, i)[0, 0] for i in idx]).mean(0)
         err[int(n)] = float((a32 - a64).norm() / a64.norm())
+    sf = StructureFactor(kmax=8)
     sf.add_state(q64, base.nbasis, dims, e64.offsets)
     e32.close()
     e64.close()
-    return {"boxes": nbox, "steps": steps, "rel_l2_ensemble_mean_density_vs_fp64": err,
-            "max_rel_l2": max(err.values()),
-            "density_S_k_fp64": {int(k): v for k, v in sf.result().items()}}
+    del states, q32, q64
+    torch.cuda.empty_cache()
+    return {"boxes": len(dims), "steps": steps, "rel_l2_ensemble_mean_density_vs_fp64": err,
+            "max_rel_l2": max(err.values()), "density_S_k_fp64": {int(k): v for k, v in sf.result().items()}}
+
+
+def ensembles(args, flush, ws, acc_steps=100):
+    """The batched fluctuating-hydro ensemble (256 periodic boxes, 10-moment
+    ivis 1 + stochastic stress, nb 4, SSP-RK2, Roe): FP32 batched against the
+    FP64 batched ensemble of the same draw and against the plain FP64 path on
+    one 48^3 box, with and without the stochastic stress; then the accuracy
+    of the FP32 ensemble means against FP64 on the same 256-box draw over
+    acc_steps of the configuration's 500 steps, with Roe and with the
+    reference's HLLC."""
+    import torch
+    from hermeshd_gb300 import config, ic
+    from hermeshd_gb300.solver import Solver
+    K = max(2, args.steps // 5)
+    dims = ensemble_draw()
+    out = {}
+    for llns, tag in ((True, ""), (False, "_no_noise")):
+        b32 = config.fh_box(48, precision="fp32", seed=0, llns=llns)
+        r32, cells, dof = time_ensemble(b32, dims, K, flush, ws)
+        r64, _, _ = time_ensemble(b32.replace(precision="fp64"), dims, K, flush, ws)
+        # plain FP64 on one 48^3 box of the same physics
+        c64 = config.fh_box(48, precision="fp64", seed=0, llns=llns)
+        s = Solver(c64)
+        q = s.from_numpy(ic.equilibrium(c64))
+        q1 = s.new_state()
+        s.advance(q, q1, 2)
+        times = time_steps(s, q, q1, K, flush)
+        v1, el = replica_throughput(c64.dof * c64.stages * K, sum(times), ws)
+        s.close()
+        r32["config"] = {"boxes": len(dims), "sizes": "uniform from {16,24,32,48}^3, seed 0", "cells": cells,
+                         "dof": dof, "nbasis": 4, "ivis": 1, "stochastic_stress": llns, "rk": "SSP-RK2",
+                         "riemann": "Roe (ihllc 2)", "noise": "kT/(rho dV) = 1e-3, eta = 1, Philox key = realisation id"}
+        r32["fp64_batched"] = r64
+        r32["speedup_vs_fp64_batched"] = r32["value"] / r64["value"]
+        r32["fp64_plain_box48"] = {"value": v1, "unit": UNIT, "ms_per_step": 1e3 * el / K,
+                                   "hbm": hbm_share(v1, "fp64", c64.iorder)}
+        r32["speedup_vs_fp64_plain_box48"] = r32["value"] / v1
+        out["fp32_batched_ensemble" + tag] = r32
+        torch.cuda.empty_cache()
+    base = config.fh_box(48, precision="fp32", seed=0)
+    out["fp32_batched_ensemble"]["accuracy"] = {
+        "roe": ensemble_accuracy(base, dims, acc_steps),
+        "hllc": ensemble_accuracy(base.replace(ihllc=1), dims, acc_steps),
+        "note": "the reference's HLLC with the stress-augmented point flux is discontinuous at S_M = 0, where an "
+                "equilibrium fluctuating state sits at every face, so FP32 and FP64 runs pick its branches by "
+                "rounding; the Roe solver is continuous there"}
+    return out
 
 
 def _time_oracle(cfg, Q0, steps, warmup, timing):

@@ -32,10 +32,11 @@ struct Launch {
     using TB = hermes_tab::Tab<NB, NQD>;
     static size_t cell_smem() { return (size_t)(NB * NQ + 4 * NQ) * CELL_CPB * sizeof(T); }
     // the split update (k_cell's volume phase + k_update); with the
-    // stochastic stress only in FP32 (the batched ensemble), which keeps the
-    // FP64 stochastic-stress units' compile time down
+    // stochastic stress in FP32 and, in FP64, for nbasis 4 (the basis of the
+    // fluctuating-hydro ensemble), which keeps the compile time of the other
+    // FP64 stochastic-stress units down
     template <bool NOISE>
-    static constexpr bool has_split() { return !NOISE || std::is_same<T, float>::value; }
+    static constexpr bool has_split() { return !NOISE || std::is_same<T, float>::value || NB == 4; }
     template <bool NOISE>
     static cudaError_t prepare_cell() {
         cudaError_t e = cudaFuncSetAttribute(k_cell<T, TB, NOISE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,

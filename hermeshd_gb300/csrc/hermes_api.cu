@@ -498,7 +498,7 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
             c->d_noise_cell = c->d_noise_face = nullptr;
         }
     }
-    if (cfg->ivis < 2 && (!cfg->llns || c->K.elem_size == (int)sizeof(float))) {
+    if (cfg->ivis < 2 && (!cfg->llns || c->K.elem_size == (int)sizeof(float) || cfg->nbasis == 4)) {
         // split cell update: NQ x nbasis volume terms per cell
         if (cudaMalloc(&c->d_accbuf, (size_t)ncell * NQ * c->K.nb * c->K.elem_size) == cudaSuccess) c->split_update = true;
         else { cudaGetLastError(); c->d_accbuf = nullptr; }   // no room: one kernel
@@ -806,7 +806,8 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     const bool traces = l->face_traces == 1;
     if (l->split_update != 0 && l->split_update != 1) return fail(c, HERMES_ERR_ARG, "split_update must be 0 or 1");
     if (l->split_update == 1 && !c->d_accbuf)
-        return fail(c, HERMES_ERR_ARG, "the split update needs FP64, ivis 0/1, no stochastic stress and room for the buffer");
+        return fail(c, HERMES_ERR_ARG, "the split update needs ivis 0/1, room for the buffer and, with the stochastic "
+                                       "stress in FP64, nbasis 4");
     const bool split = l->split_update == 1;
     if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged || traces != c->face_traces ||
         split != c->split_update) {

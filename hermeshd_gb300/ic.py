@@ -91,18 +91,29 @@ def isentropic_vortex(cfg: Config, ver: int = 1, beta: float = 5.0) -> np.ndarra
     return Q
 
 
-def isentropic_vortex_exact(cfg: Config, t: float, ver: int = 1, beta: float = 5.0) -> np.ndarray:
-    """Cell-average density of the exactly advected vortex at time t (the IC
-    shifted by the mean flow, periodically wrapped), sampled at cell centres."""
+def isentropic_vortex_exact(cfg: Config, t: float, ver: int = 1, beta: float = 5.0, quad: int = 1) -> np.ndarray:
+    """Density of the exactly advected vortex at time t (the IC shifted by the
+    mean flow, periodically wrapped, initialcon.f90:158-177): sampled at the
+    cell centres (quad = 1) or averaged over each cell by a quad x quad
+    Gauss-Legendre rule (quad > 1), shape (nx, ny, nz)."""
     vx_amb, vy_amb, Rgsqi = (1.0, 0.0, 1.0) if ver == 0 else (1.0, 1.0, 0.5)
     g = cfg.aindex
     xc, yc, zc = cell_centres(cfg)
-    X, Y = np.meshgrid(xc, yc, indexing="ij")
-    Xs = (X - vx_amb * t + cfg.lx / 2) % cfg.lx - cfg.lx / 2
-    Ys = (Y - vy_amb * t + cfg.ly / 2) % cfg.ly - cfg.ly / 2
-    r2 = Xs ** 2 + Ys ** 2
-    dT = -((g - 1) * beta ** 2) / (16 * Rgsqi * g * math.pi ** 2) * np.exp(2 * Rgsqi * (1 - r2))
-    return (1.0 + dT) ** (1.0 / (g - 1))
+    dx, dy = cfg.lx / cfg.nx, cfg.ly / cfg.ny
+    if quad > 1:
+        pts, wts = np.polynomial.legendre.leggauss(quad)
+    else:
+        pts, wts = np.zeros(1), np.full(1, 2.0)
+    out = np.zeros((cfg.nx, cfg.ny))
+    for a, wa in zip(pts, wts):
+        for b, wb in zip(pts, wts):
+            X, Y = np.meshgrid(xc + 0.5 * dx * a, yc + 0.5 * dy * b, indexing="ij")
+            Xs = (X - vx_amb * t + cfg.lx / 2) % cfg.lx - cfg.lx / 2
+            Ys = (Y - vy_amb * t + cfg.ly / 2) % cfg.ly - cfg.ly / 2
+            r2 = Xs ** 2 + Ys ** 2
+            dT = -((g - 1) * beta ** 2) / (16 * Rgsqi * g * math.pi ** 2) * np.exp(2 * Rgsqi * (1 - r2))
+            out += 0.25 * wa * wb * (1.0 + dT) ** (1.0 / (g - 1))
+    return np.broadcast_to(out[:, :, None], (cfg.nx, cfg.ny, cfg.nz)).copy()
 
 
 def taylor_green(cfg: Config, rho: float = 1.0, V0: float = 1.0, perturb: float = 0.0, seed: int = 0) -> np.ndarray:

@@ -220,8 +220,9 @@ typedef struct hermes_launch {
                                 creation); 0: the face kernels evaluate them.  Equal to rounding. */
     int32_t split_update;    /* 1: the cell update in two kernels, the volume terms (k_cell) and the
                                 surface sums + update (k_update, one thread per cell and variable);
-                                ivis 0/1 (FP64 without the stochastic stress), the default there
-                                (the buffer is allocated at creation); 0: one kernel.
+                                ivis 0/1 without the stochastic stress, and with it in FP32 and in
+                                FP64 for nbasis 4; the default there (the buffer is allocated at
+                                creation); 0: one kernel.
                                 Bit-identical. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);

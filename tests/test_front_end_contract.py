@@ -58,7 +58,8 @@ def test_shape_and_order_mismatch_are_rejected():
 def test_reference_driver_loop_with_float32_arrays():
     """src/test_hermeshd.py:44-83 as written: float32 Fortran arrays (nx 50,
     nQ 11, nB 8), 0-d float64 scalars mutated in place, setup / step /
-    generate_output until t >= tf = 7e-4, cleanup.  The FP32 state is held
+    generate_output until t >= tf = 7e-4 (one CFL step of this grid), then 9
+    more steps through the same calls, cleanup.  The FP32 state is held
     against the FP64 oracle over the same steps (FP32 bound 1e-5)."""
     import oracle as O
     cfg = config.sod_1d(nx=50, nbasis=8, iquad=2, precision="fp32")
@@ -73,12 +74,20 @@ def test_reference_driver_loop_with_float32_arrays():
     o = O.Oracle(cfg.replace(precision="fp64"))
     Qo = ic.sod(cfg)
     to, n = 0.0, 0
-    while t < tf:
+
+    def one():
+        nonlocal to, n
         m.step(Qio, Q1, Q2, t, dt)
         m.generate_output(Qio, t, dt, t1, dtout, nout)
         to, _ = o.step(Qo, o.new(), o.new(), to, 0.0)
         n += 1
+
+    while t < tf:
+        one()
+    assert n >= 1 and float(t) >= 7.0e-4
+    for _ in range(9):
+        one()
     m.cleanup(t_start)
-    assert n >= 3 and Qio.dtype == np.float32
+    assert Qio.dtype == np.float32 and Q1.dtype == np.float32
     assert abs(float(t) - to) <= 1e-5 * to
     assert rel_l2(Qio, Qo) < 1e-5
