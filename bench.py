@@ -397,7 +397,7 @@ def vortex_one_period(cfg, T=10.0):
     from hermeshd_gb300.solver import Solver
 
     Q0 = ic.isentropic_vortex(cfg)
-    ex0 = ic.isentropic_vortex_exact(cfg, 0.0, quad=5)[:, :, 0]
+    ex0 = ic.isentropic_vortex_exact(cfg, 0.0, quad=5)
     r0 = Q0[:, :, 0, 0, 0]
     out = {"t_target": T, "initial_state": {"rel_l2": float(np.linalg.norm(r0 - ex0) / np.linalg.norm(ex0)),
                                             "max_abs": float(np.abs(r0 - ex0).max())}}
@@ -412,7 +412,7 @@ def vortex_one_period(cfg, T=10.0):
             n += k
         rho = s.to_numpy(q)[:, :, 0, 0, 0]
         s.close()
-        ex = ic.isentropic_vortex_exact(cfg, t, quad=5)[:, :, 0]
+        ex = ic.isentropic_vortex_exact(cfg, t, quad=5)
         out[prec] = {"steps": n, "t_end": t, "rel_l2": float(np.linalg.norm(rho - ex) / np.linalg.norm(ex)),
                      "max_abs": float(np.abs(rho - ex).max())}
     out["definition"] = ("cell-average density (coefficient 1 of rho) against the exact solution at t_end "
@@ -758,14 +758,15 @@ def ensemble_accuracy(base, dims, steps):
             "max_rel_l2": max(err.values()), "density_S_k_fp64": {int(k): v for k, v in sf.result().items()}}
 
 
-def ensembles(args, flush, ws, acc_steps=100):
+def ensembles(args, flush, ws, acc_steps=40, acc_steps_hllc=20):
     """The batched fluctuating-hydro ensemble (256 periodic boxes, 10-moment
     ivis 1 + stochastic stress, nb 4, SSP-RK2, Roe): FP32 batched against the
     FP64 batched ensemble of the same draw and against the plain FP64 path on
     one 48^3 box, with and without the stochastic stress; then the accuracy
     of the FP32 ensemble means against FP64 on the same 256-box draw over
     acc_steps of the configuration's 500 steps, with Roe and with the
-    reference's HLLC."""
+    reference's HLLC (the FP64 ensemble's steps dominate the bench's
+    wall time, so the accuracy runs cover the first acc_steps steps)."""
     import torch
     from hermeshd_gb300 import config, ic
     from hermeshd_gb300.solver import Solver
@@ -775,7 +776,7 @@ def ensembles(args, flush, ws, acc_steps=100):
     for llns, tag in ((True, ""), (False, "_no_noise")):
         b32 = config.fh_box(48, precision="fp32", seed=0, llns=llns)
         r32, cells, dof = time_ensemble(b32, dims, K, flush, ws)
-        r64, _, _ = time_ensemble(b32.replace(precision="fp64"), dims, K, flush, ws)
+        r64, _, _ = time_ensemble(b32.replace(precision="fp64"), dims, K, flush, ws, tune=False)
         # plain FP64 on one 48^3 box of the same physics
         c64 = config.fh_box(48, precision="fp64", seed=0, llns=llns)
         s = Solver(c64)
@@ -798,7 +799,7 @@ def ensembles(args, flush, ws, acc_steps=100):
     base = config.fh_box(48, precision="fp32", seed=0)
     out["fp32_batched_ensemble"]["accuracy"] = {
         "roe": ensemble_accuracy(base, dims, acc_steps),
-        "hllc": ensemble_accuracy(base.replace(ihllc=1), dims, acc_steps),
+        "hllc": ensemble_accuracy(base.replace(ihllc=1), dims, acc_steps_hllc),
         "note": "the reference's HLLC with the stress-augmented point flux is discontinuous at S_M = 0, where an "
                 "equilibrium fluctuating state sits at every face, so FP32 and FP64 runs pick its branches by "
                 "rounding; the Roe solver is continuous there"}

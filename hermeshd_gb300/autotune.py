@@ -18,8 +18,11 @@ include/hermes_gb300.h):
                        exists (FP64, nbasis 8/10, no stochastic stress);
 * ``split_update``     the cell update as the volume kernel plus a surface and
                        update kernel of one thread per (cell, variable) (1) or
-                       one kernel (0); tuned where it exists (ivis 0/1, no
-                       stochastic stress).
+                       one kernel (0); tuned where it exists (ivis 0/1);
+* ``tile_stage``       each stage as one fused kernel over tiles of cells (1)
+                       or the separate kernels (0); tried last, where the
+                       context has it (nbasis 4, ivis 0/1).  With it on, only
+                       steps_per_graph still applies.
 
 The cell kernel keeps 32 cells per block: its hydro and stress thread groups
 must each fill whole warps, and its register cap is fixed at compile time.
@@ -45,6 +48,7 @@ KNOBS = {
     "noise_inline": (0, 1),          # tuned only with the stochastic stress on
     "face_traces": (1, 0),           # tuned only where the context has the trace buffer
     "split_update": (1, 0),          # tuned only where the context has the split-update buffer
+    "tile_stage": (0, 1),            # tuned only where the context has the fused stage
 }
 
 
@@ -91,6 +95,17 @@ def _store(key: str, value: dict) -> None:
         pass
 
 
+def _can_tile(solver, cur) -> bool:
+    """Whether the context has the fused stage (it is off by default)."""
+    from ._lib import HermesError
+    try:
+        solver.set_launch(**dict(cur, tile_stage=1))
+    except HermesError:
+        return False
+    solver.set_launch(**cur)
+    return True
+
+
 def time_steps(solver, q, q1, steps: int, repeats: int) -> float:
     """Best-of-repeats milliseconds per step, CUDA events on the kernels' stream."""
     torch = _torch()
@@ -127,6 +142,8 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
     for k in ("face_traces", "split_update"):
         if cur[k] == 0:
             knobs.pop(k, None)
+    if cur["tile_stage"] == 0 and not _can_tile(solver, cur):
+        knobs.pop("tile_stage", None)
     qt, q1t = q.clone(), q.clone()
     best = {k: v[0] for k, v in knobs.items()}
     solver.set_launch(**best)

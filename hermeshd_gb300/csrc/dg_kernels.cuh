@@ -183,8 +183,23 @@ __host__ __device__ constexpr double lim_maxabs(int b) {
     return m;
 }
 
-template <class TB, class U>
-__device__ __forceinline__ bool limit_cell(const Phys& ph, U q[5][TB::NB]) {
+// the rh..en rows of one cell held elsewhere than a register array: element
+// (v, b) at p[v * row + b * col] (shared memory in k_update)
+template <class T>
+struct StridedRows {
+    T* p;
+    int row, col;
+    struct Row {
+        T* p;
+        int col;
+        __device__ __forceinline__ T& operator[](int b) const { return p[b * col]; }
+    };
+    __device__ __forceinline__ Row operator[](int v) const { return Row{p + v * row, col}; }
+};
+
+// q: the rh..en rows, q[v][b] (a U[5][NB] register array or StridedRows<U>)
+template <class TB, class U, class QA>
+__device__ __forceinline__ bool limit_cell(const Phys& ph, QA& q) {
     // returns true if q was modified
     constexpr int NB = TB::NB;
     const U rh_floor = U(ph.rh_floor), epsi = U(ph.rh_floor), epsiP = U(ph.rh_floor) * U(ph.T_floor);
@@ -260,8 +275,8 @@ __device__ __forceinline__ bool limit_cell(const Phys& ph, U q[5][TB::NB]) {
     return changed;
 }
 
-template <class TB, class U>
-__device__ __forceinline__ bool limit_bound_clear(const Phys& ph, const U q[5][TB::NB]) {
+template <class TB, class U, class QA>
+__device__ __forceinline__ bool limit_bound_clear(const Phys& ph, const QA& q) {
     // true if no face point can fall below the density or pressure floor
     constexpr int NB = TB::NB;
     U B[5];
@@ -555,6 +570,26 @@ __global__ void __launch_bounds__(FACE_TPB, (FaceMinBlocks<T>::value)) k_face(co
     });
 }
 
+// the faces of all three directions in one launch: blockIdx.z = direction,
+// blockIdx.y = face point (the blocks of a direction with fewer faces than
+// the largest return at once).  One launch instead of three per stage lets
+// the directions fill each other's tails.
+template <class T, class TB, bool NOISE, bool TRB>
+__global__ void __launch_bounds__(FACE_TPB, (FaceMinBlocks<T>::value)) k_faces(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
+    const long long gf = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int dir = blockIdx.z, p = blockIdx.y;
+    if (gf >= a.G.nface[dir]) return;
+    sfor<3>([&](auto dd) {
+        constexpr int D = decltype(dd)::value;
+        if (dir == D) {
+            sfor<TB::NF>([&](auto pp) {
+                constexpr int P = decltype(pp)::value;
+                if (p == P) face_point<T, TB, D, P, NOISE, TRB>(Q, flux, a, gf);
+            });
+        }
+    });
+}
+
 // ===========================================================================
 // k_cell: two threads per cell.  In a block of 2*CELL_CPB threads, thread
 // c < CELL_CPB owns the hydro variables rh..en of cell c and thread
@@ -576,6 +611,7 @@ struct CellArgs {
     int split_source;   // Grad closure with RK2: the implicit source step after the update
     const void* noise;  // staged interior stochastic stress (k_noise_cell), or null: drawn here
     void* accbuf;       // split update: k_cell stores the volume terms here, k_update finishes
+    int limit_out;      // k_update (FP64): apply the next stage's positivity limiter to the output
 };
 
 // RK combination of integrator.f90:62-86
@@ -1213,50 +1249,85 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
     if (cx.bad) a.flags[0] |= FLAG_NONFINITE;   // integrator.f90:234-250 (the reference exits)
 }
 
-// k_update: the second half of a split k_cell (ivis 0/1): thread per (cell,
-// variable), blockIdx.y = variable.  r = surface sums - volume terms, then the
-// forward-Euler update (integrator.f90:147-149,171-174), the RK combination and
-// the NaN check of the cell average, as cell_surface_update does.
-constexpr int UPD_TPB = 128;
+// k_update: the second half of a split k_cell (ivis 0/1): a block of UPD_CPB
+// cells x NQ variables, thread (cell, variable).  r = surface sums - volume
+// terms, then the forward-Euler update (integrator.f90:147-149,171-174), the
+// RK combination and the NaN check of the cell average, as
+// cell_surface_update does.  With a.limit_out (FP64 stages whose output is the
+// next stage's input), the rh..en outputs of the block's cells go through
+// shared memory to the next stage's positivity limiter (k_limit's operations,
+// flux.f90:1077-1164), one thread per cell, before they are stored: the
+// reference limits that stage's input in place (integrator.f90:110).
+constexpr int UPD_CPB = 16;
+
+// the limiter's full evaluation on rows in shared memory, out of line: the
+// bound check clears almost every cell, and inlined this rare path would set
+// the register allocation of the whole update kernel
+template <class TB, class T>
+__device__ __noinline__ void limit_rows_smem(const Phys& ph, T* p, int row, int col) {
+    StridedRows<T> q{p, row, col};
+    limit_cell<TB, T>(ph, q);
+}
+
 template <class T, class TB>
-__global__ void __launch_bounds__(UPD_TPB) k_update(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux,
-                                                   CellArgs a) {
+__global__ void __launch_bounds__(UPD_CPB * NQ, 3) k_update(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux,
+                                                            CellArgs a) {
     constexpr int NB = TB::NB;
-    const long long gc = (long long)blockIdx.x * UPD_TPB + threadIdx.x;
-    if (gc >= a.G.ncell) return;
-    const int v = blockIdx.y;
-    const int bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
-    const Box& B = a.G.boxes[bx];
-    const long long le = gc - B.cell0, nc = B.ncell, ncl = a.G.ncell;
-    long long fm[3], fp[3], nfd[3];
-    cell_faces(B, le, fm, fp, nfd);
-    const T* ab = static_cast<const T*>(a.accbuf);
-    T r[NB];
+    __shared__ T hyd[5 * NB * UPD_CPB];                 // [variable][basis][cell of the block]
+    const int lc = threadIdx.x, v = threadIdx.y;
+    const long long gc = (long long)blockIdx.x * UPD_CPB + lc;
+    const bool act = gc < a.G.ncell;
+    const bool lim = std::is_same<T, double>::value && a.limit_out && a.mode == MODE_STAGE;   // uniform
+    int bx = 0;
+    long long le = 0, nc = 1;
+    if (act) {
+        bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
+        const Box& B = a.G.boxes[bx];
+        le = gc - B.cell0;
+        nc = B.ncell;
+        const long long ncl = a.G.ncell;
+        long long fm[3], fp[3], nfd[3];
+        cell_faces(B, le, fm, fp, nfd);
+        const T* ab = static_cast<const T*>(a.accbuf);
+        T r[NB];
 #pragma unroll
-    for (int b = 0; b < NB; ++b) r[b] = -ab[((long long)v * NB + b) * ncl + gc];
-    surface_add<T, TB>(flux, B, fm, fp, nfd, v, r);
-    T* ob = out + B.q0;
-    if (a.mode == MODE_RHS) {
+        for (int b = 0; b < NB; ++b) r[b] = -ab[((long long)v * NB + b) * ncl + gc];
+        surface_add<T, TB>(flux, B, fm, fp, nfd, v, r);
+        T* ob = out + B.q0;
+        if (a.mode == MODE_RHS) {
 #pragma unroll
-        for (int b = 0; b < NB; ++b) ob[(long long)(b * NQ + v) * nc + le] = r[b];
-        return;
+            for (int b = 0; b < NB; ++b) ob[(long long)(b * NQ + v) * nc + le] = r[b];
+            return;
+        }
+        const T dt = T(a.st[bx].dt), faci = T(1) / (T(1) + dt * T(a.ph.coll));
+        const T* qb = Qin + B.q0;
+        const T* q0b = Q0 ? Q0 + B.q0 : nullptr;
+        const bool stress_faci = v >= PXX && a.ph.ivis == 1;
+        bool bad = false;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            const long long ix = (long long)(b * NQ + v) * nc + le;
+            T e = qb[ix] - dt * r[b];
+            if (stress_faci) e = faci * e;
+            T o = e;
+            if (a.comb != COMB_NONE) o = rk_combine(a.comb, q0b[ix], o);
+            if (b == 0 && o != o) bad = true;
+            if (lim && v < 5) hyd[(v * NB + b) * UPD_CPB + lc] = o;
+            else ob[ix] = o;
+        }
+        if (bad) a.flags[0] |= FLAG_NONFINITE;
     }
-    const T dt = T(a.st[bx].dt), faci = T(1) / (T(1) + dt * T(a.ph.coll));
-    const T* qb = Qin + B.q0;
-    const T* q0b = Q0 ? Q0 + B.q0 : nullptr;
-    const bool stress_faci = v >= PXX && a.ph.ivis == 1;
-    bool bad = false;
+    if (!lim) return;
+    __syncthreads();
+    if (v != 0 || !act) return;
+    StridedRows<T> q{hyd + lc, NB * UPD_CPB, UPD_CPB};
+    if (!(q[RH][0] >= T(a.ph.rh_floor) && limit_bound_clear<TB, T>(a.ph, q)))
+        limit_rows_smem<TB, T>(a.ph, hyd + lc, NB * UPD_CPB, UPD_CPB);
+    T* ob = out + a.G.boxes[bx].q0;
 #pragma unroll
-    for (int b = 0; b < NB; ++b) {
-        const long long ix = (long long)(b * NQ + v) * nc + le;
-        T e = qb[ix] - dt * r[b];
-        if (stress_faci) e = faci * e;
-        T o = e;
-        if (a.comb != COMB_NONE) o = rk_combine(a.comb, q0b[ix], o);
-        if (b == 0 && o != o) bad = true;
-        ob[ix] = o;
-    }
-    if (bad) a.flags[0] |= FLAG_NONFINITE;
+    for (int w = 0; w < 5; ++w)
+#pragma unroll
+        for (int b = 0; b < NB; ++b) ob[(long long)(b * NQ + w) * nc + le] = q[w][b];
 }
 
 // ===========================================================================

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include "dg_kernels.cuh"
+#include "dg_tile.cuh"
 #include "dg_trace.cuh"
 
 namespace hermes {
@@ -16,12 +17,45 @@ struct KernelSet {
     int nb, nqd, nf;
     cudaError_t (*prepare)();
     void (*limit)(void* Q, const Geom& G, const Phys& ph, cudaStream_t s);
+    // dir 0..2: the faces of one direction; dir -1: all three in one launch
     void (*face)(int dir, const void* Q, void* flux, const FaceArgs& a, cudaStream_t s);
     void (*cell)(const void* Qin, const void* Q0, void* out, const void* flux, const CellArgs& a, cudaStream_t s);
     void (*mindt)(const void* Q, const DtArgs& a, cudaStream_t s);
+    // the CFL reduction fused with the first stage's limiter (FP64: the
+    // stages after it are limited by k_update's fused limiter)
+    void (*mindt_limit_any)(void* Q, const DtArgs& a, cudaStream_t s);
     // face traces into a buffer for the face kernels (FaceArgs.traces); null
     // where the face kernels evaluate the traces themselves
     void (*trace)(const void* Q, void* tr, const Geom& G, cudaStream_t s);
+    // the fused stage (dg_tile.cuh) and the CFL reduction fused with the first
+    // stage's limiter; null where they do not exist (nbasis 8 and 10)
+    void (*tile)(const void* Qin, const void* Q0, void* out, unsigned ntiles, const TileArgs& a, cudaStream_t s);
+    void (*mindt_limit)(void* Q, const DtArgs& a, cudaStream_t s);
+    cudaError_t (*prepare_tile)();
+};
+
+// launchers of the fused stage of one (T, nbasis 4) instantiation (inst_tile.cu)
+template <class T, bool NOISE>
+struct TileLaunch {
+    using TB = hermes_tab::Tab<4, 2>;
+    static constexpr int FMAX = (TILE_X + 1) * TILE_Y * TILE_Z > TILE_X * TILE_Y * (TILE_Z + 1)
+                                    ? (TILE_X + 1) * TILE_Y * TILE_Z : TILE_X * TILE_Y * (TILE_Z + 1);
+    static size_t smem() { return tile_smem<T, TB>(FMAX); }
+    static cudaError_t prepare() {
+        return cudaFuncSetAttribute(k_tile<T, TB, NOISE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem());
+    }
+    static void tile(const void* Qin, const void* Q0, void* out, unsigned ntiles, const TileArgs& a, cudaStream_t s) {
+        if (ntiles == 0) return;
+        TileArgs b = a;
+        b.fmax = FMAX;
+        k_tile<T, TB, NOISE><<<ntiles, TILE_NT, smem(), s>>>(static_cast<const T*>(Qin), static_cast<const T*>(Q0),
+                                                            static_cast<T*>(out), b);
+    }
+    static void mindt_limit(void* Q, const DtArgs& a, cudaStream_t s) {
+        if (a.G.ncell <= 0) return;
+        const unsigned nb = (unsigned)((a.G.ncell + DT_TPB - 1) / DT_TPB);
+        k_mindt_limit<T, TB><<<nb, DT_TPB, 0, s>>>(static_cast<T*>(Q), a);
+    }
 };
 
 // launchers of one (T, NB, NQD) instantiation; the stochastic-stress
@@ -64,12 +98,25 @@ struct Launch {
     }
     template <bool NOISE>
     static void face(int dir, const void* Q, void* flux, const FaceArgs& a, cudaStream_t s) {
-        const long long n = a.G.nface[dir];
-        if (n <= 0) return;
         const int tpb = a.tpb > 0 ? a.tpb : FACE_TPB;
-        dim3 grid((unsigned)((n + tpb - 1) / tpb), TB::NF);
         const T* q = static_cast<const T*>(Q);
         T* f = static_cast<T*>(flux);
+        if (dir < 0) {
+            const long long n = a.G.nface[0] > a.G.nface[1] ? (a.G.nface[0] > a.G.nface[2] ? a.G.nface[0] : a.G.nface[2])
+                                                             : (a.G.nface[1] > a.G.nface[2] ? a.G.nface[1] : a.G.nface[2]);
+            if (n <= 0) return;
+            const dim3 grid((unsigned)((n + tpb - 1) / tpb), TB::NF, 3);
+            if constexpr (HAS_TRACE && !NOISE) {
+                if (a.traces) { k_faces<T, TB, NOISE, true><<<grid, tpb, 0, s>>>(q, f, a); return; }
+            }
+            FaceArgs b = a;
+            b.traces = nullptr;
+            k_faces<T, TB, NOISE, false><<<grid, tpb, 0, s>>>(q, f, b);
+            return;
+        }
+        const long long n = a.G.nface[dir];
+        if (n <= 0) return;
+        dim3 grid((unsigned)((n + tpb - 1) / tpb), TB::NF);
         if constexpr (HAS_TRACE && !NOISE) {
             if (a.traces) { face_dirs<NOISE, true>(dir, grid, tpb, q, f, a, s); return; }
         }
@@ -95,12 +142,17 @@ struct Launch {
         if constexpr (has_split<NOISE>()) {
             if (a.accbuf && a.ph.ivis < 2 && !a.split_source) {
                 k_cell<T, TB, NOISE, true><<<nb, 2 * CELL_CPB, cell_smem(), s>>>(qi, q0, o, f, a);
-                const dim3 grid((unsigned)((a.G.ncell + UPD_TPB - 1) / UPD_TPB), NQ);
-                k_update<T, TB><<<grid, UPD_TPB, 0, s>>>(qi, q0, o, f, a);
+                const unsigned ub = (unsigned)((a.G.ncell + UPD_CPB - 1) / UPD_CPB);
+                k_update<T, TB><<<ub, dim3(UPD_CPB, NQ), 0, s>>>(qi, q0, o, f, a);
                 return;
             }
         }
         k_cell<T, TB, NOISE, false><<<nb, 2 * CELL_CPB, cell_smem(), s>>>(qi, q0, o, f, a);
+    }
+    static void mindt_limit(void* Q, const DtArgs& a, cudaStream_t s) {
+        if (a.G.ncell <= 0) return;
+        const unsigned nb = (unsigned)((a.G.ncell + DT_TPB - 1) / DT_TPB);
+        k_mindt_limit<T, TB><<<nb, DT_TPB, 0, s>>>(static_cast<T*>(Q), a);
     }
     static void mindt(const void* Q, const DtArgs& a, cudaStream_t s) {
         if (a.G.ncell <= 0) return;
@@ -120,6 +172,9 @@ using LimitFn = void (*)(void*, const Geom&, const Phys&, cudaStream_t);
 using DtFn = void (*)(const void*, const DtArgs&, cudaStream_t);
 using TraceFn = void (*)(const void*, void*, const Geom&, cudaStream_t);
 using PrepFn = cudaError_t (*)();
+
+using TileFn = void (*)(const void*, const void*, void*, unsigned, const TileArgs&, cudaStream_t);
+using DtLimitFn = void (*)(void*, const DtArgs&, cudaStream_t);
 
 // precision 64 or 32, nb 4/8/10; false if unsupported
 bool kernel_set(int precision, int nb, bool noise, KernelSet* out);

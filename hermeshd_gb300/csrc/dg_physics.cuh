@@ -14,8 +14,12 @@ namespace hermes {
 // ---------------------------------------------------------------------------
 // Philox-4x32-10 (Salmon et al., SC'11).  Counter scheme:
 //   key = seed, counter = (site, pt | kind<<8 | sub<<12 | stage<<16, step_lo, step_hi)
-// kind: 0..2 face call in x/y/z, 3..5 interior call in x/y/z.  Nine normals per
-// point come from five blocks, one Box-Muller pair per block.
+// kind: 0..2 face call in x/y/z, 3..5 interior call in x/y/z.  The stress of
+// a point needs six independent normals: random.f90:124-141 symmetrises a
+// 3x3 matrix of nine iid N(0,1) values, whose three diagonal entries and three
+// scaled sums sqrt(1/2) (G_ij + G_ji) are six iid N(0,1) values -- drawn here
+// directly.  Two blocks (sub 0, 1) give eight 32-bit words, one uniform each;
+// three Box-Muller pairs of the first six give the six normals.
 // ---------------------------------------------------------------------------
 struct NoiseCtr {
     unsigned long long step;
@@ -34,66 +38,73 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
     }
 }
 
+// one Box-Muller pair from two 32-bit words; every rounding explicit (no
+// contraction into FMAs), so the numbers do not depend on the kernel the
+// generator is inlined into
 template <class T>
-__device__ __forceinline__ void normals9(unsigned long long seed, NoiseCtr nc, unsigned kind, unsigned long long site,
-                                         unsigned pt, T G[9]) {
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, T& z0, T& z1) {
+    if constexpr (std::is_same<T, double>::value) {
+        // 32-bit uniforms in (0,1): (w + 1/2) 2^-32
+        const double u1 = __dmul_rn(__dadd_rn((double)a, 0.5), 1.0 / 4294967296.0);
+        const double u2 = __dmul_rn(__dadd_rn((double)b, 0.5), 1.0 / 4294967296.0);
+        double r = sqrt(__dmul_rn(-2.0, log(u1))), s, co;
+        sincos(__dmul_rn(6.283185307179586476925286766559, u2), &s, &co);
+        z0 = __dmul_rn(r, co); z1 = __dmul_rn(r, s);
+    } else {
+        // the top 24 bits of the same words; the hardware log2 and sin/cos
+        // (absolute error ~2^-21 on (-pi, pi)), with the angle moved to
+        // (-pi, pi) by cos(t - pi) = -cos t, sin(t - pi) = -sin t
+        const float u1 = __fmul_rn(__fadd_rn((float)(a >> 8), 0.5f), 1.0f / 16777216.0f);
+        const float u2 = __fmul_rn(__fadd_rn((float)(b >> 8), 0.5f), 1.0f / 16777216.0f);
+        float r = sqrtf(__fmul_rn(-2.0f, __logf(u1))), s, co;
+        __sincosf(__fmul_rn(6.2831853071795864769f, __fsub_rn(u2, 0.5f)), &s, &co);
+        z0 = -__fmul_rn(r, co); z1 = -__fmul_rn(r, s);
+    }
+}
+
+// G = {xx, yy, zz, xy, xz, yz}: the diagonal and the symmetrised off-diagonal normals
+template <class T>
+__device__ __forceinline__ void normals6(unsigned long long seed, NoiseCtr nc, unsigned kind, unsigned long long site,
+                                         unsigned pt, T G[6]) {
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    uint32_t w[8];
 #pragma unroll
-    for (int sub = 0; sub < 5; ++sub) {
-        uint32_t c[4];
+    for (int sub = 0; sub < 2; ++sub) {
+        uint32_t* c = w + 4 * sub;
         c[0] = (uint32_t)site;
         c[1] = (pt & 0xFFu) | ((kind & 0xFu) << 8) | (((unsigned)sub & 0xFu) << 12) | ((nc.stage & 0xFFFFu) << 16);
         c[2] = (uint32_t)nc.step;
         c[3] = (uint32_t)(nc.step >> 32);
         philox4x32_10(c, k0, k1);
-        // every rounding explicit (no contraction into FMAs), so the numbers do
-        // not depend on the kernel the generator is inlined into
-        T z0, z1;
-        if constexpr (std::is_same<T, double>::value) {
-            // 53-bit uniforms in (0,1)
-            unsigned long long m1 = ((unsigned long long)c[0] << 21) | (unsigned long long)(c[1] >> 11);
-            unsigned long long m2 = ((unsigned long long)c[2] << 21) | (unsigned long long)(c[3] >> 11);
-            double u1 = __dmul_rn(__dadd_rn((double)m1, 0.5), 1.0 / 9007199254740992.0);
-            double u2 = __dmul_rn(__dadd_rn((double)m2, 0.5), 1.0 / 9007199254740992.0);
-            double r = sqrt(__dmul_rn(-2.0, log(u1))), s, co;
-            sincos(__dmul_rn(6.283185307179586476925286766559, u2), &s, &co);
-            z0 = __dmul_rn(r, co); z1 = __dmul_rn(r, s);
-        } else {
-            // the top 24 bits of the same words; the hardware log2 and sin/cos
-            // (absolute error ~2^-21 on (-pi, pi)), with the angle moved to
-            // (-pi, pi) by cos(t - pi) = -cos t, sin(t - pi) = -sin t
-            float u1 = __fmul_rn(__fadd_rn((float)(c[0] >> 8), 0.5f), 1.0f / 16777216.0f);
-            float u2 = __fmul_rn(__fadd_rn((float)(c[2] >> 8), 0.5f), 1.0f / 16777216.0f);
-            float r = sqrtf(__fmul_rn(-2.0f, __logf(u1))), s, co;
-            __sincosf(__fmul_rn(6.2831853071795864769f, __fsub_rn(u2, 0.5f)), &s, &co);
-            z0 = -__fmul_rn(r, co); z1 = -__fmul_rn(r, s);
-        }
-        if (2 * sub < 9) G[2 * sub] = z0;
-        if (2 * sub + 1 < 9) G[2 * sub + 1] = z1;
     }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) box_muller<T>(w[2 * k], w[2 * k + 1], G[2 * k], G[2 * k + 1]);
 }
 
 // random.f90:106-145: S = eta (sym G - tr G/3 I) + zeta tr G I, the
 // amplitudes already carrying 1/sqrt(dV dt).  S = {xx, yy, zz, xy, xz, yz}.
 template <class T>
-__device__ __forceinline__ void random_stress(const Phys& ph, unsigned long long seed, NoiseCtr nc, unsigned kind,
-                                              unsigned long long site, unsigned pt, T S[6]) {
-    T G[9];
-    normals9<T>(seed, nc, kind, site, pt, G);
-    const T s2i = T(0.70710678118654752440);
-    const T eta = T(ph.eta_sd), zeta = T(ph.zeta_sd);
-    // explicit roundings, as in normals9: the same numbers in every kernel
+__device__ __forceinline__ void random_stress_amp(T eta, T zeta, unsigned long long seed, NoiseCtr nc, unsigned kind,
+                                                  unsigned long long site, unsigned pt, T S[6]) {
+    T G[6];
+    normals6<T>(seed, nc, kind, site, pt, G);
+    // explicit roundings, as in box_muller: the same numbers in every kernel
     auto add = [](T x, T y) { if constexpr (std::is_same<T, double>::value) return __dadd_rn(x, y); else return __fadd_rn(x, y); };
     auto sub = [](T x, T y) { if constexpr (std::is_same<T, double>::value) return __dsub_rn(x, y); else return __fsub_rn(x, y); };
     auto mul = [](T x, T y) { if constexpr (std::is_same<T, double>::value) return __dmul_rn(x, y); else return __fmul_rn(x, y); };
-    T Gxy = mul(s2i, add(G[1], G[3])), Gxz = mul(s2i, add(G[2], G[6])), Gyz = mul(s2i, add(G[5], G[7]));
-    T trG = add(add(G[0], G[4]), G[8]), trGd3 = trG / T(3), trGz = mul(zeta, trG);
+    T trG = add(add(G[0], G[1]), G[2]), trGd3 = trG / T(3), trGz = mul(zeta, trG);
     S[0] = add(mul(eta, sub(G[0], trGd3)), trGz);
-    S[1] = add(mul(eta, sub(G[4], trGd3)), trGz);
-    S[2] = add(mul(eta, sub(G[8], trGd3)), trGz);
-    S[3] = mul(eta, Gxy);
-    S[4] = mul(eta, Gxz);
-    S[5] = mul(eta, Gyz);
+    S[1] = add(mul(eta, sub(G[1], trGd3)), trGz);
+    S[2] = add(mul(eta, sub(G[2], trGd3)), trGz);
+    S[3] = mul(eta, G[3]);
+    S[4] = mul(eta, G[4]);
+    S[5] = mul(eta, G[5]);
+}
+
+template <class T>
+__device__ __forceinline__ void random_stress(const Phys& ph, unsigned long long seed, NoiseCtr nc, unsigned kind,
+                                              unsigned long long site, unsigned pt, T S[6]) {
+    random_stress_amp<T>(T(ph.eta_sd), T(ph.zeta_sd), seed, nc, kind, site, pt, S);
 }
 
 // ---------------------------------------------------------------------------

@@ -140,7 +140,7 @@ struct hermes_ctx {
     struct Rec { int kind; cudaEvent_t a, b; };
     std::vector<Rec> recs;
     std::vector<cudaEvent_t> pool;
-    static constexpr int NKIND = 8;
+    static constexpr int NKIND = 9;
     double prof_ms[NKIND] = {};
     long long prof_n[NKIND] = {};
     // launch shape (hermes_set_launch); 0 = the compiled defaults
@@ -156,6 +156,15 @@ struct hermes_ctx {
     // split cell update: volume terms of k_cell for k_update
     void* d_accbuf = nullptr;
     bool split_update = false;
+    // fused stage (dg_tile.cuh): first tile of each box, tile count, and a
+    // third state for the RK3 stage whose output cannot overwrite its input
+    long long* d_tile0 = nullptr;
+    unsigned ntiles = 0;
+    void* d_qs = nullptr;
+    bool tile_stage = false;
+    bool tile_ok_default = false;   // the autotuner tries the fused stage here
+    // the three face directions in one launch (k_faces)
+    bool faces_merged = true;
     // adjoint scratch, allocated on first use
     AdjFn adj = nullptr;
     double* d_tadj = nullptr;   // trace adjoints: 2 x the face-flux size
@@ -326,15 +335,21 @@ void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
         ProfScope ps(c, 7);
         c->K.trace(q, c->d_traces, c->G, c->stream);
     }
+    if (c->faces_merged) {
+        ProfScope ps(c, 2);
+        c->K.face(-1, q, c->d_flux, a, c->stream);
+        return;
+    }
     for (int d = 0; d < 3; ++d) {
         ProfScope ps(c, 2 + d);
         c->K.face(d, q, c->d_flux, a, c->stream);
     }
 }
-void enq_cell(hermes_ctx* c, const void* qin, const void* q0, void* out, int mode, int comb, unsigned stage) {
+void enq_cell(hermes_ctx* c, const void* qin, const void* q0, void* out, int mode, int comb, unsigned stage,
+              int limit_out = 0) {
     const int split = (mode == MODE_STAGE && c->cfg.ivis == 3 && c->cfg.iorder == 2) ? 1 : 0;
     CellArgs a{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb, split,
-               c->noise_staged ? c->d_noise_cell : nullptr, c->split_update ? c->d_accbuf : nullptr};
+               c->noise_staged ? c->d_noise_cell : nullptr, c->split_update ? c->d_accbuf : nullptr, limit_out};
     ProfScope ps(c, 5);
     c->K.cell(qin, q0, out, c->d_flux, a, c->stream);
 }
@@ -344,12 +359,38 @@ void enq_noise(hermes_ctx* c, unsigned stage) {
     ProfScope ps(c, 6);
     c->noise_fn(c->d_noise_cell, c->d_noise_face, a, c->stream);
 }
-void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, unsigned stage) {
+// the fused stage: out = comb(q0, E(qin)), with the next stage's limiter
+// applied to out when limit_out (qin must not alias out)
+void enq_tile(hermes_ctx* c, const void* qin, const void* q0, void* out, int mode, int comb, unsigned stage,
+              int limit_out) {
+    TileArgs a{};
+    a.c = CellArgs{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb, 0, nullptr, nullptr};
+    a.tile0 = c->d_tile0;
+    a.limit_out = limit_out;
+    ProfScope ps(c, 8);
+    c->K.tile(qin, q0, out, c->ntiles, a, c->stream);
+}
+// limit_in: the stage's limiter as a pass of its own (else already applied
+// by the kernel that wrote qin); limit_out: the next stage's limiter applied
+// to out by k_update (FP64 split update)
+void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, unsigned stage, bool limit_in = true,
+               int limit_out = 0) {
     NvtxRange r("hermes stage");
-    enq_limit(c, qin);
+    if (limit_in) enq_limit(c, qin);
+    if (c->tile_stage && qin != out) {
+        enq_tile(c, qin, q0, out, MODE_STAGE, comb, stage, 0);
+        return;
+    }
     enq_noise(c, stage);
     enq_faces(c, qin, stage);
-    enq_cell(c, qin, q0, out, MODE_STAGE, comb, stage);
+    enq_cell(c, qin, q0, out, MODE_STAGE, comb, stage, limit_out);
+}
+
+// the limiter fused into the CFL reduction and into k_update: FP64 with the
+// split update (the separate kernels otherwise)
+bool fused_limiter(const hermes_ctx* c) {
+    return c->split_update && c->K.elem_size == (int)sizeof(double) && c->cfg.ivis < 2 && c->K.mindt_limit_any &&
+           (c->cfg.ieos == 1 || c->cfg.ieos == 2);
 }
 void enq_mindt(hermes_ctx* c, const void* q, bool advance) {
     DtArgs a{c->G, c->ph, c->d_st, c->dt_tpb};
@@ -359,15 +400,50 @@ void enq_mindt(hermes_ctx* c, const void* q, bool advance) {
     if (advance) k_dt_finalize<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st, c->d_step);
     else k_dt_finalize_only<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st);
 }
-void enq_step(hermes_ctx* c, void* q, void* q1) {
+// a step of fused stages: the CFL reduction with the first stage's limiter,
+// then one kernel per stage, each applying the next stage's limiter to its
+// output (the reference limits each stage's input in place, integrator.f90:110)
+void enq_step_tile(hermes_ctx* c, void* q, void* q1) {
     NvtxRange r("hermes step");
-    enq_mindt(c, q, true);                           // hermeshd.f90:59
-    enq_stage(c, q, nullptr, q1, COMB_NONE, 0);      // Q_1 = E(Q)
+    {
+        DtArgs a{c->G, c->ph, c->d_st, 0};
+        ProfScope ps(c, 0);
+        c->K.mindt_limit(q, a, c->stream);          // hermeshd.f90:59 get_min_dt, then limiter(Q)
+        const int nb = c->G.nbox, tpb = 128;
+        k_dt_finalize<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st, c->d_step);
+    }
+    enq_tile(c, q, nullptr, q1, MODE_STAGE, COMB_NONE, 0, 1);          // Q_1 = lim(E(Q))
     if (c->cfg.iorder == 3) {
-        enq_stage(c, q1, q, q1, COMB_34, 1);         // Q_1 = 3/4 Q + 1/4 E(Q_1)
-        enq_stage(c, q1, q, q, COMB_13, 2);          // Q = 1/3 Q + 2/3 E(Q_1)
+        enq_tile(c, q1, q, c->d_qs, MODE_STAGE, COMB_34, 1, 1);        // Q_s = lim(3/4 Q + 1/4 E(Q_1))
+        enq_tile(c, c->d_qs, q, q, MODE_STAGE, COMB_13, 2, 0);         // Q = 1/3 Q + 2/3 E(Q_s)
     } else {
-        enq_stage(c, q1, q, q, COMB_HALF, 1);        // Q = (Q + E(Q_1))/2
+        enq_tile(c, q1, q, q, MODE_STAGE, COMB_HALF, 1, 0);            // Q = (Q + E(Q_1))/2
+    }
+}
+
+void enq_step(hermes_ctx* c, void* q, void* q1) {
+    if (c->tile_stage) {
+        enq_step_tile(c, q, q1);
+        return;
+    }
+    NvtxRange r("hermes step");
+    const bool fl = fused_limiter(c);
+    if (fl) {
+        // hermeshd.f90:59 get_min_dt on the unlimited Q, then the first stage's limiter
+        DtArgs a{c->G, c->ph, c->d_st, 0};
+        ProfScope ps(c, 0);
+        c->K.mindt_limit_any(q, a, c->stream);
+        const int nb = c->G.nbox, tpb = 128;
+        k_dt_finalize<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st, c->d_step);
+    } else {
+        enq_mindt(c, q, true);                                   // hermeshd.f90:59
+    }
+    enq_stage(c, q, nullptr, q1, COMB_NONE, 0, !fl, fl);        // Q_1 = E(Q)
+    if (c->cfg.iorder == 3) {
+        enq_stage(c, q1, q, q1, COMB_34, 1, !fl, fl);           // Q_1 = 3/4 Q + 1/4 E(Q_1)
+        enq_stage(c, q1, q, q, COMB_13, 2, !fl, 0);             // Q = 1/3 Q + 2/3 E(Q_1)
+    } else {
+        enq_stage(c, q1, q, q, COMB_HALF, 1, !fl, 0);           // Q = (Q + E(Q_1))/2
     }
 }
 
@@ -503,6 +579,32 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
         if (cudaMalloc(&c->d_accbuf, (size_t)ncell * NQ * c->K.nb * c->K.elem_size) == cudaSuccess) c->split_update = true;
         else { cudaGetLastError(); c->d_accbuf = nullptr; }   // no room: one kernel
     }
+    if (c->K.tile && cfg->ivis < 2) {
+        // fused stage: the tiles of every box, a third state, launch attributes
+        std::vector<long long> t0(nbox + 1, 0);
+        bool three_d = true;
+        for (int i = 0; i < nbox; ++i) {
+            const Box& b = c->h_boxes[i];
+            const long long nt = (long long)((b.n[0] + TILE_X - 1) / TILE_X) * ((b.n[1] + TILE_Y - 1) / TILE_Y) *
+                                 ((b.n[2] + TILE_Z - 1) / TILE_Z);
+            t0[i + 1] = t0[i] + nt;
+            three_d = three_d && b.n[2] >= TILE_Z;
+        }
+        if (t0[nbox] < (1ll << 31) && c->K.prepare_tile() == cudaSuccess &&
+            cudaMalloc(&c->d_tile0, sizeof(long long) * (nbox + 1)) == cudaSuccess &&
+            cudaMemcpy(c->d_tile0, t0.data(), sizeof(long long) * (nbox + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMalloc(&c->d_qs, c->q_elems * c->K.elem_size) == cudaSuccess) {
+            c->ntiles = (unsigned)t0[nbox];
+            // off by default: measured slower than the separate kernels on
+            // every workload (register and shared-memory bound); the
+            // autotuner tries it on grids at least one tile deep in z
+            c->tile_ok_default = three_d;
+        } else {
+            cudaGetLastError();
+            cudaFree(c->d_tile0); cudaFree(c->d_qs);
+            c->d_tile0 = nullptr; c->d_qs = nullptr;
+        }
+    }
     if (c->K.trace) {
         // face traces: 2 sides x 3 directions x NQ x NF values per cell
         const size_t bytes = (size_t)ncell * 6 * NQ * c->K.nf * c->K.elem_size;
@@ -593,6 +695,8 @@ int hermes_destroy(hermes_ctx* c) {
     cudaFree(c->d_noise_face);
     cudaFree(c->d_traces);
     cudaFree(c->d_accbuf);
+    cudaFree(c->d_tile0);
+    cudaFree(c->d_qs);
     delete c;
     return HERMES_OK;
 }
@@ -629,6 +733,10 @@ int hermes_rhs(hermes_ctx* c, void* q, void* rhs, int apply_limiter) {
     int rc = enter(c);
     if (rc) return rc;
     if (apply_limiter) enq_limit(c, q);
+    if (c->tile_stage) {
+        enq_tile(c, q, nullptr, rhs, MODE_RHS, COMB_NONE, 0, 0);
+        return leave(c, launch_status(c));
+    }
     enq_noise(c, 0);
     enq_faces(c, q, 0);
     enq_cell(c, q, nullptr, rhs, MODE_RHS, COMB_NONE, 0);
@@ -809,8 +917,12 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
         return fail(c, HERMES_ERR_ARG, "the split update needs ivis 0/1, room for the buffer and, with the stochastic "
                                        "stress in FP64, nbasis 4");
     const bool split = l->split_update == 1;
+    if (l->tile_stage != 0 && l->tile_stage != 1) return fail(c, HERMES_ERR_ARG, "tile_stage must be 0 or 1");
+    if (l->tile_stage == 1 && !c->d_tile0)
+        return fail(c, HERMES_ERR_ARG, "the fused stage needs nbasis 4, ivis 0/1 and room for a third state");
+    const bool tile = l->tile_stage == 1;
     if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged || traces != c->face_traces ||
-        split != c->split_update) {
+        split != c->split_update || tile != c->tile_stage) {
         // captured graphs hold the old launch shape
         HCK(c, cudaSetDevice(c->device));
         HCK(c, cudaStreamSynchronize(c->stream));
@@ -822,6 +934,7 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     c->noise_staged = staged;
     c->face_traces = traces;
     c->split_update = split;
+    c->tile_stage = tile;
     return HERMES_OK;
 }
 
@@ -833,6 +946,7 @@ int hermes_get_launch(hermes_ctx* c, hermes_launch* l) {
     l->noise_inline = (c->cfg.llns && !c->noise_staged) ? 1 : 0;
     l->face_traces = c->face_traces ? 1 : 0;
     l->split_update = c->split_update ? 1 : 0;
+    l->tile_stage = c->tile_stage ? 1 : 0;
     return HERMES_OK;
 }
 

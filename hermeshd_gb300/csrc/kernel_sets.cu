@@ -54,9 +54,33 @@ void celln_f32_nb10(const void*, const void*, void*, const void*, const CellArgs
 cudaError_t prep_f32_nb10();
 cudaError_t prepn_f32_nb10();
 
+void tile_f32_nb4(const void*, const void*, void*, unsigned, const TileArgs&, cudaStream_t);
+void tilen_f32_nb4(const void*, const void*, void*, unsigned, const TileArgs&, cudaStream_t);
+void tile_f64_nb4(const void*, const void*, void*, unsigned, const TileArgs&, cudaStream_t);
+void tilen_f64_nb4(const void*, const void*, void*, unsigned, const TileArgs&, cudaStream_t);
+void dtlim_f32_nb4(void*, const DtArgs&, cudaStream_t);
+void dtlim_f64_nb4(void*, const DtArgs&, cudaStream_t);
+cudaError_t tprep_f32_nb4();
+cudaError_t tprepn_f32_nb4();
+cudaError_t tprep_f64_nb4();
+cudaError_t tprepn_f64_nb4();
+
+// the CFL reduction fused with the first stage's limiter, every instantiation
+// (a small kernel, instantiated here)
+static DtLimitFn dt_limit_fn(int precision, int nb) {
+    if (precision == 64) return nb == 4 ? &Launch<double, 4, 2>::mindt_limit
+                              : nb == 8 ? &Launch<double, 8, 2>::mindt_limit : &Launch<double, 10, 3>::mindt_limit;
+    return nb == 4 ? &Launch<float, 4, 2>::mindt_limit : nb == 8 ? &Launch<float, 8, 2>::mindt_limit
+                                                               : &Launch<float, 10, 3>::mindt_limit;
+}
+
 bool kernel_set(int precision, int nb, bool noise, KernelSet* out) {
     KernelSet k;
+    k.mindt_limit_any = dt_limit_fn(precision, nb);
     k.trace = nullptr;
+    k.tile = nullptr;
+    k.mindt_limit = nullptr;
+    k.prepare_tile = nullptr;
     if (precision == 64 && nb == 4) {
         k.elem_size = sizeof(double); k.nb = 4; k.nqd = 2; k.nf = 4;
         k.prepare = noise ? &prepn_f64_nb4 : &prep_f64_nb4;
@@ -64,6 +88,9 @@ bool kernel_set(int precision, int nb, bool noise, KernelSet* out) {
         k.face = noise ? &facen_f64_nb4 : &face_f64_nb4;
         k.cell = noise ? &celln_f64_nb4 : &cell_f64_nb4;
         k.mindt = &mindt_f64_nb4;
+        k.tile = noise ? &tilen_f64_nb4 : &tile_f64_nb4;
+        k.mindt_limit = &dtlim_f64_nb4;
+        k.prepare_tile = noise ? &tprepn_f64_nb4 : &tprep_f64_nb4;
         *out = k;
         return true;
     }
@@ -96,6 +123,9 @@ bool kernel_set(int precision, int nb, bool noise, KernelSet* out) {
         k.face = noise ? &facen_f32_nb4 : &face_f32_nb4;
         k.cell = noise ? &celln_f32_nb4 : &cell_f32_nb4;
         k.mindt = &mindt_f32_nb4;
+        k.tile = noise ? &tilen_f32_nb4 : &tile_f32_nb4;
+        k.mindt_limit = &dtlim_f32_nb4;
+        k.prepare_tile = noise ? &tprepn_f32_nb4 : &tprep_f32_nb4;
         *out = k;
         return true;
     }

@@ -95,7 +95,7 @@ def isentropic_vortex_exact(cfg: Config, t: float, ver: int = 1, beta: float = 5
     """Density of the exactly advected vortex at time t (the IC shifted by the
     mean flow, periodically wrapped, initialcon.f90:158-177): sampled at the
     cell centres (quad = 1) or averaged over each cell by a quad x quad
-    Gauss-Legendre rule (quad > 1), shape (nx, ny, nz)."""
+    Gauss-Legendre rule (quad > 1), shape (nx, ny)."""
     vx_amb, vy_amb, Rgsqi = (1.0, 0.0, 1.0) if ver == 0 else (1.0, 1.0, 0.5)
     g = cfg.aindex
     xc, yc, zc = cell_centres(cfg)
@@ -113,7 +113,7 @@ def isentropic_vortex_exact(cfg: Config, t: float, ver: int = 1, beta: float = 5
             r2 = Xs ** 2 + Ys ** 2
             dT = -((g - 1) * beta ** 2) / (16 * Rgsqi * g * math.pi ** 2) * np.exp(2 * Rgsqi * (1 - r2))
             out += 0.25 * wa * wb * (1.0 + dT) ** (1.0 / (g - 1))
-    return np.broadcast_to(out[:, :, None], (cfg.nx, cfg.ny, cfg.nz)).copy()
+    return out
 
 
 def taylor_green(cfg: Config, rho: float = 1.0, V0: float = 1.0, perturb: float = 0.0, seed: int = 0) -> np.ndarray:

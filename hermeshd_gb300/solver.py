@@ -137,7 +137,7 @@ class Solver:
     def profile(self, enable: bool = True):
         check(lib().hermes_profile_enable(self.ctx, int(enable)), self.ctx)
 
-    KERNEL_KINDS = ("cfl_dt", "limiter", "face_x", "face_y", "face_z", "cell", "noise", "trace")
+    KERNEL_KINDS = ("cfl_dt", "limiter", "face_x", "face_y", "face_z", "cell", "noise", "trace", "tile")
 
     def profile_read(self):
         ms = np.zeros(len(self.KERNEL_KINDS))
@@ -175,21 +175,25 @@ class Solver:
         l = _lib.HermesLaunch()
         check(lib().hermes_get_launch(self.ctx, C.byref(l)), self.ctx)
         return {"face_tpb": l.face_tpb, "dt_tpb": l.dt_tpb, "steps_per_graph": l.steps_per_graph,
-                "noise_inline": l.noise_inline, "face_traces": l.face_traces, "split_update": l.split_update}
+                "noise_inline": l.noise_inline, "face_traces": l.face_traces, "split_update": l.split_update,
+                "tile_stage": l.tile_stage}
 
     def set_launch(self, face_tpb: int = 0, dt_tpb: int = 0, steps_per_graph: int = 1, noise_inline: int = 0,
-                   face_traces=None, split_update=None):
-        """face_traces / split_update None keep the context's current choice
-        (on by default where they exist: the trace kernel for FP64, nbasis
-        8/10, no stochastic stress; the split update for ivis 0/1, no
-        stochastic stress)."""
+                   face_traces=None, split_update=None, tile_stage=None):
+        """face_traces / split_update / tile_stage None keep the context's
+        current choice (the trace kernel and the split update are on by
+        default where they exist: FP64 nbasis 8/10 without the stochastic
+        stress, and ivis 0/1; the fused stage, nbasis 4 ivis 0/1, is off by
+        default)."""
         cur = self.get_launch()
         if face_traces is None:
             face_traces = cur["face_traces"]
         if split_update is None:
             split_update = cur["split_update"]
+        if tile_stage is None:
+            tile_stage = cur["tile_stage"]
         l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), int(noise_inline), int(face_traces),
-                              int(split_update))
+                              int(split_update), int(tile_stage))
         check(lib().hermes_set_launch(self.ctx, C.byref(l)), self.ctx)
 
     def set_noise_step(self, step: int):

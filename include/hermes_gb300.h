@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define HERMES_ABI_VERSION 5
+#define HERMES_ABI_VERSION 6
 
 typedef enum hermes_status {
     HERMES_OK = 0,
@@ -224,6 +224,13 @@ typedef struct hermes_launch {
                                 FP64 for nbasis 4; the default there (the buffer is allocated at
                                 creation); 0: one kernel.
                                 Bit-identical. */
+    int32_t tile_stage;      /* 1: each RK stage as one fused kernel over tiles of 8x8x4 cells (faces,
+                                surface and volume quadrature, update, RK combination and the next
+                                stage's limiter; the stochastic stress drawn in place), the CFL
+                                reduction fused with the first stage's limiter; nbasis 4, ivis 0/1
+                                (a third state is allocated at creation).  Off by default: slower
+                                than the separate kernels on the measured workloads; the autotuner
+                                tries it.  0: the separate kernels.  Equal to rounding. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
 int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);
@@ -232,10 +239,11 @@ int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);
  * enabled, steps run without the graph and every kernel launch is bracketed
  * by an event pair.  hermes_profile_read synchronises, returns accumulated
  * milliseconds and launch counts per kernel kind and resets them.  Kinds:
- * 0 CFL reduction, 1 limiter, 2 x faces, 3 y faces, 4 z faces, 5 cell update,
- * 6 staged stochastic stress (the four noise kernels of a stage), 7 face traces. */
+ * 0 CFL reduction (with the fused stage: and the first stage's limiter), 1 limiter,
+ * 2 x faces, 3 y faces, 4 z faces, 5 cell update, 6 staged stochastic stress (the
+ * four noise kernels of a stage), 7 face traces, 8 fused stage. */
 int hermes_profile_enable(hermes_ctx *ctx, int enable);
-int hermes_profile_read(hermes_ctx *ctx, double *ms /* [8] */, int64_t *launches /* [8] */);
+int hermes_profile_read(hermes_ctx *ctx, double *ms /* [9] */, int64_t *launches /* [9] */);
 
 /* Per-box time and last time step of an ensemble (nbox entries each). */
 int hermes_box_times(hermes_ctx *ctx, double *t, double *dt);

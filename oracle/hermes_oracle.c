@@ -422,14 +422,13 @@ int orc_get_table(const orc_ctx *c, const char *name, double *out, int maxn) {
 enum { NOISE_FACE_X = 0, NOISE_FACE_Y = 1, NOISE_FACE_Z = 2, NOISE_INT_X = 3, NOISE_INT_Y = 4, NOISE_INT_Z = 5 };
 
 static void stress_at(const orc_ctx *c, int kind, unsigned long long site, int pt, double S[6]) {
-    double G[9];
-    hermes_philox_normals9(c->p.seed, c->noise_step, (unsigned)c->noise_stage, (unsigned)kind, site, (unsigned)pt, G);
-    /* random.f90:124-141 (amplitudes eta_sd, zeta_sd already carry 1/sqrt(dV dt)) */
-    const double s2i = 1. / sqrt(2.);
-    double Gxx = G[0], Gyy = G[4], Gzz = G[8];
-    double Gxy = s2i * (G[1] + G[3]);
-    double Gxz = s2i * (G[2] + G[6]);
-    double Gyz = s2i * (G[5] + G[7]);
+    double G[6];
+    hermes_philox_normals6(c->p.seed, c->noise_step, (unsigned)c->noise_stage, (unsigned)kind, site, (unsigned)pt, G);
+    /* random.f90:124-141 (amplitudes eta_sd, zeta_sd already carry 1/sqrt(dV dt)):
+     * the diagonal G_ii and the symmetrised off-diagonal sqrt(1/2) (G_ij + G_ji)
+     * of an iid N(0,1) matrix are six iid N(0,1) values, drawn directly */
+    double Gxx = G[0], Gyy = G[1], Gzz = G[2];
+    double Gxy = G[3], Gxz = G[4], Gyz = G[5];
     double trG = Gxx + Gyy + Gzz, trGd3 = trG / 3.0, trGz = c->p.zeta_sd * trG;
     S[0] = c->p.eta_sd * (Gxx - trGd3) + trGz;  /* Sxx */
     S[1] = c->p.eta_sd * (Gyy - trGd3) + trGz;  /* Syy */
@@ -1454,7 +1453,7 @@ double orc_test_basis(const orc_ctx *c, double *cell_dev, double *face_dev) {
 }
 
 void orc_noise_sample(unsigned long long seed, unsigned long long step, unsigned stage, unsigned kind,
-                      unsigned long long site, unsigned pt, double eta, double zeta, double G9[9], double S6[6]) {
+                      unsigned long long site, unsigned pt, double eta, double zeta, double G6[6], double S6[6]) {
     orc_ctx c;
     memset(&c, 0, sizeof(c));
     c.p.seed = seed;
@@ -1462,7 +1461,7 @@ void orc_noise_sample(unsigned long long seed, unsigned long long step, unsigned
     c.p.zeta_sd = zeta;
     c.noise_step = step;
     c.noise_stage = (int)stage;
-    hermes_philox_normals9(seed, step, stage, kind, site, pt, G9);
+    hermes_philox_normals6(seed, step, stage, kind, site, pt, G6);
     stress_at(&c, (int)kind, site, (int)pt, S6);
 }
 

@@ -84,7 +84,7 @@ void orc_set_noise_counter(orc_ctx *c, unsigned long long step);
 /* nine Philox normals and the stochastic stress {xx,yy,zz,xy,xz,yz} of one
  * quadrature point of one flux call (for statistical tests) */
 void orc_noise_sample(unsigned long long seed, unsigned long long step, unsigned stage, unsigned kind,
-                      unsigned long long site, unsigned pt, double eta, double zeta, double G9[9], double S6[6]);
+                      unsigned long long site, unsigned pt, double eta, double zeta, double G6[6], double S6[6]);
 /* one Philox-4x32-10 block (known-answer tests) */
 void orc_philox4x32_10(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]);
 

@@ -230,8 +230,9 @@ def set_num_threads(n):
 
 
 def noise_sample(seed, step, stage, kind, site, pt, eta=1.0, zeta=0.0):
-    """(9 normals, stress {xx,yy,zz,xy,xz,yz}) of one point of one flux call."""
-    G = np.zeros(9)
+    """(6 normals {xx, yy, zz, xy, xz, yz}, stress {xx,yy,zz,xy,xz,yz}) of one
+    point of one flux call."""
+    G = np.zeros(6)
     S = np.zeros(6)
     lib().orc_noise_sample(seed, step, stage, kind, site, pt, eta, zeta, G, S)
     return G, S

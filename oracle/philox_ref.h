@@ -12,8 +12,12 @@
  *   counter = (site, pt | kind<<8 | sub<<12 | stage<<16, step_lo, step_hi)
  * where site is the face or cell index, pt the quadrature point of the call,
  * kind the flux call (face x/y/z, interior x/y/z), sub the Philox block
- * (0..4) and stage the RK stage.  Each block gives two 53-bit uniforms and
- * one Box-Muller pair; nine normals per point use five blocks.
+ * (0, 1) and stage the RK stage.  The stress needs six independent normals
+ * per point (random.f90 symmetrises a 3x3 matrix of nine: its three diagonal
+ * entries and the three scaled sums sqrt(1/2) (G_ij + G_ji) are six
+ * independent N(0,1) values, drawn here directly).  Each 32-bit output word
+ * is one uniform in (0,1), (w + 1/2) 2^-32; two blocks give eight, and three
+ * Box-Muller pairs of the first six give the six normals.
  */
 #ifndef HERMES_PHILOX_REF_H
 #define HERMES_PHILOX_REF_H
@@ -36,31 +40,30 @@ static inline void hermes_philox4x32_10(const uint32_t ctr_in[4], uint32_t k0, u
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-/* 53-bit uniform in (0,1) from two 32-bit words */
-static inline double hermes_u53(uint32_t a, uint32_t b) {
-    uint64_t m = ((uint64_t)a << 21) | (uint64_t)(b >> 11);
-    return ((double)m + 0.5) * (1.0 / 9007199254740992.0);
-}
+/* uniform in (0,1) from one 32-bit word */
+static inline double hermes_u32(uint32_t w) { return ((double)w + 0.5) * (1.0 / 4294967296.0); }
 
-/* nine N(0,1) values for one quadrature point of one flux call */
-static inline void hermes_philox_normals9(unsigned long long seed, unsigned long long step, unsigned stage,
-                                          unsigned kind, unsigned long long site, unsigned pt, double G[9]) {
+/* six N(0,1) values for one quadrature point of one flux call: the diagonal
+ * (xx, yy, zz) and off-diagonal (xy, xz, yz) normals of the stress */
+static inline void hermes_philox_normals6(unsigned long long seed, unsigned long long step, unsigned stage,
+                                          unsigned kind, unsigned long long site, unsigned pt, double G[6]) {
     const double two_pi = 6.283185307179586476925286766559;
     uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-    double z[10];
-    for (unsigned sub = 0; sub < 5; ++sub) {
-        uint32_t ctr[4], o[4];
+    uint32_t w[8];
+    for (unsigned sub = 0; sub < 2; ++sub) {
+        uint32_t ctr[4];
         ctr[0] = (uint32_t)site;
         ctr[1] = (pt & 0xFFu) | ((kind & 0xFu) << 8) | ((sub & 0xFu) << 12) | ((stage & 0xFFFFu) << 16);
         ctr[2] = (uint32_t)step;
         ctr[3] = (uint32_t)(step >> 32);
-        hermes_philox4x32_10(ctr, k0, k1, o);
-        double u1 = hermes_u53(o[0], o[1]), u2 = hermes_u53(o[2], o[3]);
-        double r = sqrt(-2.0 * log(u1));
-        z[2 * sub] = r * cos(two_pi * u2);
-        z[2 * sub + 1] = r * sin(two_pi * u2);
+        hermes_philox4x32_10(ctr, k0, k1, w + 4 * sub);
     }
-    for (int i = 0; i < 9; ++i) G[i] = z[i];
+    for (int k = 0; k < 3; ++k) {
+        double u1 = hermes_u32(w[2 * k]), u2 = hermes_u32(w[2 * k + 1]);
+        double r = sqrt(-2.0 * log(u1));
+        G[2 * k] = r * cos(two_pi * u2);
+        G[2 * k + 1] = r * sin(two_pi * u2);
+    }
 }
 
 #endif

@@ -10,7 +10,8 @@ Each case stores: the input state Q0 (Fortran order Q(nx,ny,nz,nQ,nbasis)),
 the right-hand side of Q0 (limiter applied), the state after `steps` steps
 with the time and last time step, and the Config fields.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [case ...]
+(no arguments: every case; otherwise only the named ones)
 """
 import dataclasses
 import json
@@ -57,9 +58,11 @@ def config_json(cfg):
     return json.dumps(dataclasses.asdict(cfg), sort_keys=True)
 
 
-def main():
+def main(names=()):
     import oracle as O
     for name, (cfg, Q0, steps) in cases().items():
+        if names and name not in names:
+            continue
         o = O.Oracle(cfg)
         Q0 = np.asfortranarray(Q0)
         rhs = o.rhs(Q0.copy(order="F"), limit=True)
@@ -71,4 +74,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

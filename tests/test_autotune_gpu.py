@@ -19,15 +19,24 @@ def test_launch_defaults_and_validation():
     from hermeshd_gb300.solver import Solver
     s = Solver(config.sod_1d(nx=64))
     assert s.get_launch() == {"face_tpb": 128, "dt_tpb": 256, "steps_per_graph": 1, "noise_inline": 0,
-                              "face_traces": 0, "split_update": 1}
+                              "face_traces": 0, "split_update": 1, "tile_stage": 0}   # 1-D: no fused stage by default
     for bad in ({"face_tpb": 96}, {"face_tpb": 256}, {"dt_tpb": 48}, {"dt_tpb": 512}, {"steps_per_graph": 65}):
         with pytest.raises(HermesError):
             s.set_launch(**bad)
     s.set_launch(face_tpb=32, dt_tpb=64, steps_per_graph=4)
     assert s.get_launch() == {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 4, "noise_inline": 0,
-                              "face_traces": 0, "split_update": 1}
+                              "face_traces": 0, "split_update": 1, "tile_stage": 0}
     with pytest.raises(HermesError):   # no trace kernel for nbasis 4
         s.set_launch(face_traces=1)
+    s.set_launch(tile_stage=1)          # the fused stage exists for nbasis 4 and may be forced on
+    assert s.get_launch()["tile_stage"] == 1
+    s10 = Solver(config.isentropic_vortex_2d(n=8))
+    with pytest.raises(HermesError):   # no fused stage for nbasis 10
+        s10.set_launch(tile_stage=1)
+    s4 = Solver(config.fh_box(8, precision="fp32"))
+    assert s4.get_launch()["tile_stage"] == 0   # off by default, available for nbasis 4
+    s4.set_launch(tile_stage=1)
+    assert s4.get_launch()["tile_stage"] == 1
 
 
 @pytest.mark.parametrize("mk", [lambda: config.isentropic_vortex_2d(n=12),
@@ -45,7 +54,9 @@ def test_every_launch_shape_is_bit_identical(mk):
         shapes.append({"noise_inline": 1})
     for shape in shapes:
         s = Solver(cfg)
-        s.set_launch(**shape)
+        # the separate kernels' launch shapes (the fused stage, on by default
+        # for this box, has its own bit-identity tests in test_tile_gpu.py)
+        s.set_launch(**dict(shape, tile_stage=0) if s.get_launch()["tile_stage"] else shape)
         q, q1 = s.from_numpy(Q), s.new_state()
         t, dt = s.advance(q, q1, 7)
         out = (s.to_numpy(q), t, dt)
@@ -95,12 +106,13 @@ def test_autotune_resets_state_and_caches(tmp_path, monkeypatch):
     r = autotune.autotune(ens, q, steps=2, repeats=2)
     assert not r["cached"] and r["ms_per_step"] <= r["default_ms_per_step"]
     assert set(r["launch"]) == {"face_tpb", "dt_tpb", "steps_per_graph", "noise_inline", "face_traces",
-                                "split_update"}
+                                "split_update", "tile_stage"}
     assert ens.get_launch() == r["launch"]
     # tuning stepped copies of q; the context's time and noise counter are reset
     qa, qa1 = q.clone(), ens.new_state()
     ens.advance(qa, qa1, 5)
     fresh = Ensemble(base, dims, lengths, seeds=[0, 1, 2])
+    fresh.set_launch(**r["launch"])   # the fused stage and the separate kernels agree to rounding only
     qb, qb1 = q.clone(), fresh.new_state()
     fresh.advance(qb, qb1, 5)
     assert _torch().equal(qa, qb)
