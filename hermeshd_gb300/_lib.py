@@ -33,7 +33,8 @@ class HermesLaunch(C.Structure):
     """hermes_launch of include/hermes_gb300.h."""
     _fields_ = [("face_tpb", C.c_int32), ("dt_tpb", C.c_int32), ("steps_per_graph", C.c_int32),
                 ("noise_inline", C.c_int32), ("face_traces", C.c_int32), ("split_update", C.c_int32),
-                ("tile_stage", C.c_int32)]
+                ("tile_stage", C.c_int32), ("pdl", C.c_int32),
+                ("faces_merged", C.c_int32)]
 
 
 class HermesOutputUnits(C.Structure):

@@ -19,6 +19,10 @@ include/hermes_gb300.h):
 * ``split_update``     the cell update as the volume kernel plus a surface and
                        update kernel of one thread per (cell, variable) (1) or
                        one kernel (0); tuned where it exists (ivis 0/1);
+* ``pdl``              programmatic dependent launch of the step's kernels (1)
+                       or plain launches (0);
+* ``faces_merged``     the three face directions in one launch (1) or one
+                       launch each (0), starting from the context's default;
 * ``tile_stage``       each stage as one fused kernel over tiles of cells (1)
                        or the separate kernels (0); tried last, where the
                        context has it (nbasis 4, ivis 0/1).  With it on, only
@@ -48,6 +52,8 @@ KNOBS = {
     "noise_inline": (0, 1),          # tuned only with the stochastic stress on
     "face_traces": (1, 0),           # tuned only where the context has the trace buffer
     "split_update": (1, 0),          # tuned only where the context has the split-update buffer
+    "pdl": (0, 1),
+    "faces_merged": (1, 0),          # the context's default is tried first
     "tile_stage": (0, 1),            # tuned only where the context has the fused stage
 }
 
@@ -144,6 +150,8 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
             knobs.pop(k, None)
     if cur["tile_stage"] == 0 and not _can_tile(solver, cur):
         knobs.pop("tile_stage", None)
+    if "faces_merged" in knobs:
+        knobs["faces_merged"] = (cur["faces_merged"], 1 - cur["faces_merged"])
     qt, q1t = q.clone(), q.clone()
     best = {k: v[0] for k, v in knobs.items()}
     solver.set_launch(**best)

@@ -41,10 +41,31 @@ enum CellMode { MODE_RHS = 0, MODE_STAGE = 1 };
 struct Geom {
     const Box* boxes;
     int nbox;
+    int pdl;                  // launch the step kernels with programmatic dependent launch
     long long ncell;          // all boxes
     long long nface[3];       // all boxes, per direction
     long long face0_dir[3];   // faces of the directions before this one (staged face-noise layout)
+    // box of each chunk of 32 cells / faces of a direction (ensembles; null
+    // for one box): one load instead of a binary search over the boxes
+    const int* cbox;
+    const int* fbox[3];
 };
+
+// the box of global cell gc / face gf of direction DIR: the box of its
+// 32-element chunk's first element, stepped over boxes smaller than a chunk
+__device__ __forceinline__ int box_of_cell(const Geom& G, long long gc) {
+    if (!G.cbox) return find_box(G.boxes, G.nbox, gc, [](const Box& b) { return b.cell0; });
+    int bx = __ldg(G.cbox + (gc >> 5));
+    while (bx + 1 < G.nbox && G.boxes[bx + 1].cell0 <= gc) ++bx;
+    return bx;
+}
+template <int DIR>
+__device__ __forceinline__ int box_of_face(const Geom& G, long long gf) {
+    if (!G.fbox[DIR]) return find_box(G.boxes, G.nbox, gf, [](const Box& b) { return b.face0[DIR]; });
+    int bx = __ldg(G.fbox[DIR] + (gf >> 5));
+    while (bx + 1 < G.nbox && G.boxes[bx + 1].face0[DIR] <= gf) ++bx;
+    return bx;
+}
 
 // face tables of one direction and side (0 = minus face, 1 = plus face)
 template <class TB, int DIR, int SIDE>
@@ -303,10 +324,11 @@ __device__ __forceinline__ bool limit_bound_clear(const Phys& ph, const QA& q) {
 
 template <class T, class TB>
 __global__ void __launch_bounds__(LIMIT_TPB) k_limit(T* __restrict__ Q, Geom G, Phys ph) {
+    pdl_enter();
     constexpr int NB = TB::NB;
     long long gc = (long long)blockIdx.x * LIMIT_TPB + threadIdx.x;
     if (gc >= G.ncell) return;
-    int bx = find_box(G.boxes, G.nbox, gc, [](const Box& b) { return b.cell0; });
+    int bx = box_of_cell(G, gc);
     const Box& B = G.boxes[bx];
     const long long le = gc - B.cell0, nc = B.ncell;
     T* Qb = Q + B.q0;
@@ -426,7 +448,7 @@ template <class T, class TB, int DIR, int P, bool NOISE, bool TRB>
 __device__ __forceinline__ void face_point(const T* __restrict__ Q, T* __restrict__ flux, const FaceArgs& a, long long gf) {
     const Geom& G = a.G;
     const Phys& ph = a.ph;
-    int bx = find_box(G.boxes, G.nbox, gf, [](const Box& b) { return b.face0[DIR]; });
+    int bx = box_of_face<DIR>(G, gf);
     const Box& B = G.boxes[bx];
     const long long lf = gf - B.face0[DIR];
     const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
@@ -561,6 +583,7 @@ struct FaceMinBlocks {
 
 template <class T, class TB, int DIR, bool NOISE, bool TRB>
 __global__ void __launch_bounds__(FACE_TPB, (FaceMinBlocks<T>::value)) k_face(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
+    pdl_enter();
     long long gf = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gf >= a.G.nface[DIR]) return;
     const int p = blockIdx.y;
@@ -576,6 +599,7 @@ __global__ void __launch_bounds__(FACE_TPB, (FaceMinBlocks<T>::value)) k_face(co
 // the directions fill each other's tails.
 template <class T, class TB, bool NOISE, bool TRB>
 __global__ void __launch_bounds__(FACE_TPB, (FaceMinBlocks<T>::value)) k_faces(const T* __restrict__ Q, T* __restrict__ flux, FaceArgs a) {
+    pdl_enter();
     const long long gf = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int dir = blockIdx.z, p = blockIdx.y;
     if (gf >= a.G.nface[dir]) return;
@@ -1174,6 +1198,7 @@ struct CellMinBlocks {
 template <class T, class TB, bool NOISE, bool SPLIT>
 __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value))
     k_cell(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux, CellArgs a) {
+    pdl_enter();
     // Qin, Q0 and out may alias (the RK stages write in place); every element
     // is read before the thread that owns it writes it.
     constexpr int NB = TB::NB;
@@ -1188,7 +1213,7 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
     cx.act = gc < a.G.ncell;
     cx.bx = 0; cx.le = 0; cx.nc = 1;
     if (cx.act) {
-        cx.bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
+        cx.bx = box_of_cell(a.G, gc);
         cx.le = gc - a.G.boxes[cx.bx].cell0;
         cx.nc = a.G.boxes[cx.bx].ncell;
     }
@@ -1249,15 +1274,18 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
     if (cx.bad) a.flags[0] |= FLAG_NONFINITE;   // integrator.f90:234-250 (the reference exits)
 }
 
-// k_update: the second half of a split k_cell (ivis 0/1): a block of UPD_CPB
-// cells x NQ variables, thread (cell, variable).  r = surface sums - volume
-// terms, then the forward-Euler update (integrator.f90:147-149,171-174), the
-// RK combination and the NaN check of the cell average, as
-// cell_surface_update does.  With a.limit_out (FP64 stages whose output is the
-// next stage's input), the rh..en outputs of the block's cells go through
-// shared memory to the next stage's positivity limiter (k_limit's operations,
-// flux.f90:1077-1164), one thread per cell, before they are stored: the
-// reference limits that stage's input in place (integrator.f90:110).
+// k_update: the second half of a split k_cell (ivis 0/1).  r = surface sums
+// - volume terms, then the forward-Euler update (integrator.f90:147-149,171-174),
+// the RK combination and the NaN check of the cell average, as
+// cell_surface_update does.
+//
+// Without the limiter: thread per (cell, variable), blockIdx.y = variable.
+// With it (k_update_limit, FP64 stages whose output is the next stage's
+// input): a block of UPD_CPB cells x NQ variables whose rh..en outputs go
+// through shared memory to the next stage's positivity limiter (k_limit's
+// operations, flux.f90:1077-1164), one thread per cell, before they are
+// stored: the reference limits that stage's input in place (integrator.f90:110).
+constexpr int UPD_TPB = 128;
 constexpr int UPD_CPB = 16;
 
 // the limiter's full evaluation on rows in shared memory, out of line: the
@@ -1269,61 +1297,75 @@ __device__ __noinline__ void limit_rows_smem(const Phys& ph, T* p, int row, int 
     limit_cell<TB, T>(ph, q);
 }
 
+// the update of variable v of cell gc; a stage's rh..en outputs go to hyd
+// (the limiter's rows, stride hcol) instead of out when hyd is not null
 template <class T, class TB>
-__global__ void __launch_bounds__(UPD_CPB * NQ, 3) k_update(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux,
-                                                            CellArgs a) {
+__device__ __forceinline__ void update_cell_var(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux,
+                                                const CellArgs& a, long long gc, int v, T* hyd, int hcol) {
+    constexpr int NB = TB::NB;
+    const int bx = box_of_cell(a.G, gc);
+    const Box& B = a.G.boxes[bx];
+    const long long le = gc - B.cell0, nc = B.ncell, ncl = a.G.ncell;
+    long long fm[3], fp[3], nfd[3];
+    cell_faces(B, le, fm, fp, nfd);
+    const T* ab = static_cast<const T*>(a.accbuf);
+    T r[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) r[b] = -ab[((long long)v * NB + b) * ncl + gc];
+    surface_add<T, TB>(flux, B, fm, fp, nfd, v, r);
+    T* ob = out + B.q0;
+    if (a.mode == MODE_RHS) {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) ob[(long long)(b * NQ + v) * nc + le] = r[b];
+        return;
+    }
+    const T dt = T(a.st[bx].dt), faci = T(1) / (T(1) + dt * T(a.ph.coll));
+    const T* qb = Qin + B.q0;
+    const T* q0b = Q0 ? Q0 + B.q0 : nullptr;
+    const bool stress_faci = v >= PXX && a.ph.ivis == 1;
+    bool bad = false;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const long long ix = (long long)(b * NQ + v) * nc + le;
+        T e = qb[ix] - dt * r[b];
+        if (stress_faci) e = faci * e;
+        T o = e;
+        if (a.comb != COMB_NONE) o = rk_combine(a.comb, q0b[ix], o);
+        if (b == 0 && o != o) bad = true;
+        if (hyd && v < 5) hyd[(v * NB + b) * hcol] = o;
+        else ob[ix] = o;
+    }
+    if (bad) a.flags[0] |= FLAG_NONFINITE;
+}
+
+template <class T, class TB>
+__global__ void __launch_bounds__(UPD_TPB) k_update(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux,
+                                                   CellArgs a) {
+    pdl_enter();
+    const long long gc = (long long)blockIdx.x * UPD_TPB + threadIdx.x;
+    if (gc >= a.G.ncell) return;
+    update_cell_var<T, TB>(Qin, Q0, out, flux, a, gc, blockIdx.y, nullptr, 0);
+}
+
+template <class T, class TB>
+__global__ void __launch_bounds__(UPD_CPB * NQ, 3) k_update_limit(const T* Qin, const T* Q0, T* out,
+                                                                  const T* __restrict__ flux, CellArgs a) {
+    pdl_enter();
     constexpr int NB = TB::NB;
     __shared__ T hyd[5 * NB * UPD_CPB];                 // [variable][basis][cell of the block]
     const int lc = threadIdx.x, v = threadIdx.y;
     const long long gc = (long long)blockIdx.x * UPD_CPB + lc;
     const bool act = gc < a.G.ncell;
-    const bool lim = std::is_same<T, double>::value && a.limit_out && a.mode == MODE_STAGE;   // uniform
-    int bx = 0;
-    long long le = 0, nc = 1;
-    if (act) {
-        bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
-        const Box& B = a.G.boxes[bx];
-        le = gc - B.cell0;
-        nc = B.ncell;
-        const long long ncl = a.G.ncell;
-        long long fm[3], fp[3], nfd[3];
-        cell_faces(B, le, fm, fp, nfd);
-        const T* ab = static_cast<const T*>(a.accbuf);
-        T r[NB];
-#pragma unroll
-        for (int b = 0; b < NB; ++b) r[b] = -ab[((long long)v * NB + b) * ncl + gc];
-        surface_add<T, TB>(flux, B, fm, fp, nfd, v, r);
-        T* ob = out + B.q0;
-        if (a.mode == MODE_RHS) {
-#pragma unroll
-            for (int b = 0; b < NB; ++b) ob[(long long)(b * NQ + v) * nc + le] = r[b];
-            return;
-        }
-        const T dt = T(a.st[bx].dt), faci = T(1) / (T(1) + dt * T(a.ph.coll));
-        const T* qb = Qin + B.q0;
-        const T* q0b = Q0 ? Q0 + B.q0 : nullptr;
-        const bool stress_faci = v >= PXX && a.ph.ivis == 1;
-        bool bad = false;
-#pragma unroll
-        for (int b = 0; b < NB; ++b) {
-            const long long ix = (long long)(b * NQ + v) * nc + le;
-            T e = qb[ix] - dt * r[b];
-            if (stress_faci) e = faci * e;
-            T o = e;
-            if (a.comb != COMB_NONE) o = rk_combine(a.comb, q0b[ix], o);
-            if (b == 0 && o != o) bad = true;
-            if (lim && v < 5) hyd[(v * NB + b) * UPD_CPB + lc] = o;
-            else ob[ix] = o;
-        }
-        if (bad) a.flags[0] |= FLAG_NONFINITE;
-    }
-    if (!lim) return;
+    if (act) update_cell_var<T, TB>(Qin, Q0, out, flux, a, gc, v, hyd + lc, UPD_CPB);
     __syncthreads();
     if (v != 0 || !act) return;
     StridedRows<T> q{hyd + lc, NB * UPD_CPB, UPD_CPB};
     if (!(q[RH][0] >= T(a.ph.rh_floor) && limit_bound_clear<TB, T>(a.ph, q)))
         limit_rows_smem<TB, T>(a.ph, hyd + lc, NB * UPD_CPB, UPD_CPB);
-    T* ob = out + a.G.boxes[bx].q0;
+    const int bx = box_of_cell(a.G, gc);
+    const Box& B = a.G.boxes[bx];
+    const long long le = gc - B.cell0, nc = B.ncell;
+    T* ob = out + B.q0;
 #pragma unroll
     for (int w = 0; w < 5; ++w)
 #pragma unroll
@@ -1342,12 +1384,13 @@ struct DtArgs {
 
 template <class T>
 __global__ void __launch_bounds__(DT_TPB) k_mindt(const T* __restrict__ Q, DtArgs a) {
+    pdl_enter();
     const long long gc = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = gc < a.G.ncell;
     int bx = 0;
     double vmag0 = 0.0;
     if (act) {
-        bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
+        bx = box_of_cell(a.G, gc);
         const Box& B = a.G.boxes[bx];
         const long long le = gc - B.cell0, nc = B.ncell;
         const T* Qb = Q + B.q0;

@@ -48,13 +48,13 @@ struct TileLaunch {
         if (ntiles == 0) return;
         TileArgs b = a;
         b.fmax = FMAX;
-        k_tile<T, TB, NOISE><<<ntiles, TILE_NT, smem(), s>>>(static_cast<const T*>(Qin), static_cast<const T*>(Q0),
-                                                            static_cast<T*>(out), b);
+        launch_k(a.c.G.pdl, k_tile<T, TB, NOISE>, ntiles, TILE_NT, smem(), s, static_cast<const T*>(Qin),
+                 static_cast<const T*>(Q0), static_cast<T*>(out), b);
     }
     static void mindt_limit(void* Q, const DtArgs& a, cudaStream_t s) {
         if (a.G.ncell <= 0) return;
         const unsigned nb = (unsigned)((a.G.ncell + DT_TPB - 1) / DT_TPB);
-        k_mindt_limit<T, TB><<<nb, DT_TPB, 0, s>>>(static_cast<T*>(Q), a);
+        launch_k(a.G.pdl, k_mindt_limit<T, TB>, nb, DT_TPB, 0, s, static_cast<T*>(Q), a);
     }
 };
 
@@ -85,16 +85,16 @@ struct Launch {
     static void limit(void* Q, const Geom& G, const Phys& ph, cudaStream_t s) {
         if (G.ncell <= 0) return;
         const unsigned nb = (unsigned)((G.ncell + LIMIT_TPB - 1) / LIMIT_TPB);
-        k_limit<T, TB><<<nb, LIMIT_TPB, 0, s>>>(static_cast<T*>(Q), G, ph);
+        launch_k(G.pdl, k_limit<T, TB>, nb, LIMIT_TPB, 0, s, static_cast<T*>(Q), G, ph);
     }
     // the trace-buffer face kernels exist for the FP64 path of nbasis 8 and 10
     // without the stochastic stress
     static constexpr bool HAS_TRACE = std::is_same<T, double>::value && NB >= 8;
     template <bool NOISE, bool TRB>
     static void face_dirs(int dir, dim3 grid, int tpb, const T* q, T* f, const FaceArgs& a, cudaStream_t s) {
-        if (dir == 0) k_face<T, TB, 0, NOISE, TRB><<<grid, tpb, 0, s>>>(q, f, a);
-        else if (dir == 1) k_face<T, TB, 1, NOISE, TRB><<<grid, tpb, 0, s>>>(q, f, a);
-        else k_face<T, TB, 2, NOISE, TRB><<<grid, tpb, 0, s>>>(q, f, a);
+        if (dir == 0) launch_k(a.G.pdl, k_face<T, TB, 0, NOISE, TRB>, grid, tpb, 0, s, q, f, a);
+        else if (dir == 1) launch_k(a.G.pdl, k_face<T, TB, 1, NOISE, TRB>, grid, tpb, 0, s, q, f, a);
+        else launch_k(a.G.pdl, k_face<T, TB, 2, NOISE, TRB>, grid, tpb, 0, s, q, f, a);
     }
     template <bool NOISE>
     static void face(int dir, const void* Q, void* flux, const FaceArgs& a, cudaStream_t s) {
@@ -107,11 +107,11 @@ struct Launch {
             if (n <= 0) return;
             const dim3 grid((unsigned)((n + tpb - 1) / tpb), TB::NF, 3);
             if constexpr (HAS_TRACE && !NOISE) {
-                if (a.traces) { k_faces<T, TB, NOISE, true><<<grid, tpb, 0, s>>>(q, f, a); return; }
+                if (a.traces) { launch_k(a.G.pdl, k_faces<T, TB, NOISE, true>, grid, tpb, 0, s, q, f, a); return; }
             }
             FaceArgs b = a;
             b.traces = nullptr;
-            k_faces<T, TB, NOISE, false><<<grid, tpb, 0, s>>>(q, f, b);
+            launch_k(a.G.pdl, k_faces<T, TB, NOISE, false>, grid, tpb, 0, s, q, f, b);
             return;
         }
         const long long n = a.G.nface[dir];
@@ -128,7 +128,7 @@ struct Launch {
         if constexpr (HAS_TRACE) {
             if (G.ncell <= 0) return;
             dim3 grid((unsigned)((G.ncell + TRACE_TPB - 1) / TRACE_TPB), 3 * NQ);
-            k_trace<T, TB><<<grid, TRACE_TPB, 0, s>>>(static_cast<const T*>(Q), static_cast<T*>(tr), G);
+            launch_k(G.pdl, k_trace<T, TB>, grid, TRACE_TPB, 0, s, static_cast<const T*>(Q), static_cast<T*>(tr), G);
         }
     }
     template <bool NOISE>
@@ -141,24 +141,31 @@ struct Launch {
         const T* f = static_cast<const T*>(flux);
         if constexpr (has_split<NOISE>()) {
             if (a.accbuf && a.ph.ivis < 2 && !a.split_source) {
-                k_cell<T, TB, NOISE, true><<<nb, 2 * CELL_CPB, cell_smem(), s>>>(qi, q0, o, f, a);
-                const unsigned ub = (unsigned)((a.G.ncell + UPD_CPB - 1) / UPD_CPB);
-                k_update<T, TB><<<ub, dim3(UPD_CPB, NQ), 0, s>>>(qi, q0, o, f, a);
+                launch_k(a.G.pdl, k_cell<T, TB, NOISE, true>, nb, 2 * CELL_CPB, cell_smem(), s, qi, q0, o, f, a);
+                if constexpr (std::is_same<T, double>::value) {
+                    if (a.limit_out && a.mode == MODE_STAGE) {
+                        const unsigned ub = (unsigned)((a.G.ncell + UPD_CPB - 1) / UPD_CPB);
+                        launch_k(a.G.pdl, k_update_limit<T, TB>, ub, dim3(UPD_CPB, NQ), 0, s, qi, q0, o, f, a);
+                        return;
+                    }
+                }
+                const dim3 grid((unsigned)((a.G.ncell + UPD_TPB - 1) / UPD_TPB), NQ);
+                launch_k(a.G.pdl, k_update<T, TB>, grid, UPD_TPB, 0, s, qi, q0, o, f, a);
                 return;
             }
         }
-        k_cell<T, TB, NOISE, false><<<nb, 2 * CELL_CPB, cell_smem(), s>>>(qi, q0, o, f, a);
+        launch_k(a.G.pdl, k_cell<T, TB, NOISE, false>, nb, 2 * CELL_CPB, cell_smem(), s, qi, q0, o, f, a);
     }
     static void mindt_limit(void* Q, const DtArgs& a, cudaStream_t s) {
         if (a.G.ncell <= 0) return;
         const unsigned nb = (unsigned)((a.G.ncell + DT_TPB - 1) / DT_TPB);
-        k_mindt_limit<T, TB><<<nb, DT_TPB, 0, s>>>(static_cast<T*>(Q), a);
+        launch_k(a.G.pdl, k_mindt_limit<T, TB>, nb, DT_TPB, 0, s, static_cast<T*>(Q), a);
     }
     static void mindt(const void* Q, const DtArgs& a, cudaStream_t s) {
         if (a.G.ncell <= 0) return;
         const int tpb = a.tpb > 0 ? a.tpb : DT_TPB;
         const unsigned nb = (unsigned)((a.G.ncell + tpb - 1) / tpb);
-        k_mindt<T><<<nb, tpb, 0, s>>>(static_cast<const T*>(Q), a);
+        launch_k(a.G.pdl, k_mindt<T>, nb, tpb, 0, s, static_cast<const T*>(Q), a);
     }
 };
 

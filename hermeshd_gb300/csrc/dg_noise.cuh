@@ -33,12 +33,13 @@ struct NoiseArgs {
 // grid (cells / NOISE_TPB, 3 NPG): blockIdx.y = d * NPG + g
 template <class T, class TB>
 __global__ void __launch_bounds__(NOISE_TPB) k_noise_cell(T* __restrict__ out, NoiseArgs a) {
+    pdl_enter();
     const long long ncl = a.G.ncell;
     const long long gc = (long long)blockIdx.x * NOISE_TPB + threadIdx.x;
     if (gc >= ncl) return;
     const int r = blockIdx.y;
     const int d = r / TB::NPG, g = r % TB::NPG;
-    const int bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
+    const int bx = box_of_cell(a.G, gc);
     const Box& B = a.G.boxes[bx];
     T S[6];
     random_stress<T>(a.ph, B.seed, NoiseCtr{*a.step, a.stage}, 3 + d, (unsigned long long)(gc - B.cell0), g, S);
@@ -49,12 +50,13 @@ __global__ void __launch_bounds__(NOISE_TPB) k_noise_cell(T* __restrict__ out, N
 // grid (faces / NOISE_TPB, 2 NF): blockIdx.y = side * NF + P
 template <class T, class TB, int DIR>
 __global__ void __launch_bounds__(NOISE_TPB) k_noise_face(T* __restrict__ out, NoiseArgs a) {
+    pdl_enter();
     const long long nfa = a.G.nface[DIR];
     const long long gf = (long long)blockIdx.x * NOISE_TPB + threadIdx.x;
     if (gf >= nfa) return;
     const int r = blockIdx.y;
     const int P = r % TB::NF, side = r / TB::NF;
-    const int bx = find_box(a.G.boxes, a.G.nbox, gf, [](const Box& b) { return b.face0[DIR]; });
+    const int bx = box_of_face<DIR>(a.G, gf);
     const Box& B = a.G.boxes[bx];
     T S[6];
     random_stress<T>(a.ph, B.seed, NoiseCtr{*a.step, a.stage}, DIR, (unsigned long long)(gf - B.face0[DIR]),
@@ -69,13 +71,17 @@ cudaError_t noise_launch(void* cellbuf, void* facebuf, const NoiseArgs& a, cudaS
     using TB = hermes_tab::Tab<NB, NQD>;
     auto blocks = [](long long n) { return (unsigned)((n + NOISE_TPB - 1) / NOISE_TPB); };
     if (a.G.ncell > 0)
-        k_noise_cell<T, TB><<<dim3(blocks(a.G.ncell), 3 * TB::NPG), NOISE_TPB, 0, s>>>(static_cast<T*>(cellbuf), a);
+        launch_k(a.G.pdl, k_noise_cell<T, TB>, dim3(blocks(a.G.ncell), 3 * TB::NPG), NOISE_TPB, 0, s,
+                 static_cast<T*>(cellbuf), a);
     if (a.G.nface[0] > 0)
-        k_noise_face<T, TB, 0><<<dim3(blocks(a.G.nface[0]), 2 * TB::NF), NOISE_TPB, 0, s>>>(static_cast<T*>(facebuf), a);
+        launch_k(a.G.pdl, k_noise_face<T, TB, 0>, dim3(blocks(a.G.nface[0]), 2 * TB::NF), NOISE_TPB, 0, s,
+                 static_cast<T*>(facebuf), a);
     if (a.G.nface[1] > 0)
-        k_noise_face<T, TB, 1><<<dim3(blocks(a.G.nface[1]), 2 * TB::NF), NOISE_TPB, 0, s>>>(static_cast<T*>(facebuf), a);
+        launch_k(a.G.pdl, k_noise_face<T, TB, 1>, dim3(blocks(a.G.nface[1]), 2 * TB::NF), NOISE_TPB, 0, s,
+                 static_cast<T*>(facebuf), a);
     if (a.G.nface[2] > 0)
-        k_noise_face<T, TB, 2><<<dim3(blocks(a.G.nface[2]), 2 * TB::NF), NOISE_TPB, 0, s>>>(static_cast<T*>(facebuf), a);
+        launch_k(a.G.pdl, k_noise_face<T, TB, 2>, dim3(blocks(a.G.nface[2]), 2 * TB::NF), NOISE_TPB, 0, s,
+                 static_cast<T*>(facebuf), a);
     return cudaGetLastError();
 }
 

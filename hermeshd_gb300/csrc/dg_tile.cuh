@@ -266,6 +266,7 @@ __host__ __device__ constexpr bool volume_terms_one_direction() {
 template <class T, class TB, bool NOISE>
 __global__ void __launch_bounds__(TILE_NT, (TileMinBlocks<T>::value))
     k_tile(const T* __restrict__ Qin, const T* Q0, T* out, TileArgs ta) {
+    pdl_enter();
     constexpr int NB = TB::NB, NF = TB::NF;
     static_assert(volume_terms_one_direction<TB>(), "the fused stage folds the volume terms one direction at a time");
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -480,6 +481,7 @@ __global__ void __launch_bounds__(TILE_NT, (TileMinBlocks<T>::value))
 // as the reference's step computes dt before euler_step limits Q.
 template <class T, class TB>
 __global__ void __launch_bounds__(DT_TPB) k_mindt_limit(T* __restrict__ Q, DtArgs a) {
+    pdl_enter();
     constexpr int NB = TB::NB;
     const long long gc = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = gc < a.G.ncell;
@@ -489,7 +491,7 @@ __global__ void __launch_bounds__(DT_TPB) k_mindt_limit(T* __restrict__ Q, DtArg
     long long le = 0, nc = 1;
     T* Qb = Q;
     if (act) {
-        bx = find_box(a.G.boxes, a.G.nbox, gc, [](const Box& b) { return b.cell0; });
+        bx = box_of_cell(a.G, gc);
         const Box& B = a.G.boxes[bx];
         le = gc - B.cell0;
         nc = B.ncell;

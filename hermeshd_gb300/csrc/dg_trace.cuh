@@ -63,9 +63,10 @@ __device__ __forceinline__ void trace_cell(const T* __restrict__ Qb, long long n
 // blockIdx.y = direction * NQ + variable
 template <class T, class TB>
 __global__ void __launch_bounds__(TRACE_TPB) k_trace(const T* __restrict__ Q, T* __restrict__ tr, Geom G) {
+    pdl_enter();
     const long long gc = (long long)blockIdx.x * TRACE_TPB + threadIdx.x;
     if (gc >= G.ncell) return;
-    const int bx = find_box(G.boxes, G.nbox, gc, [](const Box& b) { return b.cell0; });
+    const int bx = box_of_cell(G, gc);
     const Box& B = G.boxes[bx];
     const T* Qb = Q + B.q0;
     const long long le = gc - B.cell0;

@@ -50,6 +50,7 @@ __global__ void k_set_step(unsigned long long* step, unsigned long long s) {
 }
 // dt = cflm / ((vmag + cs_last) * dxi); t += dt; one thread per box
 __global__ void k_dt_finalize(const Box* __restrict__ boxes, int nbox, BoxState* st, unsigned long long* step) {
+    pdl_enter();
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b == 0) { step[0] = step[1]; step[1] = step[1] + 1; }
     if (b >= nbox) return;
@@ -163,7 +164,9 @@ struct hermes_ctx {
     void* d_qs = nullptr;
     bool tile_stage = false;
     bool tile_ok_default = false;   // the autotuner tries the fused stage here
-    // the three face directions in one launch (k_faces)
+    // box lookup tables of an ensemble (Geom.cbox, Geom.fbox)
+    int* d_boxtab = nullptr;
+    // the three face directions in one launch (k_faces): FP64 by default
     bool faces_merged = true;
     // adjoint scratch, allocated on first use
     AdjFn adj = nullptr;
@@ -387,7 +390,9 @@ void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, un
 }
 
 // the limiter fused into the CFL reduction and into k_update: FP64 with the
-// split update (the separate kernels otherwise)
+// split update (the separate kernels otherwise: in FP32 the block layout of
+// the limiting update kernel measured ~10 % slower on the ensemble step than
+// k_update plus k_limit)
 bool fused_limiter(const hermes_ctx* c) {
     return c->split_update && c->K.elem_size == (int)sizeof(double) && c->cfg.ivis < 2 && c->K.mindt_limit_any &&
            (c->cfg.ieos == 1 || c->cfg.ieos == 2);
@@ -397,7 +402,7 @@ void enq_mindt(hermes_ctx* c, const void* q, bool advance) {
     ProfScope ps(c, 0);
     c->K.mindt(q, a, c->stream);
     const int nb = c->G.nbox, tpb = 128;
-    if (advance) k_dt_finalize<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st, c->d_step);
+    if (advance) launch_k(c->G.pdl, k_dt_finalize, (nb + tpb - 1) / tpb, tpb, 0, c->stream, (const Box*)c->d_boxes, nb, c->d_st, c->d_step);
     else k_dt_finalize_only<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st);
 }
 // a step of fused stages: the CFL reduction with the first stage's limiter,
@@ -410,7 +415,7 @@ void enq_step_tile(hermes_ctx* c, void* q, void* q1) {
         ProfScope ps(c, 0);
         c->K.mindt_limit(q, a, c->stream);          // hermeshd.f90:59 get_min_dt, then limiter(Q)
         const int nb = c->G.nbox, tpb = 128;
-        k_dt_finalize<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st, c->d_step);
+        launch_k(c->G.pdl, k_dt_finalize, (nb + tpb - 1) / tpb, tpb, 0, c->stream, (const Box*)c->d_boxes, nb, c->d_st, c->d_step);
     }
     enq_tile(c, q, nullptr, q1, MODE_STAGE, COMB_NONE, 0, 1);          // Q_1 = lim(E(Q))
     if (c->cfg.iorder == 3) {
@@ -434,7 +439,7 @@ void enq_step(hermes_ctx* c, void* q, void* q1) {
         ProfScope ps(c, 0);
         c->K.mindt_limit_any(q, a, c->stream);
         const int nb = c->G.nbox, tpb = 128;
-        k_dt_finalize<<<(nb + tpb - 1) / tpb, tpb, 0, c->stream>>>(c->d_boxes, nb, c->d_st, c->d_step);
+        launch_k(c->G.pdl, k_dt_finalize, (nb + tpb - 1) / tpb, tpb, 0, c->stream, (const Box*)c->d_boxes, nb, c->d_st, c->d_step);
     } else {
         enq_mindt(c, q, true);                                   // hermeshd.f90:59
     }
@@ -537,6 +542,11 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     long long ncell, nface[3];
     make_boxes(*cfg, nbox, dims, lengths, seeds, c->K.nf, c->h_boxes, c->h_len, ncell, nface, c->q_elems, c->flux_elems);
     c->G.nbox = nbox;
+    // one launch for the three face directions: measured faster in FP64 (the
+    // directions fill each other's tails), slower in FP32 (the merged kernel
+    // spills under FP32's register cap)
+    c->faces_merged = cfg->precision == 64;
+    c->G.pdl = 0;   // programmatic dependent launch measured neutral here: an autotuned option
     c->G.ncell = ncell;
     for (int d = 0; d < 3; ++d) c->G.nface[d] = nface[d];
     c->G.face0_dir[0] = 0;
@@ -560,6 +570,35 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
         return bail(HERMES_ERR_ALLOC);
     }
     c->G.boxes = c->d_boxes;
+    if (nbox > 1) {
+        // the box of each chunk of 32 cells and of 32 faces per direction
+        std::vector<int> tab;
+        auto build = [&](auto first, long long n) {
+            const long long nch = (n + 31) / 32;
+            int b = 0;
+            for (long long k = 0; k < nch; ++k) {
+                while (b + 1 < nbox && first(c->h_boxes[b + 1]) <= 32 * k) ++b;
+                tab.push_back(b);
+            }
+            return nch;
+        };
+        const long long nc = build([](const Box& b) { return b.cell0; }, ncell);
+        long long nf[3];
+        nf[0] = build([](const Box& b) { return b.face0[0]; }, nface[0]);
+        nf[1] = build([](const Box& b) { return b.face0[1]; }, nface[1]);
+        nf[2] = build([](const Box& b) { return b.face0[2]; }, nface[2]);
+        if (cudaMalloc(&c->d_boxtab, sizeof(int) * tab.size()) == cudaSuccess &&
+            cudaMemcpy(c->d_boxtab, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice) == cudaSuccess) {
+            c->G.cbox = c->d_boxtab;
+            c->G.fbox[0] = c->G.cbox + nc;
+            c->G.fbox[1] = c->G.fbox[0] + nf[0];
+            c->G.fbox[2] = c->G.fbox[1] + nf[1];
+        } else {
+            cudaGetLastError();   // no room: the kernels search the boxes
+            cudaFree(c->d_boxtab);
+            c->d_boxtab = nullptr;
+        }
+    }
     if (cfg->llns && noise_launcher(cfg->precision, cfg->nbasis, &c->noise_fn)) {
         // staged stochastic stress: 18 NPG values per cell, 12 NF per face
         const size_t npg = (size_t)c->K.nqd * c->K.nqd * c->K.nqd, nf = (size_t)c->K.nf;
@@ -697,6 +736,7 @@ int hermes_destroy(hermes_ctx* c) {
     cudaFree(c->d_accbuf);
     cudaFree(c->d_tile0);
     cudaFree(c->d_qs);
+    cudaFree(c->d_boxtab);
     delete c;
     return HERMES_OK;
 }
@@ -921,8 +961,11 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     if (l->tile_stage == 1 && !c->d_tile0)
         return fail(c, HERMES_ERR_ARG, "the fused stage needs nbasis 4, ivis 0/1 and room for a third state");
     const bool tile = l->tile_stage == 1;
+    if (l->pdl != 0 && l->pdl != 1) return fail(c, HERMES_ERR_ARG, "pdl must be 0 or 1");
+    if (l->faces_merged != 0 && l->faces_merged != 1) return fail(c, HERMES_ERR_ARG, "faces_merged must be 0 or 1");
     if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged || traces != c->face_traces ||
-        split != c->split_update || tile != c->tile_stage) {
+        split != c->split_update || tile != c->tile_stage || l->pdl != c->G.pdl ||
+        (l->faces_merged == 1) != c->faces_merged) {
         // captured graphs hold the old launch shape
         HCK(c, cudaSetDevice(c->device));
         HCK(c, cudaStreamSynchronize(c->stream));
@@ -935,6 +978,8 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     c->face_traces = traces;
     c->split_update = split;
     c->tile_stage = tile;
+    c->G.pdl = l->pdl;
+    c->faces_merged = l->faces_merged == 1;
     return HERMES_OK;
 }
 
@@ -947,6 +992,8 @@ int hermes_get_launch(hermes_ctx* c, hermes_launch* l) {
     l->face_traces = c->face_traces ? 1 : 0;
     l->split_update = c->split_update ? 1 : 0;
     l->tile_stage = c->tile_stage ? 1 : 0;
+    l->pdl = c->G.pdl;
+    l->faces_merged = c->faces_merged ? 1 : 0;
     return HERMES_OK;
 }
 

@@ -4,6 +4,8 @@
 // with cell = i + nx*(j + ny*k).  An ensemble stores its boxes back to back.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <type_traits>
 #include <utility>
@@ -92,5 +94,36 @@ __device__ __forceinline__ int find_box(const Box* __restrict__ boxes, int nbox,
 
 template <class T>
 __device__ __forceinline__ T tfma(T a, T b, T c) { return fma(a, b, c); }
+
+// Programmatic dependent launch: a step kernel launched with the
+// programmatic-serialisation attribute may start while the kernel before it
+// in the stream finishes.  It waits for that kernel's completion and memory
+// (griddepcontrol.wait) before its first global memory access, and lets the
+// kernel after it start launching (griddepcontrol.launch_dependents), which
+// overlaps each launch with the previous kernel's tail.  Without the
+// attribute both instructions do nothing.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// launch a step kernel, with the programmatic-serialisation attribute when
+// pdl is set (the kernel then begins with pdl_enter); errors are left for
+// cudaGetLastError, as with <<<>>>
+template <class... KArgs, class... Args>
+inline void launch_k(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                     Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    (void)cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 }  // namespace hermes

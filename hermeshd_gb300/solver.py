@@ -176,15 +176,18 @@ class Solver:
         check(lib().hermes_get_launch(self.ctx, C.byref(l)), self.ctx)
         return {"face_tpb": l.face_tpb, "dt_tpb": l.dt_tpb, "steps_per_graph": l.steps_per_graph,
                 "noise_inline": l.noise_inline, "face_traces": l.face_traces, "split_update": l.split_update,
-                "tile_stage": l.tile_stage}
+                "tile_stage": l.tile_stage, "pdl": l.pdl,
+                "faces_merged": l.faces_merged}
 
     def set_launch(self, face_tpb: int = 0, dt_tpb: int = 0, steps_per_graph: int = 1, noise_inline: int = 0,
-                   face_traces=None, split_update=None, tile_stage=None):
+                   face_traces=None, split_update=None, tile_stage=None, pdl=None,
+                   faces_merged=None):
         """face_traces / split_update / tile_stage None keep the context's
         current choice (the trace kernel and the split update are on by
         default where they exist: FP64 nbasis 8/10 without the stochastic
         stress, and ivis 0/1; the fused stage, nbasis 4 ivis 0/1, is off by
-        default)."""
+        default); pdl None keeps the current choice (off by default); faces_merged None keeps
+        the current choice (on by default in FP64, off in FP32)."""
         cur = self.get_launch()
         if face_traces is None:
             face_traces = cur["face_traces"]
@@ -192,8 +195,12 @@ class Solver:
             split_update = cur["split_update"]
         if tile_stage is None:
             tile_stage = cur["tile_stage"]
+        if pdl is None:
+            pdl = cur["pdl"]
+        if faces_merged is None:
+            faces_merged = cur["faces_merged"]
         l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), int(noise_inline), int(face_traces),
-                              int(split_update), int(tile_stage))
+                              int(split_update), int(tile_stage), int(pdl), int(faces_merged))
         check(lib().hermes_set_launch(self.ctx, C.byref(l)), self.ctx)
 
     def set_noise_step(self, step: int):

@@ -231,6 +231,13 @@ typedef struct hermes_launch {
                                 (a third state is allocated at creation).  Off by default: slower
                                 than the separate kernels on the measured workloads; the autotuner
                                 tries it.  0: the separate kernels.  Equal to rounding. */
+    int32_t pdl;             /* 1: the step's kernels use programmatic dependent launch (each may
+                                start launching while the one before it finishes, and waits for its
+                                results before touching memory); 0 (default, measured neutral on
+                                the benchmarked step): plain launches.  Bit-identical. */
+    int32_t faces_merged;    /* 1: the face fluxes of the three directions in one launch (the default
+                                in FP64, where the directions fill each other's tails); 0: one
+                                launch per direction (the default in FP32).  Bit-identical. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
 int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);
