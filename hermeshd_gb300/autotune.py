@@ -21,8 +21,10 @@ include/hermes_gb300.h):
                        one kernel (0); tuned where it exists (ivis 0/1);
 * ``pdl``              programmatic dependent launch of the step's kernels (1)
                        or plain launches (0);
-* ``faces_merged``     the three face directions in one launch (1) or one
-                       launch each (0), starting from the context's default;
+* ``faces_merged``     the face kernels: the three directions in one launch
+                       (1), one launch each with a thread per face point (0),
+                       or one launch each with a thread per face looping
+                       over its points (2); the context's default first;
 * ``tile_stage``       each stage as one fused kernel over tiles of cells (1)
                        or the separate kernels (0); tried last, where the
                        context has it (nbasis 4, ivis 0/1).  With it on, only
@@ -151,7 +153,7 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
     if cur["tile_stage"] == 0 and not _can_tile(solver, cur):
         knobs.pop("tile_stage", None)
     if "faces_merged" in knobs:
-        knobs["faces_merged"] = (cur["faces_merged"], 1 - cur["faces_merged"])
+        knobs["faces_merged"] = (cur["faces_merged"],) + tuple(m for m in (0, 1, 2) if m != cur["faces_merged"])
     qt, q1t = q.clone(), q.clone()
     best = {k: v[0] for k, v in knobs.items()}
     solver.set_launch(**best)

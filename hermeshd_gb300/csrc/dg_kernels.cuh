@@ -372,6 +372,7 @@ struct FaceArgs {
     int tpb;                         // faces per block (32, 64 or 128; 0 = FACE_TPB)
     const void* noise;               // staged stochastic stress of the faces (k_noise_face), or null: drawn here
     const void* traces;              // face traces of every cell (k_trace), or null: evaluated here
+    int point_loop;                  // one thread per face looping over its points (k_face_pl)
 };
 
 // where k_face takes the traces of its two cells from: evaluated from the

@@ -116,6 +116,14 @@ struct Launch {
         }
         const long long n = a.G.nface[dir];
         if (n <= 0) return;
+        if (a.point_loop && !a.noise && !a.traces) {
+            // one thread per face, its points in a loop (k_face_pl)
+            const unsigned g = (unsigned)((n + tpb - 1) / tpb);
+            if (dir == 0) launch_k(a.G.pdl, k_face_pl<T, TB, 0, NOISE>, g, tpb, 0, s, q, f, a);
+            else if (dir == 1) launch_k(a.G.pdl, k_face_pl<T, TB, 1, NOISE>, g, tpb, 0, s, q, f, a);
+            else launch_k(a.G.pdl, k_face_pl<T, TB, 2, NOISE>, g, tpb, 0, s, q, f, a);
+            return;
+        }
         dim3 grid((unsigned)((n + tpb - 1) / tpb), TB::NF);
         if constexpr (HAS_TRACE && !NOISE) {
             if (a.traces) { face_dirs<NOISE, true>(dir, grid, tpb, q, f, a, s); return; }

@@ -98,9 +98,10 @@ __device__ __forceinline__ void trace_rt(const T* __restrict__ Qb, long long nc,
 // the numerical flux at face point P of the face with coordinates fc (the
 // DIR coordinate is the face plane 0..n) of box B, scaled by the inverse
 // spacing: the same operations as face_point (dg_kernels.cuh), with the
-// point chosen at run time
-template <class T, class TB, int DIR, bool NOISE>
-__device__ __forceinline__ void tile_face_flux(const T* __restrict__ Q, const CellArgs& a, const Box& B, const int fc[3],
+// point chosen at run time and the stochastic stress drawn in place.  Args:
+// CellArgs or FaceArgs (ph, step, stage)
+template <class T, class TB, int DIR, bool NOISE, class Args>
+__device__ __forceinline__ void tile_face_flux(const T* __restrict__ Q, const Args& a, const Box& B, const int fc[3],
                                                int P, T F[NQ]) {
     const Phys& ph = a.ph;
     constexpr int NF = TB::NF;
@@ -205,6 +206,35 @@ __device__ __forceinline__ void tile_face_flux(const T* __restrict__ Q, const Ce
         rho_i_last = T(1) / rlast;
     }
     face_flux_fn<T, DIR>(ph, qL, qR, SL, SR, rho_i_last, F, T(B.di[DIR]));
+}
+
+// k_face_pl: the face fluxes of one direction, one thread per face looping
+// over the face's points at run time (blockIdx.y = 1).  Only the trace
+// evaluation is instantiated per point, so the body exists once (the point
+// per block of k_face instantiates it NF times) and the face's set-up (box,
+// coordinates, boundary kind) is done once for its points.  The stochastic
+// stress is drawn in place; the same operations as k_face, so the same bits.
+template <class T, class TB, int DIR, bool NOISE>
+__global__ void __launch_bounds__(FACE_TPB, (FaceMinBlocks<T>::value)) k_face_pl(const T* __restrict__ Q, T* __restrict__ flux,
+                                                                              FaceArgs a) {
+    pdl_enter();
+    const long long gf = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gf >= a.G.nface[DIR]) return;
+    const int bx = box_of_face<DIR>(a.G, gf);
+    const Box& B = a.G.boxes[bx];
+    const long long lf = gf - B.face0[DIR];
+    const int ex = DIR == 0 ? B.nfp[0] : B.n[0], ey = DIR == 1 ? B.nfp[1] : B.n[1];
+    const unsigned lfu = (unsigned)lf, t = lfu / (unsigned)ex;   // fewer than 2^31 faces per box
+    const int fc[3] = {(int)(lfu - t * (unsigned)ex), (int)(t % (unsigned)ey), (int)(t / (unsigned)ey)};
+    const long long nfd = (long long)ex * ey * (DIR == 2 ? B.nfp[2] : B.n[2]);
+    T* fb = flux + B.fbase[DIR];
+#pragma unroll 1
+    for (int P = 0; P < TB::NF; ++P) {
+        T F[NQ];
+        tile_face_flux<T, TB, DIR, NOISE>(Q, a, B, fc, P, F);
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) fb[(long long)(v * TB::NF + P) * nfd + lf] = F[v];
+    }
 }
 
 // resident tiles per SM: one (no register cap: at two per SM, FP32's 128

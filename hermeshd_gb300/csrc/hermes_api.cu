@@ -166,8 +166,10 @@ struct hermes_ctx {
     bool tile_ok_default = false;   // the autotuner tries the fused stage here
     // box lookup tables of an ensemble (Geom.cbox, Geom.fbox)
     int* d_boxtab = nullptr;
-    // the three face directions in one launch (k_faces): FP64 by default
-    bool faces_merged = true;
+    // face kernels: 0 one launch per direction, thread per (face, point)
+    // (k_face); 1 the three directions in one launch (k_faces); 2 one launch
+    // per direction, thread per face looping over its points (k_face_pl)
+    int face_mode = 1;
     // adjoint scratch, allocated on first use
     AdjFn adj = nullptr;
     double* d_tadj = nullptr;   // trace adjoints: 2 x the face-flux size
@@ -333,12 +335,12 @@ void enq_limit(hermes_ctx* c, void* q) {
 }
 void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
     FaceArgs a{c->G, c->ph, c->d_step, stage, c->face_tpb, c->noise_staged ? c->d_noise_face : nullptr,
-               c->face_traces ? c->d_traces : nullptr};
+               c->face_traces ? c->d_traces : nullptr, c->face_mode == 2 ? 1 : 0};
     if (c->face_traces) {
         ProfScope ps(c, 7);
         c->K.trace(q, c->d_traces, c->G, c->stream);
     }
-    if (c->faces_merged) {
+    if (c->face_mode == 1) {
         ProfScope ps(c, 2);
         c->K.face(-1, q, c->d_flux, a, c->stream);
         return;
@@ -545,7 +547,7 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     // one launch for the three face directions: measured faster in FP64 (the
     // directions fill each other's tails), slower in FP32 (the merged kernel
     // spills under FP32's register cap)
-    c->faces_merged = cfg->precision == 64;
+    c->face_mode = cfg->precision == 64 ? 1 : 0;
     c->G.pdl = 0;   // programmatic dependent launch measured neutral here: an autotuned option
     c->G.ncell = ncell;
     for (int d = 0; d < 3; ++d) c->G.nface[d] = nface[d];
@@ -962,10 +964,10 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
         return fail(c, HERMES_ERR_ARG, "the fused stage needs nbasis 4, ivis 0/1 and room for a third state");
     const bool tile = l->tile_stage == 1;
     if (l->pdl != 0 && l->pdl != 1) return fail(c, HERMES_ERR_ARG, "pdl must be 0 or 1");
-    if (l->faces_merged != 0 && l->faces_merged != 1) return fail(c, HERMES_ERR_ARG, "faces_merged must be 0 or 1");
+    if (l->faces_merged < 0 || l->faces_merged > 2) return fail(c, HERMES_ERR_ARG, "faces_merged must be 0, 1 or 2");
     if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged || traces != c->face_traces ||
         split != c->split_update || tile != c->tile_stage || l->pdl != c->G.pdl ||
-        (l->faces_merged == 1) != c->faces_merged) {
+        l->faces_merged != c->face_mode) {
         // captured graphs hold the old launch shape
         HCK(c, cudaSetDevice(c->device));
         HCK(c, cudaStreamSynchronize(c->stream));
@@ -979,7 +981,7 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     c->split_update = split;
     c->tile_stage = tile;
     c->G.pdl = l->pdl;
-    c->faces_merged = l->faces_merged == 1;
+    c->face_mode = l->faces_merged;
     return HERMES_OK;
 }
 
@@ -993,7 +995,7 @@ int hermes_get_launch(hermes_ctx* c, hermes_launch* l) {
     l->split_update = c->split_update ? 1 : 0;
     l->tile_stage = c->tile_stage ? 1 : 0;
     l->pdl = c->G.pdl;
-    l->faces_merged = c->faces_merged ? 1 : 0;
+    l->faces_merged = c->face_mode;
     return HERMES_OK;
 }
 

@@ -235,9 +235,12 @@ typedef struct hermes_launch {
                                 start launching while the one before it finishes, and waits for its
                                 results before touching memory); 0 (default, measured neutral on
                                 the benchmarked step): plain launches.  Bit-identical. */
-    int32_t faces_merged;    /* 1: the face fluxes of the three directions in one launch (the default
-                                in FP64, where the directions fill each other's tails); 0: one
-                                launch per direction (the default in FP32).  Bit-identical. */
+    int32_t faces_merged;    /* the face kernels: 1 the three directions in one launch (the default
+                                in FP64, where the directions fill each other's tails); 0 one launch
+                                per direction, thread per (face, point) (the default in FP32); 2 one
+                                launch per direction, thread per face looping over its points (with
+                                the stochastic stress drawn in place or absent, no trace buffer;
+                                else as 0).  Bit-identical. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
 int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);

@@ -48,7 +48,8 @@ def test_every_launch_shape_is_bit_identical(mk):
     ref = None
     shapes = [{}, {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 3},
               {"face_tpb": 64, "dt_tpb": 128, "steps_per_graph": 2, "pdl": 1},
-              {"faces_merged": 0}, {"faces_merged": 1}]
+              {"faces_merged": 0}, {"faces_merged": 1}, {"faces_merged": 2},
+              {"faces_merged": 2, "noise_inline": 1}]
     if cfg.ivis < 2 and (cfg.precision == "fp32" or not cfg.llns):   # the cell update in one kernel
         shapes.append({"split_update": 0})
     if cfg.llns:   # the stochastic stress drawn inside the face and cell kernels instead of staged
