@@ -166,6 +166,10 @@ struct hermes_ctx {
     bool tile_ok_default = false;   // the autotuner tries the fused stage here
     // box lookup tables of an ensemble (Geom.cbox, Geom.fbox)
     int* d_boxtab = nullptr;
+    // pinned landing place of the first box's time record and the flags read
+    // back after a step (one synchronisation, no pageable staging)
+    struct HostRec { BoxState st; int flags; };
+    HostRec* h_rec = nullptr;
     // face kernels: 0 one launch per direction, thread per (face, point)
     // (k_face); 1 the three directions in one launch (k_faces); 2 one launch
     // per direction, thread per face looping over its points (k_face_pl)
@@ -476,12 +480,34 @@ int leave(hermes_ctx* c, int rc) {
     return rc;
 }
 
+// enqueue the copies of the first box's time record and the flags into the
+// pinned record (allocated on first use)
+int enq_record(hermes_ctx* c) {
+    if (!c->h_rec) HCK(c, cudaMallocHost(reinterpret_cast<void**>(&c->h_rec), sizeof(hermes_ctx::HostRec)));
+    HCK(c, cudaMemcpyAsync(&c->h_rec->st, c->d_st, sizeof(BoxState), cudaMemcpyDeviceToHost, c->stream));
+    HCK(c, cudaMemcpyAsync(&c->h_rec->flags, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    return HERMES_OK;
+}
+
+// after the stream has been synchronised: time, time step and the NaN flag
+int take_record(hermes_ctx* c, double* t, double* dt) {
+    if (t) *t = c->h_rec->st.t;
+    if (dt) *dt = c->h_rec->st.dt;
+    if (c->h_rec->flags & FLAG_NONFINITE) {
+        HCK(c, cudaMemsetAsync(c->d_flags, 0, sizeof(int), c->stream));
+        return fail(c, HERMES_ERR_NONFINITE, "NaN cell average produced by the step (integrator.f90:234-250)");
+    }
+    return HERMES_OK;
+}
+
 int read_back(hermes_ctx* c, double* t, double* dt) {
     BoxState s0;
     int flags = 0;
-    HCK(c, cudaMemcpyAsync(&s0, c->d_st, sizeof(BoxState), cudaMemcpyDeviceToHost, c->stream));
-    HCK(c, cudaMemcpyAsync(&flags, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    int rc = enq_record(c);
+    if (rc) return rc;
     HCK(c, cudaStreamSynchronize(c->stream));
+    s0 = c->h_rec->st;
+    flags = c->h_rec->flags;
     if (t) *t = s0.t;
     if (dt) *dt = s0.dt;
     if (flags & FLAG_NONFINITE) {
@@ -544,10 +570,12 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     long long ncell, nface[3];
     make_boxes(*cfg, nbox, dims, lengths, seeds, c->K.nf, c->h_boxes, c->h_len, ncell, nface, c->q_elems, c->flux_elems);
     c->G.nbox = nbox;
-    // one launch for the three face directions: measured faster in FP64 (the
-    // directions fill each other's tails), slower in FP32 (the merged kernel
-    // spills under FP32's register cap)
-    c->face_mode = cfg->precision == 64 ? 1 : 0;
+    // face kernels, as measured: the linear basis (4 points per face) runs
+    // fastest with a thread per face looping over its points; nbasis 8/10 in
+    // FP64 with the three directions in one launch (they fill each other's
+    // tails), in FP32 with a thread per face point (the merged kernel spills
+    // under FP32's register cap)
+    c->face_mode = cfg->nbasis == 4 ? 2 : cfg->precision == 64 ? 1 : 0;
     c->G.pdl = 0;   // programmatic dependent launch measured neutral here: an autotuned option
     c->G.ncell = ncell;
     for (int d = 0; d < 3; ++d) c->G.nface[d] = nface[d];
@@ -739,6 +767,7 @@ int hermes_destroy(hermes_ctx* c) {
     cudaFree(c->d_tile0);
     cudaFree(c->d_qs);
     cudaFree(c->d_boxtab);
+    if (c->h_rec) cudaFreeHost(c->h_rec);
     delete c;
     return HERMES_OK;
 }
@@ -1039,12 +1068,17 @@ int hermes_advance_host(hermes_ctx* c, void* q_host, int nsteps, double* t, doub
             cudaGetLastError();
             return leave(c, fail(c, HERMES_ERR_ALLOC, "device buffers for host-array stepping"));
         }
+    // copy in, step, copy the state and the time record out, one synchronisation
     HCK(c, cudaMemcpyAsync(c->d_q[0], q_host, bytes, cudaMemcpyHostToDevice, c->stream));
-    rc = advance_impl(c, c->d_q[0], c->d_q[1], nsteps, t, dt);
+    if (t && c->G.nbox == 1) k_set_t<<<1, 32, 0, c->stream>>>(c->d_st, 1, *t);
+    rc = launch_status(c);
+    if (rc == HERMES_OK) rc = enqueue_steps_impl(c, c->d_q[0], c->d_q[1], nsteps);
     if (rc) return leave(c, rc);
     HCK(c, cudaMemcpyAsync(q_host, c->d_q[0], bytes, cudaMemcpyDeviceToHost, c->stream));
+    rc = enq_record(c);
+    if (rc) return leave(c, rc);
     HCK(c, cudaStreamSynchronize(c->stream));
-    return leave(c, HERMES_OK);
+    return leave(c, take_record(c, t, dt));
 }
 
 int hermes_box_times(hermes_ctx* c, double* t, double* dt) {

@@ -149,7 +149,9 @@ int hermes_step(hermes_ctx *ctx, void *q, void *q1, void *q2, double *t, double 
 int hermes_advance(hermes_ctx *ctx, void *q, void *q1, void *q2, int nsteps, double *t, double *dt);
 
 /* The same with host buffers: q_host (nsteps of step() on a device copy,
- * then copied back).  The reference's interface takes host arrays. */
+ * then copied back, with one synchronisation; a state with a NaN cell
+ * average is copied back as well and HERMES_ERR_NONFINITE returned).  The
+ * reference's interface takes host arrays. */
 int hermes_advance_host(hermes_ctx *ctx, void *q_host, int nsteps, double *t, double *dt);
 
 /* nsteps of step() enqueued on the context's stream from the CUDA graph,
@@ -236,11 +238,11 @@ typedef struct hermes_launch {
                                 results before touching memory); 0 (default, measured neutral on
                                 the benchmarked step): plain launches.  Bit-identical. */
     int32_t faces_merged;    /* the face kernels: 1 the three directions in one launch (the default
-                                in FP64, where the directions fill each other's tails); 0 one launch
-                                per direction, thread per (face, point) (the default in FP32); 2 one
-                                launch per direction, thread per face looping over its points (with
-                                the stochastic stress drawn in place or absent, no trace buffer;
-                                else as 0).  Bit-identical. */
+                                for nbasis 8/10 in FP64, where the directions fill each other's
+                                tails); 0 one launch per direction, thread per (face, point) (nbasis
+                                8/10 in FP32); 2 one launch per direction, thread per face looping
+                                over its points (nbasis 4; needs the stochastic stress drawn in
+                                place or absent and no trace buffer, else as 0).  Bit-identical. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
 int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);

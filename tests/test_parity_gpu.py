@@ -215,6 +215,14 @@ def test_nonfinite_is_reported_and_context_survives():
     q, q1 = s.from_numpy(Q), s.new_state()
     t, dt = s.step(q, q1, None, 0.0)
     assert np.isfinite(s.to_numpy(q)).all() and dt > 0
+    # host buffers: the non-finite state is copied back and the error raised
+    qh = np.ascontiguousarray(Qbad.T)
+    with pytest.raises(NonFiniteError):
+        s.advance_host(qh, 1)
+    assert not np.isfinite(qh).all()
+    qh = np.ascontiguousarray(Q.T)
+    t, dt = s.advance_host(qh, 2)
+    assert np.isfinite(qh).all() and dt > 0
 
 
 @pytest.mark.parametrize("kind", ["fh_nb4", "nb10_face_traces"])
