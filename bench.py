@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--n", type=int, default=128, help="vortex grid size (default 128)")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--ensemble-accuracy", type=int, default=0, metavar="STEPS",
+                    help="only the FP32-vs-FP64 ensemble-mean accuracy of the timed 256-box draw (Roe) over "
+                         "STEPS steps of the ensemble configuration's 500, printed as one JSON line")
     return ap.parse_args()
 
 
@@ -872,6 +875,15 @@ def main():
     rank, ws = dist_init()
     from hermeshd_gb300 import build
     build.build()
+    if args.ensemble_accuracy > 0:
+        if rank == 0:
+            from hermeshd_gb300 import config
+            t0 = time.perf_counter()
+            acc = ensemble_accuracy(config.fh_box(48, precision="fp32", seed=0), ensemble_draw(),
+                                    args.ensemble_accuracy)
+            acc["wall_s"] = time.perf_counter() - t0
+            print(json.dumps({"ensemble_accuracy": acc}))
+        return 0
     out = run_ours(args, rank, ws)
     if rank == 0:
         print(json.dumps(out))

@@ -13,7 +13,7 @@ from .config import Config
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libhermes_gb300.so")
 
 HERMES_OK = 0
-ABI_VERSION = 6          # HERMES_ABI_VERSION of include/hermes_gb300.h
+ABI_VERSION = 7          # HERMES_ABI_VERSION of include/hermes_gb300.h
 STATUS = {0: "HERMES_OK", 1: "HERMES_ERR_CONFIG", 2: "HERMES_ERR_SHAPE", 3: "HERMES_ERR_DTYPE",
           4: "HERMES_ERR_NONFINITE", 5: "HERMES_ERR_TIMEOUT", 6: "HERMES_ERR_CUDA", 7: "HERMES_ERR_ALLOC",
           8: "HERMES_ERR_ARG"}
@@ -23,8 +23,8 @@ EXPORTS = ("hermes_abi_version", "hermes_config_size", "hermes_sizes", "hermes_c
            "hermes_destroy", "hermes_last_error", "hermes_stream", "hermes_get_min_dt", "hermes_limiter",
            "hermes_rhs", "hermes_euler_stage", "hermes_step", "hermes_advance", "hermes_advance_host",
            "hermes_enqueue_steps", "hermes_profile_enable", "hermes_profile_read",
-           "hermes_box_times", "hermes_set_time", "hermes_set_noise_step", "hermes_check", "hermes_rhs_noalloc",
-           "hermes_rhs_vjp", "hermes_stage_vjp", "hermes_set_launch", "hermes_get_launch",
+           "hermes_box_times", "hermes_set_time", "hermes_set_noise_step", "hermes_set_noise_stage", "hermes_check", "hermes_rhs_noalloc",
+           "hermes_rhs_vjp", "hermes_stage_vjp", "hermes_limiter_vjp", "hermes_set_launch", "hermes_get_launch",
            "hermes_checkpoint_write", "hermes_checkpoint_read", "hermes_derived",
            "hermes_init_state", "hermes_conserved")
 
@@ -34,7 +34,7 @@ class HermesLaunch(C.Structure):
     _fields_ = [("face_tpb", C.c_int32), ("dt_tpb", C.c_int32), ("steps_per_graph", C.c_int32),
                 ("noise_inline", C.c_int32), ("face_traces", C.c_int32), ("split_update", C.c_int32),
                 ("tile_stage", C.c_int32), ("pdl", C.c_int32),
-                ("faces_merged", C.c_int32)]
+                ("faces_merged", C.c_int32), ("update_tpb", C.c_int32)]
 
 
 class HermesOutputUnits(C.Structure):
@@ -128,9 +128,11 @@ def lib() -> C.CDLL:
         "hermes_box_times": (i32, [vp, dp, dp]),
         "hermes_set_time": (i32, [vp, C.c_double]),
         "hermes_set_noise_step": (i32, [vp, C.c_uint64]),
+        "hermes_set_noise_stage": (i32, [vp, C.c_int32]),
         "hermes_check": (i32, [vp]),
         "hermes_rhs_noalloc": (i32, [cfgp, vp, vp, i32, vp, C.c_char_p, C.c_size_t]),
         "hermes_rhs_vjp": (i32, [vp, vp, vp, vp]),
+        "hermes_limiter_vjp": (i32, [vp, vp, vp, vp]),
         "hermes_stage_vjp": (i32, [vp, vp, vp, vp, vp, C.c_double, dp]),
         "hermes_set_launch": (i32, [vp, C.POINTER(HermesLaunch)]),
         "hermes_get_launch": (i32, [vp, C.POINTER(HermesLaunch)]),

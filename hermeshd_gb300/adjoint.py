@@ -4,8 +4,10 @@ The forward map is the library's time loop on one FP64 grid: each step takes
 dt from the CFL reduction of the cell averages (hermeshd.f90:145-199,
 ``Solver.get_min_dt``) and runs the SSP-RK stages of integrator.f90:62-86,
 each stage the library's forward-Euler stage E(q) = M (q - dt R(q)) with M the
-semi-implicit stress factor faci = 1/(1 + dt coll) of ivis 1
-(integrator.f90:174).  For RK2 the stages and combinations are the same
+semi-implicit stress factor: faci = 1/(1 + dt coll) on the stresses for ivis 1
+(integrator.f90:174), faci on the off-diagonal stresses and
+faci (I + (coll dt/3) J) on (pxx, pyy, pzz) for ivis 2 (J the 3x3 matrix of
+ones, integrator.f90:207-224).  For RK2 the stages and combinations are the same
 operations, in the same order, as the fused ``Solver.step``, so the rollout
 reproduces it bit for bit.
 
@@ -13,18 +15,35 @@ The backward pass is the transpose, step by step in reverse:
 
 * each stage's vector-Jacobian product comes from the CUDA adjoint kernels
   (``Solver.stage_vjp``): Riemann flux, volume and surface quadrature,
-  sources and the stress factor;
+  sources and the stress factor (ivis 0/1 with the ideal-gas law by
+  hand-derived reverse sweeps; ivis 2 and the Tait equation of state, ieos 2,
+  by one dual-number pass per column through the forward physics);
 * the RK combinations are linear;
 * the time step depends on the state: dL/ddt is the sum over stages of
-  lam . dE/ddt, with dE/ddt = (E - M q)/dt, minus coll faci E on the ivis-1
-  stresses, and dt = cflm / ((vmag + cs_last) dxi) is differentiated through
-  its maximum (the arg-max cell) and the last cell's sound speed;
-* the collision frequency coll (for ivis 1 the viscosity enters only as
-  coll = p/mu, since colvis = p) through faci.
+  lam . dE/ddt, with dE/ddt = (dM/ddt) y + M (y - q)/dt, y = M^-1 E, and
+  dt = cflm / ((vmag + cs_last) dxi) is differentiated through its maximum
+  (the arg-max cell) and the last cell's sound speed (ideal gas or Tait);
+* the collision frequency coll: through faci for ivis 1 (the viscosity
+  enters only as coll = p/mu, since colvis = p), through the relaxation
+  source -coll P of the right-hand side for ivis 0, through both the stage
+  factor and the source coll rho (v v - |v|^2/3) for ivis 2.
 
-The positivity limiter is treated as the identity; the forward pass counts
-the stages in which it changed the state (``Rollout.limiter_events``), so a
-gradient taken where it acted is flagged.
+With the stochastic stress on, the gradient is the pathwise one: step n,
+stage k draws the realisation of the library's Philox counters (noise step
+noise_step0 + n, stage index k), in the forward pass and again in the
+backward pass, which holds it fixed while differentiating the state
+dependence of the stress terms (their products with the velocity).
+
+Out of scope: HLLC with ieos 2 (its sound speed takes 1/rho of another face
+point, flux.f90:533-534) and ivis 3.
+
+The positivity limiter (flux.f90:1077-1164), applied in place to every stage
+input, is differentiated along the branch it takes (``Solver.limiter_vjp``:
+the identity where it leaves a cell unchanged; the arg-min face point, the
+clamp of theta and the floors as the forward pass took them), so the records
+keep each stage input before and after the limiter.  The forward pass counts
+the stages in which it acted (``Rollout.limiter_events``): near a switch of
+its branch the gradient is one-sided.
 
 Checkpointing: the forward keeps the state every ``checkpoint_every`` steps;
 the backward recomputes each segment's stage states from its checkpoint, one
@@ -33,13 +52,12 @@ extra forward pass in total, holding one segment's stage states at a time.
 from __future__ import annotations
 
 import math
-import warnings
 from typing import Dict, List, Optional, Tuple
 
 from .config import NQ, Config
 from .solver import Solver
 
-RH, MX, MY, MZ, EN, PXX = 0, 1, 2, 3, 4, 5
+RH, MX, MY, MZ, EN, PXX, PZZ = 0, 1, 2, 3, 4, 5, 7
 
 
 def _torch():
@@ -50,17 +68,23 @@ def _torch():
 class Rollout:
     """Differentiable n-step rollout of one FP64 problem."""
 
-    def __init__(self, cfg: Config, checkpoint_every: int = 20, check_limiter: bool = True):
+    def __init__(self, cfg: Config, checkpoint_every: int = 20, check_limiter: bool = True, noise_step0: int = 0):
+        """noise_step0: with the stochastic stress on, step n of the rollout
+        draws the realisation of noise step noise_step0 + n (stage k of it
+        with stage index k, as the library's fused step does)."""
         if cfg.precision != "fp64":
             raise ValueError("the adjoint runs in FP64")
-        if cfg.ivis not in (0, 1) or cfg.ieos != 1 or cfg.llns:
-            raise ValueError("the adjoint supports ivis 0/1, ieos 1, no stochastic stress")
+        if cfg.ivis not in (0, 1, 2) or cfg.ieos not in (1, 2):
+            raise ValueError("the adjoint supports ivis 0/1/2, ieos 1/2")
+        if cfg.ieos == 2 and cfg.ihllc == 1:
+            raise ValueError("the adjoint does not take HLLC with ieos 2")
         if cfg.iorder not in (2, 3):
             raise ValueError("iorder must be 2 or 3")
         self.cfg = cfg
         self.checkpoint_every = max(1, int(checkpoint_every))
         self.check_limiter = check_limiter
         self.limiter_events = 0
+        self.noise_step0 = int(noise_step0)
         self._solvers: Dict[float, Solver] = {}
 
     def solver(self, coll: float) -> Solver:
@@ -72,29 +96,43 @@ class Rollout:
         return s
 
     # ---- forward ------------------------------------------------------------
-    def _stage(self, S: Solver, x, dt: float, check: bool):
-        if check:
-            x0 = x.clone()
-            e = S.euler_stage(x, dt)
-            if not _torch().equal(x, x0):
-                self.limiter_events += 1
-            return e
-        return S.euler_stage(x, dt)
+    def _noise(self, S: Solver, n: int, k: Optional[int] = None):
+        """Point the context's stochastic-stress counters at stage k of step n."""
+        if self.cfg.llns:
+            if n is not None:
+                S.set_noise_step(self.noise_step0 + n)
+            if k is not None:
+                S.set_noise_stage(k)
 
-    def step(self, S: Solver, q, dt: float, check: Optional[bool] = None) -> Tuple[object, List[Tuple[object, object]]]:
-        """One step at a given dt; returns (q_new, [(stage input, E(input))]).
-        check: count the stages the limiter changed (default: check_limiter;
-        the backward pass's recomputation skips it, the forward counted)."""
+    def _stage(self, S: Solver, xr, dt: float, check: bool, keep: bool, k: int = 0):
+        """One forward-Euler stage of the library (limiter in place on its
+        input, then E): returns (limited input, E).  keep: xr is left as it
+        is (the limiter works on a copy), as the backward pass needs it."""
+        self._noise(S, None, k)
+        x = xr.clone() if (keep or check) else xr
+        e = S.euler_stage(x, dt)
+        if check and not _torch().equal(x, xr):
+            self.limiter_events += 1
+        return x, e
+
+    def step(self, S: Solver, q, dt: float, check: Optional[bool] = None,
+             keep: bool = True, n: int = 0) -> Tuple[object, List[Tuple[object, object, object]]]:
+        """Step n at a given dt; returns (q_new, [(stage input before the
+        limiter, after it, E)]) (the records only with keep; without it q is
+        limited in place).  check: count the stages the limiter changed
+        (default: check_limiter; the backward pass's recomputation skips it,
+        the forward counted)."""
         ck = self.check_limiter if check is None else check
+        self._noise(S, n)
         if self.cfg.iorder == 2:
-            e1 = self._stage(S, q, dt, ck)
-            e2 = self._stage(S, e1, dt, ck)
-            return 0.5 * (q + e2), [(q, e1), (e1, e2)]
-        e1 = self._stage(S, q, dt, ck)
-        e2 = self._stage(S, e1, dt, ck)
-        x2 = 0.75 * q + 0.25 * e2
-        e3 = self._stage(S, x2, dt, ck)
-        return (1.0 / 3.0) * q + (2.0 / 3.0) * e3, [(q, e1), (e1, e2), (x2, e3)]
+            x0, e1 = self._stage(S, q, dt, ck, keep, 0)
+            x1, e2 = self._stage(S, e1, dt, ck, keep, 1)
+            return 0.5 * (x0 + e2), ([(q, x0, e1), (e1, x1, e2)] if keep else [])
+        x0, e1 = self._stage(S, q, dt, ck, keep, 0)
+        x1, e2 = self._stage(S, e1, dt, ck, keep, 1)
+        x2r = 0.75 * x0 + 0.25 * e2
+        x2, e3 = self._stage(S, x2r, dt, ck, keep, 2)
+        return (1.0 / 3.0) * x0 + (2.0 / 3.0) * e3, ([(q, x0, e1), (e1, x1, e2), (x2r, x2, e3)] if keep else [])
 
     def forward(self, q0, coll: float, nsteps: int):
         """Returns (q_final, checkpoints {step: state}, dts)."""
@@ -104,23 +142,36 @@ class Rollout:
         dts: List[float] = []
         for n in range(nsteps):
             dt = S.get_min_dt(q)
-            q, _ = self.step(S, q, dt)
+            q, _ = self.step(S, q, dt, keep=False, n=n)
             dts.append(dt)
             if (n + 1) % self.checkpoint_every == 0 and n + 1 < nsteps:
                 ckpts[n + 1] = q.clone()
         return q, ckpts, dts
 
     # ---- time step and its derivative --------------------------------------
+    def _sound_speed(self, rho, en, v2):
+        """The CFL sound speed of the library's k_mindt (hermeshd.f90:165-166):
+        gamma (E/rho - |v|^2/2) for the ideal gas, 7.2 P_1 rho^6.2 + T_floor
+        for the Tait equation of state."""
+        torch = _torch()
+        c = self.cfg
+        if c.ieos == 2:
+            return torch.sqrt(7.2 * c.P_1 * torch.pow(rho, 6.2) + c.T_floor)
+        return torch.sqrt(c.aindex * (en / rho - 0.5 * v2))
+
     def dt_of(self, q):
         """dt of the CFL reduction as a differentiable torch function of the
-        cell averages (the arithmetic of the library's k_mindt, ieos 1)."""
+        cell averages (the arithmetic of the library's k_mindt)."""
         torch = _torch()
         c = self.cfg
         a = q[0, :5]
         rho, mx, my, mz, en = a[0], a[1], a[2], a[3], a[4]
         dni = 1.0 / rho
         vx, vy, vz = mx * dni, my * dni, mz * dni
-        cs = torch.sqrt(c.aindex * (en * dni - 0.5 * (vx * vx + vy * vy + vz * vz)))
+        if c.ieos == 2:
+            cs = self._sound_speed(rho, en, None)
+        else:
+            cs = torch.sqrt(c.aindex * (en * dni - 0.5 * (vx * vx + vy * vy + vz * vz)))
         v0 = torch.maximum(torch.maximum(vx.abs() + cs, vy.abs() + cs), vz.abs() + cs)
         ok = (v0 > 0) & (rho > c.rh_mult * c.rh_floor)
         vmag = v0[ok].max() if bool(ok.any()) else torch.zeros((), dtype=q.dtype, device=q.device)
@@ -134,21 +185,26 @@ class Rollout:
         arg-max cell of vmag = max_d |v_d| + cs and of the last cell (cs_last):
         d dt = -dt^2 dxi / cflm (d vmag + d cs_last), with, per cell,
         d|v_k| = sgn(v_k) dm_k / rho - |v_k| drho / rho (k the arg-max
-        direction) and cs^2 = gamma (E/rho - |v|^2/2)."""
+        direction) and cs^2 = gamma (E/rho - |v|^2/2) (ideal gas) or
+        7.2 P_1 rho^6.2 + T_floor (Tait)."""
         torch = _torch()
         c = self.cfg
         a = q[0, :5].reshape(5, -1)
         rho, m, en = a[0], a[1:4], a[4]
         v = m / rho
         v2 = (v * v).sum(0)
-        cs = torch.sqrt(c.aindex * (en / rho - 0.5 * v2))
+        cs = self._sound_speed(rho, en, v2)
         av, k = v.abs().max(0)
         v0 = av + cs
         ok = (v0 > 0) & (rho > c.rh_mult * c.rh_floor)
         imax = torch.argmax(torch.where(ok, v0, torch.full_like(v0, -math.inf)))
         ncell = a.shape[1]
-        h = c.aindex / (2.0 * cs * rho)
-        gcs = torch.stack([h * (-en / rho + v2), -h * v[0], -h * v[1], -h * v[2], h])   # d cs / d(rho, m, E)
+        if c.ieos == 2:
+            z = torch.zeros_like(cs)
+            gcs = torch.stack([7.2 * 6.2 * c.P_1 * torch.pow(rho, 5.2) / (2.0 * cs), z, z, z, z])
+        else:
+            h = c.aindex / (2.0 * cs * rho)
+            gcs = torch.stack([h * (-en / rho + v2), -h * v[0], -h * v[1], -h * v[2], h])   # d cs / d(rho, m, E)
         gv = torch.zeros_like(gcs)
         sg = torch.sign(v.gather(0, k[None])[0])
         gv[0] = -av / rho
@@ -162,59 +218,95 @@ class Rollout:
         return g
 
     def _ddt_stage(self, x, e, lam, dt: float, coll: float):
-        """lam . dE/ddt for the stage e = E(x), a 0-d device tensor."""
+        """lam . dE/ddt for the stage e = E(x), a 0-d device tensor.
+
+        E = M y, y = x - dt R(x): dE/ddt = (dM/ddt) y + M (y - x)/dt
+        = (E - M x)/dt + (dM/ddt) y.  ivis 1: M = faci on the stresses,
+        dM/ddt y = -coll faci E.  ivis 2: the same on the off-diagonal
+        stresses; on the diagonal ones M = faci (I + c J), c = coll dt/3, and
+        since sum_d y_d = sum_d E_d there, (dM/ddt y)_d = -coll faci E_d +
+        faci (coll/3) sum_k E_k."""
         g = (e - x) / dt
-        if self.cfg.ivis == 1:
+        iv = self.cfg.ivis
+        if iv in (1, 2):
             faci = 1.0 / (1.0 + dt * coll)
             es, xs = e[:, PXX:], x[:, PXX:]
             g[:, PXX:] = (es - faci * xs) / dt - coll * faci * es
+            if iv == 2:
+                ed, xd = e[:, PXX:PZZ + 1], x[:, PXX:PZZ + 1]
+                c3 = coll * dt / 3.0
+                esum = ed.sum(1, keepdim=True)
+                g[:, PXX:PZZ + 1] = ((ed - faci * (xd + c3 * xd.sum(1, keepdim=True))) / dt
+                                     - coll * faci * ed + faci * (coll / 3.0) * esum)
         return (lam * g).sum()
 
     def _dcoll_stage(self, e, lam, dt: float, coll: float):
-        """lam . dE/dcoll for the stage e = E(x) (ivis 1: the stresses are
-        faci (x - dt R) with faci = 1/(1 + dt coll), so dE/dcoll = -dt faci E
-        there), a 0-d device tensor."""
+        """lam . dE/dcoll for the stage e = E(x) of ivis 1 (the stresses are
+        faci (x - dt R) with faci = 1/(1 + dt coll) and R does not depend on
+        coll, so dE/dcoll = -dt faci E there), a 0-d device tensor."""
         faci = 1.0 / (1.0 + dt * coll)
         return (lam[:, PXX:] * e[:, PXX:]).sum() * (-dt * faci)
 
     # ---- backward -----------------------------------------------------------
-    def step_vjp(self, S: Solver, recs, lam, dt: float, coll: float, with_dt: bool = True):
+    def step_vjp(self, S: Solver, recs, lam, dt: float, coll: float, with_dt: bool = True,
+                 with_dcoll: bool = True, n: int = 0):
         """Transpose of one step: (lam_q, dL/dcoll as a 0-d device tensor) from
-        lam of its output.  Nothing in it waits for the device."""
+        lam of its output.  For ivis 1 nothing in it waits for the device; for
+        ivis 0 and 2, where coll enters the right-hand side, the stage VJPs
+        return lam_out . dE/dcoll to the host (one synchronisation per stage)
+        unless with_dcoll is False."""
         torch = _torch()
-        want = self.cfg.ivis == 1
-        dcoll = torch.zeros((), dtype=lam.dtype, device=lam.device)
+        iv = self.cfg.ivis
+        torch_dc = with_dcoll and iv == 1
+        kern_dc = with_dcoll and iv != 1
+        acc = {"dcoll": torch.zeros((), dtype=lam.dtype, device=lam.device)}
         ddt = torch.zeros((), dtype=lam.dtype, device=lam.device)
+
+        self._noise(S, n)
+
+        def svjp(x, lam_out, e, k):
+            self._noise(S, None, k)
+            if kern_dc:
+                out, dc = S.stage_vjp(x, lam_out, dt, e_out=e, want_dcoll=True)
+                acc["dcoll"] = acc["dcoll"] + dc
+                return out
+            return S.stage_vjp(x, lam_out, dt)[0]
+
+        def lvjp(xr, lam_x):   # through the limiter applied to xr, in place on lam_x
+            return S.limiter_vjp(xr, lam_x, out=lam_x)
+
         if self.cfg.iorder == 2:
-            (x0, e1), (x1, e2) = recs
+            (x0r, x0, e1), (x1r, x1, e2) = recs
             lam_e2 = 0.5 * lam
-            lam_x1, _ = S.stage_vjp(x1, lam_e2, dt)
-            if want:
-                dcoll = dcoll + self._dcoll_stage(e2, lam_e2, dt, coll) + self._dcoll_stage(e1, lam_x1, dt, coll)
+            lam_e1 = lvjp(x1r, svjp(x1, lam_e2, e2, 1))
+            if torch_dc:
+                acc["dcoll"] = acc["dcoll"] + self._dcoll_stage(e2, lam_e2, dt, coll) + self._dcoll_stage(e1, lam_e1, dt, coll)
             if with_dt:
-                ddt = ddt + self._ddt_stage(x1, e2, lam_e2, dt, coll) + self._ddt_stage(x0, e1, lam_x1, dt, coll)
-            lam_x0, _ = S.stage_vjp(x0, lam_x1, dt)
+                ddt = ddt + self._ddt_stage(x1, e2, lam_e2, dt, coll) + self._ddt_stage(x0, e1, lam_e1, dt, coll)
+            lam_x0 = svjp(x0, lam_e1, e1, 0)
             lam_x0 += 0.5 * lam
         else:
-            (x0, e1), (x1, e2), (x2, e3) = recs
+            (x0r, x0, e1), (x1r, x1, e2), (x2r, x2, e3) = recs
             lam_e3 = (2.0 / 3.0) * lam
-            lam_x2, _ = S.stage_vjp(x2, lam_e3, dt)
-            lam_e2 = 0.25 * lam_x2
-            lam_x1, _ = S.stage_vjp(x1, lam_e2, dt)
-            if want:
-                dcoll = (dcoll + self._dcoll_stage(e3, lam_e3, dt, coll) + self._dcoll_stage(e2, lam_e2, dt, coll)
-                         + self._dcoll_stage(e1, lam_x1, dt, coll))
+            lam_x2r = lvjp(x2r, svjp(x2, lam_e3, e3, 2))
+            lam_e2 = 0.25 * lam_x2r
+            lam_e1 = lvjp(x1r, svjp(x1, lam_e2, e2, 1))
+            if torch_dc:
+                acc["dcoll"] = (acc["dcoll"] + self._dcoll_stage(e3, lam_e3, dt, coll)
+                                + self._dcoll_stage(e2, lam_e2, dt, coll) + self._dcoll_stage(e1, lam_e1, dt, coll))
             if with_dt:
                 ddt = (ddt + self._ddt_stage(x2, e3, lam_e3, dt, coll) + self._ddt_stage(x1, e2, lam_e2, dt, coll)
-                       + self._ddt_stage(x0, e1, lam_x1, dt, coll))
-            lam_x0, _ = S.stage_vjp(x0, lam_x1, dt)
-            lam_x0 += (1.0 / 3.0) * lam + 0.75 * lam_x2
+                       + self._ddt_stage(x0, e1, lam_e1, dt, coll))
+            lam_x0 = svjp(x0, lam_e1, e1, 0)
+            lam_x0 += (1.0 / 3.0) * lam + 0.75 * lam_x2r
+        lam_q = lvjp(x0r, lam_x0)
         if with_dt:
-            lam_x0 += ddt * self._dt_grad(x0, dt)
-        return lam_x0, dcoll
+            lam_q += ddt * self._dt_grad(x0r, dt)
+        return lam_q, acc["dcoll"]
 
-    def backward(self, coll: float, ckpts, dts, lam, with_dt: bool = True):
-        """(lam_q0, dL/dcoll) from lam of the final state."""
+    def backward(self, coll: float, ckpts, dts, lam, with_dt: bool = True, with_dcoll: bool = True):
+        """(lam_q0, dL/dcoll) from lam of the final state (dL/dcoll 0.0 when
+        with_dcoll is False)."""
         torch = _torch()
         S = self.solver(coll)
         nsteps = len(dts)
@@ -225,10 +317,10 @@ class Rollout:
             q = ckpts[start].clone()
             seg = []
             for n in range(start, end):
-                q, recs = self.step(S, q, dts[n], check=False)
+                q, recs = self.step(S, q, dts[n], check=False, n=n)
                 seg.append(recs)
             for n in range(end - 1, start - 1, -1):
-                lam, dc = self.step_vjp(S, seg[n - start], lam, dts[n], coll, with_dt)
+                lam, dc = self.step_vjp(S, seg[n - start], lam, dts[n], coll, with_dt, with_dcoll, n)
                 dcoll = dcoll + dc
             del seg
         return lam, float(dcoll)
@@ -247,10 +339,8 @@ def _rollout_fn():
 
         @staticmethod
         def backward(ctx, lam):
-            lam0, dcoll = ctx.roll.backward(ctx.coll, ctx.ckpts, ctx.dts, lam)
-            if ctx.roll.limiter_events:
-                warnings.warn(f"the positivity limiter acted in {ctx.roll.limiter_events} stage(s); "
-                              "the adjoint treats it as the identity")
+            lam0, dcoll = ctx.roll.backward(ctx.coll, ctx.ckpts, ctx.dts, lam,
+                                            with_dcoll=bool(ctx.needs_input_grad[1]))
             g = torch.tensor(dcoll, dtype=lam.dtype, device=lam.device)
             return lam0, g, None, None
 

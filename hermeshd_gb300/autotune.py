@@ -26,12 +26,16 @@ include/hermes_gb300.h):
                        or one launch each with a thread per face looping
                        over its points (2); the context's default first;
 * ``tile_stage``       each stage as one fused kernel over tiles of cells (1)
-                       or the separate kernels (0); tried last, where the
-                       context has it (nbasis 4, ivis 0/1).  With it on, only
-                       steps_per_graph still applies.
+                       or the separate kernels (0); tried where the context
+                       has it (nbasis 4, ivis 0/1).  With it on, only
+                       steps_per_graph still applies;
+* ``update_tpb``       threads per block of the split update (64/128/256),
+                       tuned where the split update is on.
 
 The cell kernel keeps 32 cells per block: its hydro and stress thread groups
-must each fill whole warps, and its register cap is fixed at compile time.
+must each fill whole warps (with 16 cells both groups would share one warp and
+run their two code paths one after the other), and its register cap is fixed
+at compile time.
 
 Tuning is a coordinate search: each knob in turn, the others at their best so
 far, each candidate timed with CUDA events over ``steps`` steps (best of
@@ -57,6 +61,7 @@ KNOBS = {
     "pdl": (0, 1),
     "faces_merged": (1, 0),          # the context's default is tried first
     "tile_stage": (0, 1),            # tuned only where the context has the fused stage
+    "update_tpb": (128, 64, 256),    # tuned only with the split update
 }
 
 
@@ -150,6 +155,10 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
     for k in ("face_traces", "split_update"):
         if cur[k] == 0:
             knobs.pop(k, None)
+    if cur["split_update"] == 0:
+        knobs.pop("update_tpb", None)
+    elif "update_tpb" in knobs:
+        knobs["update_tpb"] = (cur["update_tpb"],) + tuple(u for u in (64, 128, 256) if u != cur["update_tpb"])
     if cur["tile_stage"] == 0 and not _can_tile(solver, cur):
         knobs.pop("tile_stage", None)
     if "faces_merged" in knobs:

@@ -5,6 +5,6 @@
 namespace hermes {
 cudaError_t cell_adj_dual_nb4(const double* Q, const double* mu, const double* tadj, double* out, const AdjArgs& a,
                                cudaStream_t s) {
-    return cell_adj_launch<4, 2, false>(Q, mu, tadj, out, a, s);
+    return cell_adj_launch<4, 2, ADJ_DUAL>(Q, mu, tadj, out, a, s);
 }
 }  // namespace hermes

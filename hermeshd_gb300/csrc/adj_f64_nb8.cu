@@ -5,4 +5,8 @@ namespace hermes {
 cudaError_t adj_f64_nb8(const double* Q, const double* mu, double* tadj, double* out, const AdjArgs& a, cudaStream_t s) {
     return adj_launch<8, 2>(Q, mu, tadj, out, a, s);
 }
+cudaError_t limit_adj_f64_nb8(const double* Q, const double* lam_out, double* lam_in, const Geom& G, const Phys& ph,
+                               cudaStream_t s) {
+    return limit_adj_launch<8, 2>(Q, lam_out, lam_in, G, ph, s);
+}
 }  // namespace hermes

@@ -5,6 +5,6 @@
 namespace hermes {
 cudaError_t cell_adj_dual_nb8(const double* Q, const double* mu, const double* tadj, double* out, const AdjArgs& a,
                                cudaStream_t s) {
-    return cell_adj_launch<8, 2, false>(Q, mu, tadj, out, a, s);
+    return cell_adj_launch<8, 2, ADJ_DUAL>(Q, mu, tadj, out, a, s);
 }
 }  // namespace hermes

@@ -18,10 +18,23 @@
 //               writes the adjoint of both traces
 //   k_cell_adj  per cell: gathers the trace adjoints, volume and source
 //               transposes; writes nu = (dR/dQ)^T mu, or mu - dt*nu
+//   k_limit_adj per cell: the positivity limiter's VJP (its active branch)
 //
-// Scope: one grid, ieos 1, no stochastic stress, ivis 0 or 1; the limiter is
-// taken as the identity (it is inactive in the smooth regime where the
-// adjoint is used; the forward pass reports if it acted).
+// Three ways to the point-wise Jacobians (MODE): ADJ_REV, the hand-derived
+// reverse sweeps (ivis 0/1, ieos 1, no stochastic stress); ADJ_DUAL, their check path (dual passes
+// for the hydro columns, the ivis 0/1 stress columns in closed form); ADJ_GEN,
+// one dual pass per column of every variable through the forward physics,
+// which covers whatever the forward computes: the 10-moment ivis 2 fluxes
+// with the freezing-speed LLF flux and the nonlinear relaxation source
+// (sources.f90:51-69), and the Tait equation of state (ieos 2) with the
+// central or Roe flux.
+//
+// The stochastic stress is held fixed: ADJ_GEN redraws the forward kernels'
+// values from the same Philox counters and passes them as constants.
+//
+// Scope: one grid, ivis 0, 1 or 2, ieos 1 or 2 (not ieos 2 with HLLC, whose
+// every point uses 1/rho of the last point of the reference's call,
+// flux.f90:533-534: a coupling across points).
 #pragma once
 
 #include "dg_dual.cuh"
@@ -58,7 +71,7 @@ __device__ __forceinline__ double trace_of(const double* __restrict__ Qb, long l
     return ((s.mask >> v) & 1u) ? acc : 0.0;
 }
 
-template <class TB, int DIR, int P, bool REV>
+template <class TB, int DIR, int P, int MODE>
 __device__ __forceinline__ void face_adj_point(const double* __restrict__ Q, const double* __restrict__ mu,
                                                double* __restrict__ tadj, const AdjArgs& a, long long gf) {
     const Geom& G = a.G;
@@ -153,7 +166,38 @@ __device__ __forceinline__ void face_adj_point(const double* __restrict__ Q, con
         lamF[v] = di * sacc;
     }
     double lamL[NQ], lamR[NQ];
-    if constexpr (REV) {
+    if constexpr (MODE == ADJ_GEN) {
+        // J^T lamF, one dual pass per column of each side's trace; the
+        // stochastic stress of the face point (the forward face kernel's
+        // draw: kind DIR, site lf, points P and P + NF) enters as a constant
+        Dual SLd[6], SRd[6];
+        if (ph.llns) {
+            double SL[6], SR[6];
+            const NoiseCtr nc{*a.nstep, a.nstage};
+            random_stress<double>(ph, B.seed, nc, DIR, (unsigned long long)lf, P, SL);
+            random_stress<double>(ph, B.seed, nc, DIR, (unsigned long long)lf, P + TB::NF, SR);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) { SLd[c] = Dual(SL[c]); SRd[c] = Dual(SR[c]); }
+        }
+#pragma unroll 1
+        for (int pass = 0; pass < 2 * NQ; ++pass) {
+            const int side = pass / NQ, jv = pass % NQ;
+            const TraceSrc& src = side == 0 ? L : R;
+            double acc = 0.0;
+            if (src.cell >= 0 && ((src.mask >> jv) & 1u)) {
+                Dual dL[NQ], dR[NQ], F[NQ];
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) {
+                    dL[v] = Dual(qL[v], (side == 0 && v == jv) ? 1.0 : 0.0);
+                    dR[v] = Dual(qR[v], (side == 1 && v == jv) ? 1.0 : 0.0);
+                }
+                face_flux_fn<Dual, DIR>(ph, dL, dR, SLd, SRd, Dual(0.0), F);
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) acc = fma(lamF[v], F[v].d, acc);
+            }
+            (side == 0 ? lamL : lamR)[jv] = acc;
+        }
+    } else if constexpr (MODE == ADJ_REV) {
         // one reverse sweep through the numerical flux (dg_flux_vjp.cuh)
         face_flux_vjp<DIR>(ph, qL, qR, lamF, lamL, lamR);
         // a zero ghost or a ghost component forced to zero owns no trace
@@ -234,7 +278,7 @@ __device__ __forceinline__ void face_adj_point(const double* __restrict__ Q, con
     }
 }
 
-template <class TB, int DIR, bool REV>
+template <class TB, int DIR, int MODE>
 __global__ void __launch_bounds__(ADJ_TPB) k_face_adj(const double* __restrict__ Q, const double* __restrict__ mu,
                                                       double* __restrict__ tadj, AdjArgs a) {
     const long long gf = (long long)blockIdx.x * ADJ_TPB + threadIdx.x;
@@ -242,17 +286,20 @@ __global__ void __launch_bounds__(ADJ_TPB) k_face_adj(const double* __restrict__
     const int p = blockIdx.y;
     sfor<TB::NF>([&](auto pp) {
         constexpr int P = decltype(pp)::value;
-        if (p == P) face_adj_point<TB, DIR, P, REV>(Q, mu, tadj, a, gf);
+        if (p == P) face_adj_point<TB, DIR, P, MODE>(Q, mu, tadj, a, gf);
     });
 }
 
-template <class TB, bool REV>
-__global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__ Q, const double* __restrict__ mu,
-                                                      const double* __restrict__ tadj, double* __restrict__ out, AdjArgs a) {
+// one cell of the cell pass; returns mu . dR/dcoll of the cell when
+// a.cpart is set (ivis 0: the relaxation -coll P; ivis 2: the source
+// coll rho (v v - |v|^2/3); R of ivis 1 does not depend on coll)
+template <class TB, int MODE>
+__device__ __forceinline__ double cell_adj_body(const double* __restrict__ Q, const double* __restrict__ mu,
+                                                const double* __restrict__ tadj, double* __restrict__ out,
+                                                const AdjArgs& a, long long le) {
     constexpr int NB = TB::NB, NF = TB::NF, NPG = TB::NPG;
-    const long long le = (long long)blockIdx.x * ADJ_TPB + threadIdx.x;
-    if (le >= a.G.ncell) return;
     const Phys& ph = a.ph;
+    double cr = 0.0;
     const Box& B = a.G.boxes[0];
     const long long nc = B.ncell;
     double nu[NB][NQ];
@@ -327,8 +374,64 @@ __global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__
             lamF[2][v] = -di[2] * a2;
             lamS[v] = -as;
         }
+        if (a.cpart) {   // mu . dR/dcoll at g: sum_v lamS[v] ds_v/dcoll
+            if (ph.ivis == 0) {
+#pragma unroll
+                for (int v = PXX; v < NQ; ++v) cr = fma(lamS[v], -u[v], cr);
+            } else if (ph.ivis == 2) {
+                Phys p1 = ph;
+                p1.coll = 1.0;
+                double sv[6];
+                ten_moment_source<double>(p1, primitives(ph, u), sv);
+#pragma unroll
+                for (int m = 0; m < 6; ++m) cr = fma(lamS[PXX + m], sv[m], cr);
+            }
+        }
         double lamu[NQ];
-        if constexpr (REV) {
+        if constexpr (MODE == ADJ_GEN) {
+            // one dual pass per column: the point fluxes of the three
+            // directions (with the stochastic stress of the forward cell
+            // kernel's draw, kind 3 + d, site le, point g) and the sources
+            double Sn[3][6];
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) Sn[d][c] = 0.0;
+            if (ph.llns) {
+                const NoiseCtr nc{*a.nstep, a.nstage};
+#pragma unroll
+                for (int d = 0; d < 3; ++d) random_stress<double>(ph, B.seed, nc, 3 + d, (unsigned long long)le, g, Sn[d]);
+            }
+#pragma unroll 1
+            for (int jv = 0; jv < NQ; ++jv) {
+                Dual ud[NQ];
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) ud[v] = Dual(u[v], v == jv ? 1.0 : 0.0);
+                const Prim<Dual> w = primitives(ph, ud);
+                double acc = 0.0;
+                sfor<3>([&](auto dd) {
+                    constexpr int d = decltype(dd)::value;
+                    const Dual Sd[6] = {Dual(Sn[d][0]), Dual(Sn[d][1]), Dual(Sn[d][2]),
+                                        Dual(Sn[d][3]), Dual(Sn[d][4]), Dual(Sn[d][5])};
+                    Dual f[NQ];
+                    point_flux<Dual, d>(ph, ud, w, Sd, f);
+#pragma unroll
+                    for (int v = 0; v < NQ; ++v) acc = fma(lamF[d][v], f[v].d, acc);
+                });
+                if (ph.ivis == 2) {   // sources.f90:51-69
+                    Dual sv[6];
+                    ten_moment_source<Dual>(ph, w, sv);
+#pragma unroll
+                    for (int m = 0; m < 6; ++m) acc = fma(lamS[PXX + m], sv[m].d, acc);
+                }
+                if (src_lin && jv >= PXX) acc = fma(lamS[jv], -ph.coll, acc);   // sources.f90:37-43
+                if (src_bf) {    // body force (no reference counterpart): linear in rho and m_x
+                    if (jv == RH) acc = fma(lamS[MX], ph.body_force, acc);
+                    if (jv == MX) acc = fma(lamS[EN], ph.body_force, acc);
+                }
+                lamu[jv] = acc;
+            }
+        } else if constexpr (MODE == ADJ_REV) {
             // one reverse sweep of the primitives and the three point fluxes
             // (dg_flux_vjp.cuh), then the linear sources
 #pragma unroll
@@ -400,18 +503,40 @@ __global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__
             const long long ix = (long long)(b * NQ + v) * nc + le;
             out[ix] = a.mode == 0 ? nu[b][v] : mu[ix] - dt * nu[b][v];
         }
+    return cr;
+}
+
+template <class TB, int MODE>
+__global__ void __launch_bounds__(ADJ_TPB) k_cell_adj(const double* __restrict__ Q, const double* __restrict__ mu,
+                                                      const double* __restrict__ tadj, double* __restrict__ out, AdjArgs a) {
+    const long long le = (long long)blockIdx.x * ADJ_TPB + threadIdx.x;
+    double cr = 0.0;
+    if (le < a.G.ncell) cr = cell_adj_body<TB, MODE>(Q, mu, tadj, out, a, le);
+    if (a.cpart) {   // block partial of mu . dR/dcoll, summed in a fixed order
+        __shared__ double ws[ADJ_TPB / 32];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cr += __shfl_down_sync(0xffffffffu, cr, o);
+        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cr;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+#pragma unroll
+            for (int w = 0; w < ADJ_TPB / 32; ++w) t += ws[w];
+            a.cpart[blockIdx.x] = t;
+        }
+    }
 }
 
 // the cell pass of one basis; the reverse-sweep and the dual-number (check
 // path) variants are compiled in units of their own (adj_f64_nb*_cell.cu,
 // adj_f64_nb*_dual.cu), the cell kernels being the slowest to compile
-template <int NB, int NQD, bool REV>
+template <int NB, int NQD, int MODE>
 cudaError_t cell_adj_launch(const double* Q, const double* mu, const double* tadj, double* out, const AdjArgs& a,
                             cudaStream_t s) {
     using TB = hermes_tab::Tab<NB, NQD>;
     if (a.G.ncell > 0) {
         const unsigned nblk = (unsigned)((a.G.ncell + ADJ_TPB - 1) / ADJ_TPB);
-        k_cell_adj<TB, REV><<<nblk, ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);
+        k_cell_adj<TB, MODE><<<nblk, ADJ_TPB, 0, s>>>(Q, mu, tadj, out, a);
     }
     return cudaGetLastError();
 }
@@ -419,6 +544,83 @@ cudaError_t cell_adj_dual(int nb, const double* Q, const double* mu, const doubl
                           const AdjArgs& a, cudaStream_t s);
 cudaError_t cell_adj_rev(int nb, const double* Q, const double* mu, const double* tadj, double* out,
                          const AdjArgs& a, cudaStream_t s);
+cudaError_t cell_adj_gen(int nb, const double* Q, const double* mu, const double* tadj, double* out,
+                         const AdjArgs& a, cudaStream_t s);
+
+// k_limit_adj: lam_in = (dL/dq)^T lam_out for the positivity limiter L of
+// flux.f90:1077-1164 (limit_cell, the forward kernels' own code), one thread
+// per cell.  The limiter is cell-local and touches only the hydro rows; where
+// the forward bound test shows it inactive the map is the identity, elsewhere
+// one dual-number pass per hydro coefficient (5 nb columns) runs limit_cell
+// and gives the derivative of its active branch (the arg-min face point, the
+// clamp of theta, the floors).  lam_out is read in full before lam_in is
+// written, so the two may be one buffer.
+template <class TB>
+__global__ void __launch_bounds__(ADJ_TPB) k_limit_adj(const double* __restrict__ Q, const double* lam_out,
+                                                       double* lam_in, Geom G, Phys ph) {
+    constexpr int NB = TB::NB;
+    const long long le = (long long)blockIdx.x * ADJ_TPB + threadIdx.x;
+    if (le >= G.ncell) return;
+    const long long nc = G.boxes[0].ncell;
+    double q[5][NB], lo[5][NB];
+    sfor<5>([&](auto vv) {
+        constexpr int v = decltype(vv)::value;
+        sfor<NB>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            q[v][b] = Q[(long long)(b * NQ + v) * nc + le];
+            lo[v][b] = lam_out[(long long)(b * NQ + v) * nc + le];
+        });
+    });
+    if (lam_in != lam_out) {   // stress rows: the identity
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int v = PXX; v < NQ; ++v) lam_in[(long long)(b * NQ + v) * nc + le] = lam_out[(long long)(b * NQ + v) * nc + le];
+    }
+    if (q[RH][0] >= ph.rh_floor && limit_bound_clear<TB, double>(ph, q)) {
+        if (lam_in != lam_out)
+            sfor<5>([&](auto vv) {
+                constexpr int v = decltype(vv)::value;
+                sfor<NB>([&](auto bb) {
+                    constexpr int b = decltype(bb)::value;
+                    lam_in[(long long)(b * NQ + v) * nc + le] = lo[v][b];
+                });
+            });
+        return;
+    }
+#pragma unroll 1
+    for (int col = 0; col < 5 * NB; ++col) {
+        const int cv = col / NB, cb = col % NB;
+        Dual qd[5][NB];
+        sfor<5>([&](auto vv) {
+            constexpr int v = decltype(vv)::value;
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                qd[v][b] = Dual(q[v][b], (v == cv && b == cb) ? 1.0 : 0.0);
+            });
+        });
+        limit_cell<TB, Dual>(ph, qd);
+        double acc = 0.0;
+        sfor<5>([&](auto vv) {
+            constexpr int v = decltype(vv)::value;
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                acc = fma(lo[v][b], qd[v][b].d, acc);
+            });
+        });
+        lam_in[(long long)(cb * NQ + cv) * nc + le] = acc;
+    }
+}
+
+template <int NB, int NQD>
+cudaError_t limit_adj_launch(const double* Q, const double* lam_out, double* lam_in, const Geom& G, const Phys& ph,
+                             cudaStream_t s) {
+    using TB = hermes_tab::Tab<NB, NQD>;
+    if (G.ncell > 0) {
+        const unsigned nblk = (unsigned)((G.ncell + ADJ_TPB - 1) / ADJ_TPB);
+        k_limit_adj<TB><<<nblk, ADJ_TPB, 0, s>>>(Q, lam_out, lam_in, G, ph);
+    }
+    return cudaGetLastError();
+}
 
 // launcher of one basis: the three face-adjoint passes, then the cell pass
 template <int NB, int NQD>
@@ -428,18 +630,23 @@ cudaError_t adj_launch(const double* Q, const double* mu, double* tadj, double* 
         const long long n = a.G.nface[d];
         if (n <= 0) continue;
         dim3 grid((unsigned)((n + ADJ_TPB - 1) / ADJ_TPB), TB::NF);
-        if (a.dual) {   // forward-mode dual passes (the check on the reverse sweep)
-            if (d == 0) k_face_adj<TB, 0, false><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
-            else if (d == 1) k_face_adj<TB, 1, false><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
-            else k_face_adj<TB, 2, false><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+        if (a.dual == ADJ_GEN) {   // one dual pass per column (ivis 2, Tait EOS)
+            if (d == 0) k_face_adj<TB, 0, ADJ_GEN><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else if (d == 1) k_face_adj<TB, 1, ADJ_GEN><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else k_face_adj<TB, 2, ADJ_GEN><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+        } else if (a.dual) {   // forward-mode dual passes (the check on the reverse sweep)
+            if (d == 0) k_face_adj<TB, 0, ADJ_DUAL><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else if (d == 1) k_face_adj<TB, 1, ADJ_DUAL><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else k_face_adj<TB, 2, ADJ_DUAL><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
         } else {
-            if (d == 0) k_face_adj<TB, 0, true><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
-            else if (d == 1) k_face_adj<TB, 1, true><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
-            else k_face_adj<TB, 2, true><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            if (d == 0) k_face_adj<TB, 0, ADJ_REV><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else if (d == 1) k_face_adj<TB, 1, ADJ_REV><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
+            else k_face_adj<TB, 2, ADJ_REV><<<grid, ADJ_TPB, 0, s>>>(Q, mu, tadj, a);
         }
     }
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (a.dual == ADJ_GEN) return cell_adj_gen(NB, Q, mu, tadj, out, a, s);
     if (a.dual) return cell_adj_dual(NB, Q, mu, tadj, out, a, s);
     return cell_adj_rev(NB, Q, mu, tadj, out, a, s);
 }

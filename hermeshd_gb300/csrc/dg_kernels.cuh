@@ -637,6 +637,7 @@ struct CellArgs {
     const void* noise;  // staged interior stochastic stress (k_noise_cell), or null: drawn here
     void* accbuf;       // split update: k_cell stores the volume terms here, k_update finishes
     int limit_out;      // k_update (FP64): apply the next stage's positivity limiter to the output
+    int utpb = 0;       // threads per block of k_update (0: UPD_TPB)
 };
 
 // RK combination of integrator.f90:62-86
@@ -928,18 +929,7 @@ __device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T
             // sources nonlinear in the state, by quadrature (ivis 2: sources.f90:51-69)
             if (GRP == 1 && ph.ivis == 2) {
                 T s[NK][6];
-                sfor<NK>([&](auto kk) {
-                    constexpr int k = decltype(kk)::value;
-                    const Prim<T>& wk = w[k];
-                    const T vx2 = wk.vx * wk.vx, vy2 = wk.vy * wk.vy, vz2 = wk.vz * wk.vz;
-                    const T colldn = T(ph.coll) * wk.dn, c1d3 = T(1.0 / 3.0);
-                    s[k][0] = colldn * (T(2) * vx2 - vy2 - vz2) * c1d3;
-                    s[k][1] = colldn * (T(2) * vy2 - vz2 - vx2) * c1d3;
-                    s[k][2] = colldn * (T(2) * vz2 - vx2 - vy2) * c1d3;
-                    s[k][3] = colldn * wk.vx * wk.vy;
-                    s[k][4] = colldn * wk.vx * wk.vz;
-                    s[k][5] = colldn * wk.vy * wk.vz;
-                });
+                sfor<NK>([&](auto kk) { ten_moment_source<T>(ph, w[decltype(kk)::value], s[decltype(kk)::value]); });
                 sfor<NB>([&](auto bb) {
                     constexpr int b = decltype(bb)::value;
                     constexpr double cA = TB::SRC(gA, b), cB = TB::SRC(gB, b);
@@ -1286,7 +1276,8 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
 // through shared memory to the next stage's positivity limiter (k_limit's
 // operations, flux.f90:1077-1164), one thread per cell, before they are
 // stored: the reference limits that stage's input in place (integrator.f90:110).
-constexpr int UPD_TPB = 128;
+constexpr int UPD_TPB = 128;       // default threads per block of k_update
+constexpr int UPD_TPB_MAX = 256;
 constexpr int UPD_CPB = 16;
 
 // the limiter's full evaluation on rows in shared memory, out of line: the
@@ -1340,10 +1331,10 @@ __device__ __forceinline__ void update_cell_var(const T* Qin, const T* Q0, T* ou
 }
 
 template <class T, class TB>
-__global__ void __launch_bounds__(UPD_TPB) k_update(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux,
-                                                   CellArgs a) {
+__global__ void __launch_bounds__(UPD_TPB_MAX) k_update(const T* Qin, const T* Q0, T* out, const T* __restrict__ flux,
+                                                       CellArgs a) {
     pdl_enter();
-    const long long gc = (long long)blockIdx.x * UPD_TPB + threadIdx.x;
+    const long long gc = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (gc >= a.G.ncell) return;
     update_cell_var<T, TB>(Qin, Q0, out, flux, a, gc, blockIdx.y, nullptr, 0);
 }

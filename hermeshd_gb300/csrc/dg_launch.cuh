@@ -157,8 +157,9 @@ struct Launch {
                         return;
                     }
                 }
-                const dim3 grid((unsigned)((a.G.ncell + UPD_TPB - 1) / UPD_TPB), NQ);
-                launch_k(a.G.pdl, k_update<T, TB>, grid, UPD_TPB, 0, s, qi, q0, o, f, a);
+                const int ut = a.utpb > 0 ? a.utpb : UPD_TPB;
+                const dim3 grid((unsigned)((a.G.ncell + ut - 1) / ut), NQ);
+                launch_k(a.G.pdl, k_update<T, TB>, grid, ut, 0, s, qi, q0, o, f, a);
                 return;
             }
         }
@@ -197,16 +198,25 @@ bool kernel_set(int precision, int nb, bool noise, KernelSet* out);
 // ---- adjoint of the right-hand side (FP64, one box; dg_adjoint.cuh) ----
 constexpr int ADJ_TPB = 64;
 
+// how the point-wise Jacobians are formed (the values of AdjArgs::dual)
+enum AdjMode { ADJ_REV = 0, ADJ_DUAL = 1, ADJ_GEN = 2 };
+
 struct AdjArgs {
     Geom G;
     Phys ph;
     const BoxState* st;
     int mode;       // 0: out = nu = (dR/dQ)^T mu; 1: out = mu - dt*nu
-    int dual;       // face flux VJP by forward-mode dual passes instead of the reverse sweep
+    int dual;       // AdjMode: 0 reverse sweeps, 1 their dual-number check, 2 one dual pass per column
+    double* cpart;  // per-block partials of mu . dR/dcoll (ceil(ncell / ADJ_TPB)), or null
+    const unsigned long long* nstep;   // stochastic stress: the step counter and stage index of the
+    unsigned nstage;                   // realisation held fixed (those of the forward stage)
 };
 
 // (Q, mu, trace-adjoint scratch of 2x the face-flux size, out, args, stream)
 using AdjFn = cudaError_t (*)(const double*, const double*, double*, double*, const AdjArgs&, cudaStream_t);
 bool adjoint_launcher(int nb, AdjFn* out);
+// (Q, lam_out, lam_in, grid, physics, stream): the positivity limiter's VJP
+using LimAdjFn = cudaError_t (*)(const double*, const double*, double*, const Geom&, const Phys&, cudaStream_t);
+bool limiter_adjoint_launcher(int nb, LimAdjFn* out);
 
 }  // namespace hermes

@@ -225,6 +225,21 @@ __device__ __forceinline__ void point_flux(const Phys& ph, const T q[NQ], const 
     }
 }
 
+// sources.f90:51-69: the ivis 2 point source of the stresses,
+// coll rho (v_i v_j - delta_ij |v|^2 / 3), S = {xx, yy, zz, xy, xz, yz}
+// (shared by the cell kernel and the adjoint's dual passes)
+template <class T>
+__device__ __forceinline__ void ten_moment_source(const Phys& ph, const Prim<T>& w, T s[6]) {
+    const T vx2 = w.vx * w.vx, vy2 = w.vy * w.vy, vz2 = w.vz * w.vz;
+    const T colldn = T(ph.coll) * w.dn, c1d3 = T(1.0 / 3.0);
+    s[0] = colldn * (T(2) * vx2 - vy2 - vz2) * c1d3;
+    s[1] = colldn * (T(2) * vy2 - vz2 - vx2) * c1d3;
+    s[2] = colldn * (T(2) * vz2 - vx2 - vy2) * c1d3;
+    s[3] = colldn * w.vx * w.vy;
+    s[4] = colldn * w.vx * w.vz;
+    s[5] = colldn * w.vy * w.vz;
+}
+
 // flux.f90:1029-1072 cfcal: freezing speed |v_d| + c
 template <class T, int DIR>
 __device__ __forceinline__ T cfcal(const Phys& ph, const T q[NQ]) {

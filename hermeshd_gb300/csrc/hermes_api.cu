@@ -62,20 +62,36 @@ __global__ void k_dt_finalize(const Box* __restrict__ boxes, int nbox, BoxState*
     st[b].vmag_bits = 0ull;
 }
 
-// adjoint stage prologue: mu = M lam_out, where M is the semi-implicit factor
-// faci on the stresses for ivis 1 (integrator.f90:174), and per-block partial
-// sums of dL/dcoll = sum_stress lam_out * dE/dcoll = sum lam_out * (-dt faci E_out)
+// adjoint stage prologue.  The stage is E = M y, y = q_in - dt R(q_in), with
+// M the semi-implicit stress factor: faci = 1/(1 + dt coll) on the stresses
+// for ivis 1 (integrator.f90:174); for ivis 2 faci on the off-diagonal
+// stresses and faci (I + (coll dt / 3) J) on (pxx, pyy, pzz), J the 3x3 matrix
+// of ones (integrator.f90:207-224); the identity elsewhere.  M is symmetric:
+// mu = M lam_out.  Per-block partial sums of lam_out . (dM/dcoll) y, which,
+// since sum_d y_d = sum_d E_d on the diagonal (1 + 3 coll dt / 3 = 1 / faci),
+// is lam_out . (-dt faci E) on the stresses plus, on the diagonal ones,
+// lam_out_d faci (dt / 3) sum_k E_k.
 __global__ void __launch_bounds__(256) k_stage_pre(const double* __restrict__ lam_out, const double* __restrict__ e_out,
                                                    double* __restrict__ mu, double* __restrict__ part, long long n,
-                                                   long long ncell, int ivis, double dt, double faci) {
+                                                   long long ncell, int ivis, double dt, double faci, double c3) {
     __shared__ double red[256];
     const long long e = (long long)blockIdx.x * 256 + threadIdx.x;
     double c = 0.0;
     if (e < n) {
         const int v = (int)((e / ncell) % NQ);
-        const bool stress = v >= PXX && ivis == 1;
-        mu[e] = stress ? faci * lam_out[e] : lam_out[e];
-        if (stress && e_out) c = lam_out[e] * (-dt * faci * e_out[e]);
+        const bool stress = v >= PXX && (ivis == 1 || ivis == 2);
+        if (ivis == 2 && v >= PXX && v <= PZZ) {
+            const long long d0 = e - (long long)(v - PXX) * ncell;   // pxx of the same coefficient and cell
+            const double ls = lam_out[d0] + lam_out[d0 + ncell] + lam_out[d0 + 2 * ncell];
+            mu[e] = faci * fma(c3, ls, lam_out[e]);
+            if (e_out) {
+                const double es = e_out[d0] + e_out[d0 + ncell] + e_out[d0 + 2 * ncell];
+                c = lam_out[e] * faci * fma(-dt, e_out[e], dt * (1.0 / 3.0) * es);
+            }
+        } else {
+            mu[e] = stress ? faci * lam_out[e] : lam_out[e];
+            if (stress && e_out) c = lam_out[e] * (-dt * faci * e_out[e]);
+        }
     }
     red[threadIdx.x] = c;
     __syncthreads();
@@ -146,6 +162,7 @@ struct hermes_ctx {
     long long prof_n[NKIND] = {};
     // launch shape (hermes_set_launch); 0 = the compiled defaults
     int face_tpb = 0, dt_tpb = 0, graph_steps = 1;
+    int update_tpb = UPD_TPB, update_tpb_default = UPD_TPB;   // threads per block of k_update
     // stochastic stress staged in HBM by its own kernels (dg_noise.cuh)
     bool noise_staged = false;
     NoiseFn noise_fn = nullptr;
@@ -174,12 +191,14 @@ struct hermes_ctx {
     // (k_face); 1 the three directions in one launch (k_faces); 2 one launch
     // per direction, thread per face looping over its points (k_face_pl)
     int face_mode = 1;
+    unsigned noise_stage = 0;   // stage index of the counters hermes_rhs / euler_stage / the VJPs draw with
     // adjoint scratch, allocated on first use
     AdjFn adj = nullptr;
     double* d_tadj = nullptr;   // trace adjoints: 2 x the face-flux size
     double* d_mu = nullptr;     // M lam of a stage
-    double* d_part = nullptr;   // partial sums of dL/dcoll
-    double* d_sum = nullptr;
+    double* d_part = nullptr;   // partial sums of dL/dcoll (stage factor)
+    double* d_cpart = nullptr;  // partial sums of dL/dcoll (right-hand side)
+    double* d_sum = nullptr;    // the two sums
     int npart = 0;
 };
 
@@ -358,7 +377,8 @@ void enq_cell(hermes_ctx* c, const void* qin, const void* q0, void* out, int mod
               int limit_out = 0) {
     const int split = (mode == MODE_STAGE && c->cfg.ivis == 3 && c->cfg.iorder == 2) ? 1 : 0;
     CellArgs a{c->G, c->ph, c->d_st, c->d_step, c->d_flags, stage, mode, comb, split,
-               c->noise_staged ? c->d_noise_cell : nullptr, c->split_update ? c->d_accbuf : nullptr, limit_out};
+               c->noise_staged ? c->d_noise_cell : nullptr, c->split_update ? c->d_accbuf : nullptr, limit_out,
+               c->update_tpb};
     ProfScope ps(c, 5);
     c->K.cell(qin, q0, out, c->d_flux, a, c->stream);
 }
@@ -576,6 +596,8 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     // tails), in FP32 with a thread per face point (the merged kernel spills
     // under FP32's register cap)
     c->face_mode = cfg->nbasis == 4 ? 2 : cfg->precision == 64 ? 1 : 0;
+    // k_update: 64 threads per block in FP32 (measured 4 % faster on the 128^2 vortex step), 128 in FP64
+    c->update_tpb_default = c->update_tpb = cfg->precision == 32 ? 64 : UPD_TPB;
     c->G.pdl = 0;   // programmatic dependent launch measured neutral here: an autotuned option
     c->G.ncell = ncell;
     for (int d = 0; d < 3; ++d) c->G.nface[d] = nface[d];
@@ -756,6 +778,7 @@ int hermes_destroy(hermes_ctx* c) {
     cudaFree(c->d_tadj);
     cudaFree(c->d_mu);
     cudaFree(c->d_part);
+    cudaFree(c->d_cpart);
     cudaFree(c->d_sum);
     cudaFree(c->d_len);
     cudaFree(c->d_cons_map);
@@ -805,12 +828,12 @@ int hermes_rhs(hermes_ctx* c, void* q, void* rhs, int apply_limiter) {
     if (rc) return rc;
     if (apply_limiter) enq_limit(c, q);
     if (c->tile_stage) {
-        enq_tile(c, q, nullptr, rhs, MODE_RHS, COMB_NONE, 0, 0);
+        enq_tile(c, q, nullptr, rhs, MODE_RHS, COMB_NONE, c->noise_stage, 0);
         return leave(c, launch_status(c));
     }
-    enq_noise(c, 0);
-    enq_faces(c, q, 0);
-    enq_cell(c, q, nullptr, rhs, MODE_RHS, COMB_NONE, 0);
+    enq_noise(c, c->noise_stage);
+    enq_faces(c, q, c->noise_stage);
+    enq_cell(c, q, nullptr, rhs, MODE_RHS, COMB_NONE, c->noise_stage);
     return leave(c, launch_status(c));
 }
 
@@ -820,7 +843,7 @@ int hermes_euler_stage(hermes_ctx* c, void* q_in, void* q_out, double dt) {
     if (rc) return rc;
     const int nb = c->G.nbox;
     k_set_dt<<<(nb + 127) / 128, 128, 0, c->stream>>>(c->d_st, nb, dt);
-    enq_stage(c, q_in, nullptr, q_out, COMB_NONE, 0);
+    enq_stage(c, q_in, nullptr, q_out, COMB_NONE, c->noise_stage);
     return leave(c, launch_status(c));
 }
 
@@ -994,9 +1017,11 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     const bool tile = l->tile_stage == 1;
     if (l->pdl != 0 && l->pdl != 1) return fail(c, HERMES_ERR_ARG, "pdl must be 0 or 1");
     if (l->faces_merged < 0 || l->faces_merged > 2) return fail(c, HERMES_ERR_ARG, "faces_merged must be 0, 1 or 2");
+    const int u = l->update_tpb ? l->update_tpb : c->update_tpb_default;
+    if (u != 0 && u != 64 && u != 128 && u != 256) return fail(c, HERMES_ERR_ARG, "update_tpb must be 0, 64, 128 or 256");
     if (f != c->face_tpb || d != c->dt_tpb || staged != c->noise_staged || traces != c->face_traces ||
         split != c->split_update || tile != c->tile_stage || l->pdl != c->G.pdl ||
-        l->faces_merged != c->face_mode) {
+        l->faces_merged != c->face_mode || u != c->update_tpb) {
         // captured graphs hold the old launch shape
         HCK(c, cudaSetDevice(c->device));
         HCK(c, cudaStreamSynchronize(c->stream));
@@ -1011,6 +1036,7 @@ int hermes_set_launch(hermes_ctx* c, const hermes_launch* l) {
     c->tile_stage = tile;
     c->G.pdl = l->pdl;
     c->face_mode = l->faces_merged;
+    c->update_tpb = u;
     return HERMES_OK;
 }
 
@@ -1025,6 +1051,7 @@ int hermes_get_launch(hermes_ctx* c, hermes_launch* l) {
     l->tile_stage = c->tile_stage ? 1 : 0;
     l->pdl = c->G.pdl;
     l->faces_merged = c->face_mode;
+    l->update_tpb = c->update_tpb;
     return HERMES_OK;
 }
 
@@ -1103,6 +1130,13 @@ int hermes_set_noise_step(hermes_ctx* c, uint64_t step) {
     return leave(c, launch_status(c));
 }
 
+int hermes_set_noise_stage(hermes_ctx* c, int32_t stage) {
+    if (!c) return HERMES_ERR_ARG;
+    if (stage < 0 || stage > 2) return fail(c, HERMES_ERR_ARG, "stage must be 0, 1 or 2");
+    c->noise_stage = (unsigned)stage;
+    return HERMES_OK;
+}
+
 int hermes_check(hermes_ctx* c) {
     if (!c) return HERMES_ERR_ARG;
     int rc = enter(c);
@@ -1117,9 +1151,9 @@ namespace {
 std::string adjoint_unsupported(const hermes_config& c, int nbox) {
     if (c.precision != 64) return "the adjoint is FP64 only";
     if (nbox != 1) return "the adjoint takes a single grid";
-    if (c.llns) return "the adjoint does not model the stochastic stress";
-    if (c.ivis != 0 && c.ivis != 1) return "the adjoint supports ivis 0 and 1";
-    if (c.ieos != 1) return "the adjoint supports ieos 1";
+    if (c.ivis < 0 || c.ivis > 2) return "the adjoint supports ivis 0, 1 and 2";
+    if (c.ieos == 2 && c.ihllc == 1)
+        return "the adjoint does not take HLLC with ieos 2 (its sound speed uses 1/rho of another face point)";
     if (c.bc[0] == HERMES_BC_INFLOW) return "the adjoint does not model the inflow boundary";
     for (int d = 0; d < 3; ++d)
         if ((c.bc[2 * d] == HERMES_BC_PERIODIC) != (c.bc[2 * d + 1] == HERMES_BC_PERIODIC))
@@ -1127,11 +1161,15 @@ std::string adjoint_unsupported(const hermes_config& c, int nbox) {
     return "";
 }
 
-// HERMES_ADJOINT_DUAL=1: the face flux VJP by forward-mode dual passes, the
-// independent check on the hand-derived reverse sweep
-int adjoint_dual() {
+// the point-wise Jacobians (AdjMode): the hand-derived reverse sweeps cover
+// ivis 0/1 with ieos 1 and no stochastic stress; ivis 2, the Tait equation of
+// state and the stochastic stress take one dual pass per column.
+// HERMES_ADJOINT_DUAL=1 selects the dual-number check of the reverse sweeps
+// (those cases), =2 the per-column passes for any case.
+int adjoint_mode(const hermes_config& c) {
     const char* e = std::getenv("HERMES_ADJOINT_DUAL");
-    return (e && e[0] == '1') ? 1 : 0;
+    if (c.ivis == 2 || c.ieos == 2 || c.llns || (e && e[0] == '2')) return ADJ_GEN;
+    return (e && e[0] == '1') ? ADJ_DUAL : ADJ_REV;
 }
 
 int adj_prepare(hermes_ctx* c) {
@@ -1143,7 +1181,8 @@ int adj_prepare(hermes_ctx* c) {
         if (cudaMalloc(&c->d_tadj, 2 * c->flux_elems * sizeof(double)) != cudaSuccess ||
             cudaMalloc(&c->d_mu, c->q_elems * sizeof(double)) != cudaSuccess ||
             cudaMalloc(&c->d_part, (size_t)c->npart * sizeof(double)) != cudaSuccess ||
-            cudaMalloc(&c->d_sum, sizeof(double)) != cudaSuccess) {
+            cudaMalloc(&c->d_cpart, (size_t)((c->G.ncell + ADJ_TPB - 1) / ADJ_TPB) * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&c->d_sum, 2 * sizeof(double)) != cudaSuccess) {
             cudaGetLastError();
             return fail(c, HERMES_ERR_ALLOC, "adjoint scratch");
         }
@@ -1159,10 +1198,25 @@ int hermes_rhs_vjp(hermes_ctx* c, const void* q, const void* mu, void* nu) {
     if (rc) return rc;
     rc = adj_prepare(c);
     if (rc) return leave(c, rc);
-    AdjArgs a{c->G, c->ph, c->d_st, 0, adjoint_dual()};
+    AdjArgs a{c->G, c->ph, c->d_st, 0, adjoint_mode(c->cfg), nullptr, c->d_step, c->noise_stage};
     cudaError_t e = c->adj(static_cast<const double*>(q), static_cast<const double*>(mu), c->d_tadj,
                            static_cast<double*>(nu), a, c->stream);
     if (e != cudaSuccess) return leave(c, cuda_fail(c, "adjoint launch", e));
+    return leave(c, HERMES_OK);
+}
+
+int hermes_limiter_vjp(hermes_ctx* c, const void* q, const void* lam_out, void* lam_in) {
+    if (!c || !q || !lam_out || !lam_in) return fail(c, HERMES_ERR_ARG, "null argument");
+    if (lam_in == q) return fail(c, HERMES_ERR_ARG, "lam_in must not alias q");
+    int rc = enter(c);
+    if (rc) return rc;
+    rc = adj_prepare(c);
+    if (rc) return leave(c, rc);
+    LimAdjFn fn = nullptr;
+    if (!limiter_adjoint_launcher(c->cfg.nbasis, &fn)) return leave(c, fail(c, HERMES_ERR_CONFIG, "no limiter adjoint for this basis"));
+    cudaError_t e = fn(static_cast<const double*>(q), static_cast<const double*>(lam_out), static_cast<double*>(lam_in),
+                       c->G, c->ph, c->stream);
+    if (e != cudaSuccess) return leave(c, cuda_fail(c, "limiter adjoint launch", e));
     return leave(c, HERMES_OK);
 }
 
@@ -1171,7 +1225,6 @@ int hermes_stage_vjp(hermes_ctx* c, const void* q_in, const void* e_out, const v
     if (!c || !q_in || !lam_out || !lam_in) return fail(c, HERMES_ERR_ARG, "null argument");
     if (lam_in == q_in || (e_out && lam_in == e_out)) return fail(c, HERMES_ERR_ARG, "lam_in must not alias q_in or e_out");
     if (dcoll && !e_out) return fail(c, HERMES_ERR_ARG, "dcoll needs e_out");
-    if (dcoll && c->cfg.ivis != 1) return fail(c, HERMES_ERR_CONFIG, "dcoll is defined for ivis 1 (coll enters through faci)");
     if (!(dt > 0.0)) return fail(c, HERMES_ERR_ARG, "dt must be positive");
     int rc = enter(c);
     if (rc) return rc;
@@ -1181,14 +1234,22 @@ int hermes_stage_vjp(hermes_ctx* c, const void* q_in, const void* e_out, const v
     const long long n = (long long)c->q_elems;
     const double faci = 1.0 / (1.0 + dt * c->cfg.coll);
     k_stage_pre<<<c->npart, 256, 0, c->stream>>>(static_cast<const double*>(lam_out), static_cast<const double*>(e_out),
-                                                 c->d_mu, c->d_part, n, c->G.ncell, c->cfg.ivis, dt, faci);
+                                                 c->d_mu, c->d_part, n, c->G.ncell, c->cfg.ivis, dt, faci,
+                                                 c->cfg.coll * dt * (1.0 / 3.0));
     if (dcoll) k_sum_partials<<<1, 256, 0, c->stream>>>(c->d_part, c->npart, c->d_sum);
-    AdjArgs a{c->G, c->ph, c->d_st, 1, adjoint_dual()};
+    // R depends on coll for ivis 0 and 2: the cell pass adds mu . dR/dcoll
+    const bool r_coll = dcoll && (c->cfg.ivis == 0 || c->cfg.ivis == 2);
+    AdjArgs a{c->G, c->ph, c->d_st, 1, adjoint_mode(c->cfg), r_coll ? c->d_cpart : nullptr, c->d_step, c->noise_stage};
     cudaError_t e = c->adj(static_cast<const double*>(q_in), c->d_mu, c->d_tadj, static_cast<double*>(lam_in), a, c->stream);
     if (e != cudaSuccess) return leave(c, cuda_fail(c, "adjoint launch", e));
     if (dcoll) {
-        HCK(c, cudaMemcpyAsync(dcoll, c->d_sum, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        if (r_coll)
+            k_sum_partials<<<1, 256, 0, c->stream>>>(c->d_cpart, (int)((c->G.ncell + ADJ_TPB - 1) / ADJ_TPB), c->d_sum + 1);
+        double h[2] = {0.0, 0.0};
+        HCK(c, cudaMemcpyAsync(h, c->d_sum, (r_coll ? 2 : 1) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         HCK(c, cudaStreamSynchronize(c->stream));
+        // lam_out . dE/dcoll = lam_out . (dM/dcoll) y + (M lam_out) . (-dt dR/dcoll)
+        *dcoll = h[0] - dt * h[1];
     }
     return leave(c, launch_status(c));
 }

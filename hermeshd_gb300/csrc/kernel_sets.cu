@@ -171,11 +171,34 @@ cudaError_t cell_adj_rev(int nb, const double* Q, const double* mu, const double
     return cell_adj_rev_nb10(Q, mu, tadj, out, a, s);
 }
 
+cudaError_t cell_adj_gen_nb4(const double*, const double*, const double*, double*, const AdjArgs&, cudaStream_t);
+cudaError_t cell_adj_gen_nb8(const double*, const double*, const double*, double*, const AdjArgs&, cudaStream_t);
+cudaError_t cell_adj_gen_nb10(const double*, const double*, const double*, double*, const AdjArgs&, cudaStream_t);
+
+cudaError_t cell_adj_gen(int nb, const double* Q, const double* mu, const double* tadj, double* out,
+                         const AdjArgs& a, cudaStream_t s) {
+    if (nb == 4) return cell_adj_gen_nb4(Q, mu, tadj, out, a, s);
+    if (nb == 8) return cell_adj_gen_nb8(Q, mu, tadj, out, a, s);
+    return cell_adj_gen_nb10(Q, mu, tadj, out, a, s);
+}
+
 cudaError_t cell_adj_dual(int nb, const double* Q, const double* mu, const double* tadj, double* out,
                           const AdjArgs& a, cudaStream_t s) {
     if (nb == 4) return cell_adj_dual_nb4(Q, mu, tadj, out, a, s);
     if (nb == 8) return cell_adj_dual_nb8(Q, mu, tadj, out, a, s);
     return cell_adj_dual_nb10(Q, mu, tadj, out, a, s);
+}
+
+cudaError_t limit_adj_f64_nb4(const double*, const double*, double*, const Geom&, const Phys&, cudaStream_t);
+cudaError_t limit_adj_f64_nb8(const double*, const double*, double*, const Geom&, const Phys&, cudaStream_t);
+cudaError_t limit_adj_f64_nb10(const double*, const double*, double*, const Geom&, const Phys&, cudaStream_t);
+
+bool limiter_adjoint_launcher(int nb, LimAdjFn* out) {
+    if (nb == 4) *out = &limit_adj_f64_nb4;
+    else if (nb == 8) *out = &limit_adj_f64_nb8;
+    else if (nb == 10) *out = &limit_adj_f64_nb10;
+    else return false;
+    return true;
 }
 
 bool adjoint_launcher(int nb, AdjFn* out) {

@@ -99,10 +99,18 @@ class Solver:
         check(lib().hermes_rhs_vjp(self.ctx, self._ptr(q), self._ptr(mu), self._ptr(out)), self.ctx)
         return out
 
+    def limiter_vjp(self, q, lam_out, out=None):
+        """(dL/dq)^T lam_out for the positivity limiter L applied in place at
+        q (the stage input before limiting): the derivative of the branch it
+        takes there.  out may be lam_out."""
+        out = self.new_state() if out is None else out
+        check(lib().hermes_limiter_vjp(self.ctx, self._ptr(q), self._ptr(lam_out), self._ptr(out)), self.ctx)
+        return out
+
     def stage_vjp(self, q_in, lam_out, dt: float, e_out=None, want_dcoll: bool = False, out=None):
         """(dE/dq_in)^T lam_out for the forward-Euler stage E of
         euler_stage(q_in, dt) (limiter inactive); with want_dcoll also
-        lam_out . dE/dcoll (ivis 1, needs e_out = E(q_in)).  Returns
+        lam_out . dE/dcoll (needs e_out = E(q_in); synchronises).  Returns
         (lam_in, dcoll or None)."""
         out = self.new_state() if out is None else out
         dc = C.c_double(0.0)
@@ -177,11 +185,11 @@ class Solver:
         return {"face_tpb": l.face_tpb, "dt_tpb": l.dt_tpb, "steps_per_graph": l.steps_per_graph,
                 "noise_inline": l.noise_inline, "face_traces": l.face_traces, "split_update": l.split_update,
                 "tile_stage": l.tile_stage, "pdl": l.pdl,
-                "faces_merged": l.faces_merged}
+                "faces_merged": l.faces_merged, "update_tpb": l.update_tpb}
 
     def set_launch(self, face_tpb: int = 0, dt_tpb: int = 0, steps_per_graph: int = 1, noise_inline: int = 0,
                    face_traces=None, split_update=None, tile_stage=None, pdl=None,
-                   faces_merged=None):
+                   faces_merged=None, update_tpb: int = 0):
         """face_traces / split_update / tile_stage None keep the context's
         current choice (the trace kernel and the split update are on by
         default where they exist: FP64 nbasis 8/10 without the stochastic
@@ -189,7 +197,9 @@ class Solver:
         default); pdl None keeps the current choice (off by default); faces_merged None keeps
         the current choice (1: one launch for three directions, the default for
         nbasis 8/10 in FP64; 0: one per direction, nbasis 8/10 in FP32; 2: one
-        per direction with a thread per face looping over its points, nbasis 4)."""
+        per direction with a thread per face looping over its points, nbasis 4);
+        update_tpb: threads per block of the split update (0: the default,
+        64 in FP32, 128 in FP64)."""
         cur = self.get_launch()
         if face_traces is None:
             face_traces = cur["face_traces"]
@@ -202,11 +212,16 @@ class Solver:
         if faces_merged is None:
             faces_merged = cur["faces_merged"]
         l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), int(noise_inline), int(face_traces),
-                              int(split_update), int(tile_stage), int(pdl), int(faces_merged))
+                              int(split_update), int(tile_stage), int(pdl), int(faces_merged), int(update_tpb))
         check(lib().hermes_set_launch(self.ctx, C.byref(l)), self.ctx)
 
     def set_noise_step(self, step: int):
         check(lib().hermes_set_noise_step(self.ctx, int(step)), self.ctx)
+
+    def set_noise_stage(self, stage: int):
+        """Stage index (0..2) of the stochastic-stress draw of rhs,
+        euler_stage and the VJPs (step and advance count their own stages)."""
+        check(lib().hermes_set_noise_stage(self.ctx, int(stage)), self.ctx)
 
     def set_time(self, t: float):
         check(lib().hermes_set_time(self.ctx, float(t)), self.ctx)

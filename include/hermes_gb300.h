@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define HERMES_ABI_VERSION 6
+#define HERMES_ABI_VERSION 7
 
 typedef enum hermes_status {
     HERMES_OK = 0,
@@ -243,6 +243,9 @@ typedef struct hermes_launch {
                                 8/10 in FP32); 2 one launch per direction, thread per face looping
                                 over its points (nbasis 4; needs the stochastic stress drawn in
                                 place or absent and no trace buffer, else as 0).  Bit-identical. */
+    int32_t update_tpb;      /* threads per block of the split update's k_update (one thread per cell
+                                and variable): 64, 128 or 256; 0 the default (64 in FP32, 128 in
+                                FP64).  Bit-identical. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
 int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);
@@ -265,6 +268,11 @@ int hermes_set_time(hermes_ctx *ctx, double t);
 /* Step counter of the stochastic-stress Philox stream (the number of
  * completed steps; stages are counted within a step). */
 int hermes_set_noise_step(hermes_ctx *ctx, uint64_t step);
+/* Stage index (0, 1 or 2; default 0) of the Philox counters with which
+ * hermes_rhs, hermes_euler_stage and the adjoint entry points draw the
+ * stochastic stress; with hermes_set_noise_step it names the draw of any
+ * stage of any step (hermes_step and hermes_advance count their own stages). */
+int hermes_set_noise_stage(hermes_ctx *ctx, int32_t stage);
 
 /* Device error flags raised since the last call (HERMES_ERR_NONFINITE if a
  * NaN cell average was produced), cleared on read.  Synchronises. */
@@ -297,21 +305,35 @@ int hermes_rhs_noalloc(const hermes_config *cfg, void *q, void *rhs, int apply_l
                        size_t errlen);
 
 /* Adjoint of the right-hand side and of one forward-Euler stage (FP64, one
- * grid, ivis 0 or 1, ieos 1, no stochastic stress; a direction is periodic at
- * both ends or at neither).  No counterpart in the reference, which has no
- * derivatives; the forward map they differentiate is hermes_rhs without the
- * limiter (flux.f90:932-1022, sources.f90:12-84) and the update of
- * integrator.f90:147-174.  Branches (HLLC wave selection, floors, outflow
- * ghosts) are differentiated on their active side.
+ * grid, ivis 0, 1 or 2, ieos 1 or 2 but not ieos 2 with HLLC; a direction is
+ * periodic at both ends or at neither).  With the stochastic stress on, the
+ * realisation is held fixed: the one of the context's noise counters
+ * (hermes_set_noise_step, hermes_set_noise_stage), as hermes_rhs and
+ * hermes_euler_stage draw it.  No
+ * counterpart in the reference, which has no derivatives; the forward map
+ * they differentiate is hermes_rhs without the limiter (flux.f90:932-1022,
+ * sources.f90:12-84) and the update of integrator.f90:147-224.  Branches
+ * (HLLC wave selection, Roe |lambda|, the LLF maximum, floors, outflow
+ * ghosts) are differentiated on their active side.  ivis 0/1 with ieos 1 use
+ * hand-derived reverse sweeps; ivis 2, ieos 2 and the stochastic stress one
+ * dual-number pass per column of every variable through the forward physics.
  *
  * hermes_rhs_vjp: nu = (dR/dq)^T mu for R = hermes_rhs(q) (apply_limiter 0).
  * hermes_stage_vjp: lam_in = (dE/dq_in)^T lam_out for the stage
- * E(q_in) = M (q_in - dt R(q_in)), M = 1/(1 + dt coll) on the stresses for
- * ivis 1 and 1 elsewhere.  e_out = E(q_in) (may be NULL when dcoll is NULL);
- * dcoll, if not NULL, receives lam_out . dE/dcoll (ivis 1), and the call then
- * synchronises.  lam_in may alias lam_out.  Scratch (2x the face-flux size
+ * E(q_in) = M (q_in - dt R(q_in)), M = faci = 1/(1 + dt coll) on the
+ * stresses for ivis 1; for ivis 2 faci on the off-diagonal stresses and
+ * faci (I + (coll dt / 3) J) on (pxx, pyy, pzz), J the 3x3 matrix of ones;
+ * the identity elsewhere.  e_out = E(q_in) (may be NULL when dcoll is NULL);
+ * dcoll, if not NULL, receives lam_out . dE/dcoll (through M for ivis 1 and
+ * 2, through R for ivis 0 and 2), and the call then synchronises.  lam_in may alias lam_out.  Scratch (2x the face-flux size
  * plus one field) is allocated on the first call. */
 int hermes_rhs_vjp(hermes_ctx *ctx, const void *q, const void *mu, void *nu);
+/* lam_in = (dL/dq)^T lam_out for the positivity limiter L (flux.f90:1077-1164)
+ * applied in place at q, the stage input before limiting: the derivative of the
+ * branch the limiter takes at q (identity where it leaves the cell unchanged;
+ * the arg-min face point, the clamp of theta and the floors followed as the
+ * forward pass takes them).  lam_in may alias lam_out, not q. */
+int hermes_limiter_vjp(hermes_ctx *ctx, const void *q, const void *lam_out, void *lam_in);
 int hermes_stage_vjp(hermes_ctx *ctx, const void *q_in, const void *e_out, const void *lam_out, void *lam_in, double dt,
                      double *dcoll);
 
