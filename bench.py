@@ -57,7 +57,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--ensemble-accuracy", type=int, default=0, metavar="STEPS",
                     help="only the FP32-vs-FP64 ensemble-mean accuracy of the timed 256-box draw (Roe) over "
-                         "STEPS steps of the ensemble configuration's 500, printed as one JSON line")
+                         "STEPS steps of the ensemble configuration's 500, with the density S(k) accumulated "
+                         "every 10 steps in both precisions, printed as one JSON line")
     return ap.parse_args()
 
 
@@ -735,17 +736,33 @@ def time_ensemble(base, dims, K, flush, ws, tune=True):
     return out, cells, dof
 
 
-def ensemble_accuracy(base, dims, steps):
+def ensemble_accuracy(base, dims, steps, sk_every=0):
     """Relative L2 error of the ensemble-averaged density field of the FP32
     batched run against the same ensemble in FP64 (same draw, seeds and
     steps from the same equilibrium), per box size; and the density S(k) of
-    the FP64 run."""
+    the FP64 run.  sk_every > 0: the static structure factor of the density
+    accumulated every sk_every steps over the run, for both precisions, with
+    each run's wall time (steps and accumulation)."""
     import torch
     from hermeshd_gb300.analysis import StructureFactor
-    states = {}
+    states, acc, wall = {}, {}, {}
     for prec in ("fp32", "fp64"):
         ens, q, q1 = make_ensemble(base.replace(precision=prec), dims)
-        ens.advance(q, q1, steps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if sk_every > 0:
+            sfa = StructureFactor(kmax=8)
+            done = 0
+            while done < steps:
+                k = min(sk_every, steps - done)
+                ens.advance(q, q1, k)
+                done += k
+                sfa.add_state(q, base.nbasis, dims, ens.offsets)
+            acc[prec] = sfa
+        else:
+            ens.advance(q, q1, steps)
+        torch.cuda.synchronize()
+        wall[prec] = time.perf_counter() - t0
         states[prec] = (ens, q)
     err = {}
     sizes = [d[0] for d in dims]
@@ -762,8 +779,16 @@ def ensemble_accuracy(base, dims, steps):
     e64.close()
     del states, q32, q64
     torch.cuda.empty_cache()
-    return {"boxes": len(dims), "steps": steps, "rel_l2_ensemble_mean_density_vs_fp64": err,
-            "max_rel_l2": max(err.values()), "density_S_k_fp64": {int(k): v for k, v in sf.result().items()}}
+    out = {"boxes": len(dims), "steps": steps, "rel_l2_ensemble_mean_density_vs_fp64": err,
+           "max_rel_l2": max(err.values()), "density_S_k_fp64": {int(k): v for k, v in sf.result().items()}}
+    if sk_every > 0:
+        r32, r64 = acc["fp32"].result(), acc["fp64"].result()
+        out["S_k_accumulated"] = {
+            "every_steps": sk_every, "samples_per_box": acc["fp32"].samples // len(dims),
+            "fp32": {int(k): v for k, v in r32.items()}, "fp64": {int(k): v for k, v in r64.items()},
+            "max_rel_diff_fp32_vs_fp64": max(abs(r32[k] - r64[k]) / abs(r64[k]) for k in r64),
+            "wall_s": wall}
+    return out
 
 
 def ensembles(args, flush, ws, acc_steps=40, acc_steps_hllc=20):
@@ -880,7 +905,7 @@ def main():
             from hermeshd_gb300 import config
             t0 = time.perf_counter()
             acc = ensemble_accuracy(config.fh_box(48, precision="fp32", seed=0), ensemble_draw(),
-                                    args.ensemble_accuracy)
+                                    args.ensemble_accuracy, sk_every=10)
             acc["wall_s"] = time.perf_counter() - t0
             print(json.dumps({"ensemble_accuracy": acc}))
         return 0

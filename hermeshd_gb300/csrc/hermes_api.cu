@@ -595,7 +595,10 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     // FP64 with the three directions in one launch (they fill each other's
     // tails), in FP32 with a thread per face point (the merged kernel spills
     // under FP32's register cap)
-    c->face_mode = cfg->nbasis == 4 ? 2 : cfg->precision == 64 ? 1 : 0;
+    // face kernels by measurement: FP64 merged directions (TGV 64^3 nb 4: 7.52 ms against 7.57 one
+    // launch per direction and 7.73 with the point loop); FP32 the point loop for nb 4 (ensemble
+    // 37.4 against 37.8 ms, TGV 0.73 against 0.83 ms), one launch per direction otherwise
+    c->face_mode = cfg->precision == 64 ? 1 : cfg->nbasis == 4 ? 2 : 0;
     // k_update: 64 threads per block in FP32 (measured 4 % faster on the 128^2 vortex step), 128 in FP64
     c->update_tpb_default = c->update_tpb = cfg->precision == 32 ? 64 : UPD_TPB;
     c->G.pdl = 0;   // programmatic dependent launch measured neutral here: an autotuned option

@@ -195,9 +195,9 @@ class Solver:
         default where they exist: FP64 nbasis 8/10 without the stochastic
         stress, and ivis 0/1; the fused stage, nbasis 4 ivis 0/1, is off by
         default); pdl None keeps the current choice (off by default); faces_merged None keeps
-        the current choice (1: one launch for three directions, the default for
-        nbasis 8/10 in FP64; 0: one per direction, nbasis 8/10 in FP32; 2: one
-        per direction with a thread per face looping over its points, nbasis 4);
+        the current choice (1: one launch for three directions, the default in
+        FP64; 0: one per direction, nbasis 8/10 in FP32; 2: one per direction
+        with a thread per face looping over its points, nbasis 4 in FP32);
         update_tpb: threads per block of the split update (0: the default,
         64 in FP32, 128 in FP64)."""
         cur = self.get_launch()

@@ -19,7 +19,7 @@ def test_launch_defaults_and_validation():
     from hermeshd_gb300.solver import Solver
     s = Solver(config.sod_1d(nx=64))
     assert s.get_launch() == {"face_tpb": 128, "dt_tpb": 256, "steps_per_graph": 1, "noise_inline": 0,
-                              "face_traces": 0, "split_update": 1, "tile_stage": 0, "pdl": 0, "faces_merged": 2,
+                              "face_traces": 0, "split_update": 1, "tile_stage": 0, "pdl": 0, "faces_merged": 1,
                               "update_tpb": 128}   # 1-D: no fused stage by default
     for bad in ({"face_tpb": 96}, {"face_tpb": 256}, {"dt_tpb": 48}, {"dt_tpb": 512}, {"steps_per_graph": 65},
                 {"update_tpb": 32}, {"update_tpb": 512}):
@@ -27,7 +27,7 @@ def test_launch_defaults_and_validation():
             s.set_launch(**bad)
     s.set_launch(face_tpb=32, dt_tpb=64, steps_per_graph=4, update_tpb=256)
     assert s.get_launch() == {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 4, "noise_inline": 0,
-                              "face_traces": 0, "split_update": 1, "tile_stage": 0, "pdl": 0, "faces_merged": 2,
+                              "face_traces": 0, "split_update": 1, "tile_stage": 0, "pdl": 0, "faces_merged": 1,
                               "update_tpb": 256}
     with pytest.raises(HermesError):   # no trace kernel for nbasis 4
         s.set_launch(face_traces=1)
