@@ -590,15 +590,16 @@ int create_impl(const hermes_config* cfg, int nbox, const int32_t* dims, const d
     long long ncell, nface[3];
     make_boxes(*cfg, nbox, dims, lengths, seeds, c->K.nf, c->h_boxes, c->h_len, ncell, nface, c->q_elems, c->flux_elems);
     c->G.nbox = nbox;
-    // face kernels, as measured: the linear basis (4 points per face) runs
-    // fastest with a thread per face looping over its points; nbasis 8/10 in
-    // FP64 with the three directions in one launch (they fill each other's
-    // tails), in FP32 with a thread per face point (the merged kernel spills
-    // under FP32's register cap)
-    // face kernels by measurement: FP64 merged directions (TGV 64^3 nb 4: 7.52 ms against 7.57 one
-    // launch per direction and 7.73 with the point loop); FP32 the point loop for nb 4 (ensemble
-    // 37.4 against 37.8 ms, TGV 0.73 against 0.83 ms), one launch per direction otherwise
-    c->face_mode = cfg->precision == 64 ? 1 : cfg->nbasis == 4 ? 2 : 0;
+    // face kernels, as measured: FP64 with the three directions in one launch
+    // (they fill each other's tails; TGV 64^3 nb 4: 7.52 ms against 7.57 with
+    // one launch per direction and 7.73 with the point loop); FP32 nb 8/10
+    // with a thread per face point (the merged kernel spills under FP32's
+    // register cap); FP32 nb 4 with a thread per face looping over its points
+    // (ensemble 37.4 against 37.8 ms, TGV 0.73 against 0.83 ms) where the grid
+    // fills the GPU -- on a small grid that loop is latency-bound (FP64 Sod 256:
+    // 0.27 s against 0.13 s with a thread per face point), so below 2^15 cells
+    // a thread per face point
+    c->face_mode = cfg->precision == 64 ? 1 : (cfg->nbasis == 4 && ncell >= (1ll << 15)) ? 2 : 0;
     // k_update: 64 threads per block in FP32 (measured 4 % faster on the 128^2 vortex step), 128 in FP64
     c->update_tpb_default = c->update_tpb = cfg->precision == 32 ? 64 : UPD_TPB;
     c->G.pdl = 0;   // programmatic dependent launch measured neutral here: an autotuned option

@@ -196,8 +196,9 @@ class Solver:
         stress, and ivis 0/1; the fused stage, nbasis 4 ivis 0/1, is off by
         default); pdl None keeps the current choice (off by default); faces_merged None keeps
         the current choice (1: one launch for three directions, the default in
-        FP64; 0: one per direction, nbasis 8/10 in FP32; 2: one per direction
-        with a thread per face looping over its points, nbasis 4 in FP32);
+        FP64; 0: one per direction, nbasis 8/10 in FP32 and nbasis 4 in FP32
+        below 2^15 cells; 2: one per direction with a thread per face looping
+        over its points, nbasis 4 in FP32 from 2^15 cells);
         update_tpb: threads per block of the split update (0: the default,
         64 in FP32, 128 in FP64)."""
         cur = self.get_launch()

@@ -240,8 +240,9 @@ typedef struct hermes_launch {
     int32_t faces_merged;    /* the face kernels: 1 the three directions in one launch (the default
                                 in FP64, where the directions fill each other's tails); 0 one
                                 launch per direction, thread per (face, point) (nbasis 8/10 in
-                                FP32); 2 one launch per direction, thread per face looping over its
-                                points (nbasis 4 in FP32; needs the stochastic stress drawn in
+                                FP32, and nbasis 4 in FP32 below 2^15 cells); 2 one launch per
+                                direction, thread per face looping over its points (nbasis 4 in
+                                FP32 from 2^15 cells; needs the stochastic stress drawn in
                                 place or absent and no trace buffer, else as 0).  Bit-identical. */
     int32_t update_tpb;      /* threads per block of the split update's k_update (one thread per cell
                                 and variable): 64, 128 or 256; 0 the default (64 in FP32, 128 in

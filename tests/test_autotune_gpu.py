@@ -38,6 +38,8 @@ def test_launch_defaults_and_validation():
         s10.set_launch(tile_stage=1)
     s4 = Solver(config.fh_box(8, precision="fp32"))
     assert s4.get_launch()["tile_stage"] == 0   # off by default, available for nbasis 4
+    assert s4.get_launch()["faces_merged"] == 0   # FP32 nb 4 below 2^15 cells: a thread per face point
+    assert Solver(config.fh_box(32, precision="fp32")).get_launch()["faces_merged"] == 2   # the point loop
     assert s4.get_launch()["update_tpb"] == 64   # FP32 default; 0 selects it again
     s4.set_launch(update_tpb=256)
     assert s4.get_launch()["update_tpb"] == 256
