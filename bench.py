@@ -294,7 +294,8 @@ def run_ours(args, rank, ws):
     qbytes = int(np.prod(cfg.shape_c)) * 8
     out["e2e"] = {"value": ws * dof_stage * Ke / e2e_s, "unit": UNIT, "h2d_bytes_per_step": qbytes,
                   "d2h_bytes_per_step": qbytes, "steps": Ke,
-                  "path": "hermes_advance_host (pinned host array -> H2D, one step, D2H, synchronise)"}
+                  "path": "hermes_advance_host (pinned host array -> H2D, one step whose last stage stores the new "
+                          "state into the pinned array over the host link, synchronise)"}
 
     # ---- per-kernel device times (event pairs around every launch) ------
     s.profile(True)

@@ -26,7 +26,7 @@ struct KernelSet {
     void (*mindt_limit_any)(void* Q, const DtArgs& a, cudaStream_t s);
     // face traces into a buffer for the face kernels (FaceArgs.traces); null
     // where the face kernels evaluate the traces themselves
-    void (*trace)(const void* Q, void* tr, const Geom& G, cudaStream_t s);
+    void (*trace)(const void* Q, void* tr, const Geom& G, cudaStream_t s, int v0, int nv);
     // the fused stage (dg_tile.cuh) and the CFL reduction fused with the first
     // stage's limiter; null where they do not exist (nbasis 8 and 10)
     void (*tile)(const void* Qin, const void* Q0, void* out, unsigned ntiles, const TileArgs& a, cudaStream_t s);
@@ -132,11 +132,12 @@ struct Launch {
         b.traces = nullptr;
         face_dirs<NOISE, false>(dir, grid, tpb, q, f, b, s);
     }
-    static void trace(const void* Q, void* tr, const Geom& G, cudaStream_t s) {
+    // the traces of the variables v0 .. v0+nv-1 (all: 0, NQ)
+    static void trace(const void* Q, void* tr, const Geom& G, cudaStream_t s, int v0, int nv) {
         if constexpr (HAS_TRACE) {
-            if (G.ncell <= 0) return;
-            dim3 grid((unsigned)((G.ncell + TRACE_TPB - 1) / TRACE_TPB), 3 * NQ);
-            launch_k(G.pdl, k_trace<T, TB>, grid, TRACE_TPB, 0, s, static_cast<const T*>(Q), static_cast<T*>(tr), G);
+            if (G.ncell <= 0 || nv <= 0) return;
+            dim3 grid((unsigned)((G.ncell + TRACE_TPB - 1) / TRACE_TPB), 3 * nv);
+            launch_k(G.pdl, k_trace<T, TB>, grid, TRACE_TPB, 0, s, static_cast<const T*>(Q), static_cast<T*>(tr), G, v0, nv);
         }
     }
     template <bool NOISE>

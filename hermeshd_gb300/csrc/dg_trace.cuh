@@ -59,10 +59,10 @@ __device__ __forceinline__ void trace_cell(const T* __restrict__ Qb, long long n
     });
 }
 
-// thread per (cell, direction, variable); grid (cells / TRACE_TPB, 3 NQ):
-// blockIdx.y = direction * NQ + variable
+// thread per (cell, direction, variable) for the variables v0 .. v0+nv-1;
+// grid (cells / TRACE_TPB, 3 nv): blockIdx.y = direction * nv + variable - v0
 template <class T, class TB>
-__global__ void __launch_bounds__(TRACE_TPB) k_trace(const T* __restrict__ Q, T* __restrict__ tr, Geom G) {
+__global__ void __launch_bounds__(TRACE_TPB) k_trace(const T* __restrict__ Q, T* __restrict__ tr, Geom G, int v0, int nv) {
     pdl_enter();
     const long long gc = (long long)blockIdx.x * TRACE_TPB + threadIdx.x;
     if (gc >= G.ncell) return;
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(TRACE_TPB) k_trace(const T* __restrict__ Q, T*
     const Box& B = G.boxes[bx];
     const T* Qb = Q + B.q0;
     const long long le = gc - B.cell0;
-    const int d = blockIdx.y / NQ, v = blockIdx.y % NQ;
+    const int d = blockIdx.y / nv, v = v0 + blockIdx.y % nv;
     if (d == 0) trace_cell<T, TB, 0>(Qb, B.ncell, le, v, tr, G.ncell, gc);
     else if (d == 1) trace_cell<T, TB, 1>(Qb, B.ncell, le, v, tr, G.ncell, gc);
     else trace_cell<T, TB, 2>(Qb, B.ncell, le, v, tr, G.ncell, gc);

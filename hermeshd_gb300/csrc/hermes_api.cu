@@ -133,6 +133,10 @@ struct hermes_ctx {
     cudaStream_t stream = nullptr;       // private stream (graph capture needs a non-legacy stream)
     cudaStream_t user_stream = nullptr;  // the caller's stream; work is ordered against it both ways
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    // hermes_advance_host's copy in: a second stream, the hydro rows first
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy_start = nullptr, ev_copy_hydro = nullptr, ev_copy_stress = nullptr;
+    cudaEvent_t pending_stress = nullptr;   // the stress rows of the stage input still arriving
     std::vector<Box> h_boxes;
     std::vector<double> h_len;           // lx, ly, lz per box
     Box* d_boxes = nullptr;
@@ -359,9 +363,22 @@ void enq_limit(hermes_ctx* c, void* q) {
 void enq_faces(hermes_ctx* c, const void* q, unsigned stage) {
     FaceArgs a{c->G, c->ph, c->d_step, stage, c->face_tpb, c->noise_staged ? c->d_noise_face : nullptr,
                c->face_traces ? c->d_traces : nullptr, c->face_mode == 2 ? 1 : 0};
-    if (c->face_traces) {
+    if (c->pending_stress) {
+        // the copy in is still delivering the stress rows: trace the hydro
+        // rows (already here) first, then wait for the rest
+        if (c->face_traces) {
+            ProfScope ps(c, 7);
+            c->K.trace(q, c->d_traces, c->G, c->stream, 0, EN + 1);
+        }
+        cudaStreamWaitEvent(c->stream, c->pending_stress, 0);
+        c->pending_stress = nullptr;
+        if (c->face_traces) {
+            ProfScope ps(c, 7);
+            c->K.trace(q, c->d_traces, c->G, c->stream, EN + 1, NQ - (EN + 1));
+        }
+    } else if (c->face_traces) {
         ProfScope ps(c, 7);
-        c->K.trace(q, c->d_traces, c->G, c->stream);
+        c->K.trace(q, c->d_traces, c->G, c->stream, 0, NQ);
     }
     if (c->face_mode == 1) {
         ProfScope ps(c, 2);
@@ -452,11 +469,14 @@ void enq_step_tile(hermes_ctx* c, void* q, void* q1) {
     }
 }
 
-void enq_step(hermes_ctx* c, void* q, void* q1) {
+// out_last: where the last stage writes the new state (default q; a mapped
+// pinned host array for hermes_advance_host, which then needs no copy back)
+void enq_step(hermes_ctx* c, void* q, void* q1, void* out_last = nullptr) {
     if (c->tile_stage) {
         enq_step_tile(c, q, q1);
         return;
     }
+    void* qo = out_last ? out_last : q;
     NvtxRange r("hermes step");
     const bool fl = fused_limiter(c);
     if (fl) {
@@ -472,9 +492,9 @@ void enq_step(hermes_ctx* c, void* q, void* q1) {
     enq_stage(c, q, nullptr, q1, COMB_NONE, 0, !fl, fl);        // Q_1 = E(Q)
     if (c->cfg.iorder == 3) {
         enq_stage(c, q1, q, q1, COMB_34, 1, !fl, fl);           // Q_1 = 3/4 Q + 1/4 E(Q_1)
-        enq_stage(c, q1, q, q, COMB_13, 2, !fl, 0);             // Q = 1/3 Q + 2/3 E(Q_1)
+        enq_stage(c, q1, q, qo, COMB_13, 2, !fl, 0);            // Q = 1/3 Q + 2/3 E(Q_1)
     } else {
-        enq_stage(c, q1, q, q, COMB_HALF, 1, !fl, 0);           // Q = (Q + E(Q_1))/2
+        enq_stage(c, q1, q, qo, COMB_HALF, 1, !fl, 0);          // Q = (Q + E(Q_1))/2
     }
 }
 
@@ -779,6 +799,10 @@ int hermes_destroy(hermes_ctx* c) {
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->ev_in) cudaEventDestroy(c->ev_in);
     if (c->ev_out) cudaEventDestroy(c->ev_out);
+    if (c->ev_copy_start) cudaEventDestroy(c->ev_copy_start);
+    if (c->ev_copy_hydro) cudaEventDestroy(c->ev_copy_hydro);
+    if (c->ev_copy_stress) cudaEventDestroy(c->ev_copy_stress);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     cudaFree(c->d_tadj);
     cudaFree(c->d_mu);
     cudaFree(c->d_part);
@@ -1099,13 +1123,75 @@ int hermes_advance_host(hermes_ctx* c, void* q_host, int nsteps, double* t, doub
             cudaGetLastError();
             return leave(c, fail(c, HERMES_ERR_ALLOC, "device buffers for host-array stepping"));
         }
+    // pinned host memory mapped into the device's address space: the last
+    // stage of the last step stores the new state into it directly, so the
+    // copy back overlaps that kernel's arithmetic instead of following it
+    void* q_mapped = nullptr;
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, q_host) == cudaSuccess) {
+        if (pa.type == cudaMemoryTypeHost && pa.devicePointer) q_mapped = pa.devicePointer;
+    } else {
+        cudaGetLastError();
+    }
+    const bool direct = q_mapped && nsteps >= 1 && !c->tile_stage;
+    // one grid in pinned memory: the copy in goes on a second stream, the
+    // hydro rows (rh..en of every coefficient) first; the first step's CFL
+    // reduction, limiter and hydro traces read only those and start while
+    // the stress rows are still arriving (the face kernels wait for them)
+    const bool split = direct && c->G.nbox == 1;
+    if (split && !c->copy_stream) {
+        cudaError_t e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_copy_start, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_copy_hydro, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_copy_stress, cudaEventDisableTiming);
+        if (e != cudaSuccess) return leave(c, cuda_fail(c, "copy stream", e));
+    }
     // copy in, step, copy the state and the time record out, one synchronisation
-    HCK(c, cudaMemcpyAsync(c->d_q[0], q_host, bytes, cudaMemcpyHostToDevice, c->stream));
+    if (split) {
+        const size_t es = (size_t)c->K.elem_size, nc = (size_t)c->G.ncell, pitch = (size_t)NQ * nc * es;
+        const size_t hydro = (size_t)(EN + 1) * nc * es;
+        char* dq = static_cast<char*>(c->d_q[0]);
+        const char* hq = static_cast<const char*>(q_host);
+        HCK(c, cudaEventRecord(c->ev_copy_start, c->stream));
+        HCK(c, cudaStreamWaitEvent(c->copy_stream, c->ev_copy_start, 0));
+        HCK(c, cudaMemcpy2DAsync(dq, pitch, hq, pitch, hydro, (size_t)c->cfg.nbasis, cudaMemcpyHostToDevice,
+                                 c->copy_stream));
+        HCK(c, cudaEventRecord(c->ev_copy_hydro, c->copy_stream));
+        HCK(c, cudaMemcpy2DAsync(dq + hydro, pitch, hq + hydro, pitch, pitch - hydro, (size_t)c->cfg.nbasis,
+                                 cudaMemcpyHostToDevice, c->copy_stream));
+        HCK(c, cudaEventRecord(c->ev_copy_stress, c->copy_stream));
+        HCK(c, cudaStreamWaitEvent(c->stream, c->ev_copy_hydro, 0));
+        c->pending_stress = c->ev_copy_stress;
+    } else {
+        HCK(c, cudaMemcpyAsync(c->d_q[0], q_host, bytes, cudaMemcpyHostToDevice, c->stream));
+    }
     if (t && c->G.nbox == 1) k_set_t<<<1, 32, 0, c->stream>>>(c->d_st, 1, *t);
     rc = launch_status(c);
-    if (rc == HERMES_OK) rc = enqueue_steps_impl(c, c->d_q[0], c->d_q[1], nsteps);
+    if (rc == HERMES_OK && direct) {
+        // the first step eagerly (it consumes the pending stress rows), the
+        // middle ones from the graphs, the last into the host array
+        if (nsteps > 1) {
+            enq_step(c, c->d_q[0], c->d_q[1]);
+            if (c->pending_stress) {
+                cudaStreamWaitEvent(c->stream, c->pending_stress, 0);
+                c->pending_stress = nullptr;
+            }
+            rc = launch_status(c);
+            if (rc == HERMES_OK && nsteps > 2) rc = enqueue_steps_impl(c, c->d_q[0], c->d_q[1], nsteps - 2);
+        }
+        if (rc == HERMES_OK) {
+            enq_step(c, c->d_q[0], c->d_q[1], q_mapped);
+            rc = launch_status(c);
+        }
+    } else if (rc == HERMES_OK) {
+        rc = enqueue_steps_impl(c, c->d_q[0], c->d_q[1], nsteps);
+    }
+    if (c->pending_stress) {   // (not consumed: wait here)
+        cudaStreamWaitEvent(c->stream, c->pending_stress, 0);
+        c->pending_stress = nullptr;
+    }
     if (rc) return leave(c, rc);
-    HCK(c, cudaMemcpyAsync(q_host, c->d_q[0], bytes, cudaMemcpyDeviceToHost, c->stream));
+    if (!direct) HCK(c, cudaMemcpyAsync(q_host, c->d_q[0], bytes, cudaMemcpyDeviceToHost, c->stream));
     rc = enq_record(c);
     if (rc) return leave(c, rc);
     HCK(c, cudaStreamSynchronize(c->stream));

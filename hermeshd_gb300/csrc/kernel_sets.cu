@@ -15,7 +15,7 @@ void face_f64_nb8(int, const void*, void*, const FaceArgs&, cudaStream_t);
 void facen_f64_nb8(int, const void*, void*, const FaceArgs&, cudaStream_t);
 void limit_f64_nb8(void*, const Geom&, const Phys&, cudaStream_t);
 void mindt_f64_nb8(const void*, const DtArgs&, cudaStream_t);
-void trace_f64_nb8(const void*, void*, const Geom&, cudaStream_t);
+void trace_f64_nb8(const void*, void*, const Geom&, cudaStream_t, int, int);
 void cell_f64_nb8(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
 void celln_f64_nb8(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
 cudaError_t prep_f64_nb8();
@@ -24,7 +24,7 @@ void face_f64_nb10(int, const void*, void*, const FaceArgs&, cudaStream_t);
 void facen_f64_nb10(int, const void*, void*, const FaceArgs&, cudaStream_t);
 void limit_f64_nb10(void*, const Geom&, const Phys&, cudaStream_t);
 void mindt_f64_nb10(const void*, const DtArgs&, cudaStream_t);
-void trace_f64_nb10(const void*, void*, const Geom&, cudaStream_t);
+void trace_f64_nb10(const void*, void*, const Geom&, cudaStream_t, int, int);
 void cell_f64_nb10(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
 void celln_f64_nb10(const void*, const void*, void*, const void*, const CellArgs&, cudaStream_t);
 cudaError_t prep_f64_nb10();

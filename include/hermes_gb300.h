@@ -150,7 +150,11 @@ int hermes_advance(hermes_ctx *ctx, void *q, void *q1, void *q2, int nsteps, dou
 
 /* The same with host buffers: q_host (nsteps of step() on a device copy,
  * then copied back, with one synchronisation; a state with a NaN cell
- * average is copied back as well and HERMES_ERR_NONFINITE returned).  The
+ * average is copied back as well and HERMES_ERR_NONFINITE returned).  When
+ * q_host is pinned memory mapped into the device's address space
+ * (cudaHostAlloc, cudaHostRegister with cudaHostRegisterMapped), the last
+ * stage stores the new state into it directly, the copy back overlapping
+ * that kernel; other host memory is copied back after the steps.  The
  * reference's interface takes host arrays. */
 int hermes_advance_host(hermes_ctx *ctx, void *q_host, int nsteps, double *t, double *dt);
 

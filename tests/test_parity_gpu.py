@@ -176,16 +176,33 @@ def test_step_equals_graph_advance():
     assert np.array_equal(s.to_numpy(qa), s.to_numpy(qb))
 
 
-def test_host_buffers_equal_device():
-    cfg = config.sod_1d(nx=64)
-    Q = ic.sod(cfg)
+@pytest.mark.parametrize("case", ["sod_rk2", "vortex_nb10_rk3", "fh_fp32_noise"])
+def test_host_buffers_equal_device(case):
+    """Host-array stepping equals the device path bit for bit: pageable host
+    memory (copied back after the steps) and pinned memory (the last stage
+    stores into it directly)."""
+    import torch
+    cfg = {"sod_rk2": lambda: config.sod_1d(nx=64),
+           "vortex_nb10_rk3": lambda: config.isentropic_vortex_2d(n=12),
+           "fh_fp32_noise": lambda: config.fh_box(6, precision="fp32", seed=4)}[case]()
+    Q = {"sod_rk2": ic.sod, "vortex_nb10_rk3": ic.isentropic_vortex, "fh_fp32_noise": ic.equilibrium}[case](cfg)
     s = _solver(cfg)
     q, q1 = s.from_numpy(Q), s.new_state()
     t_d, _ = s.advance(q, q1, 12)
-    qh = np.ascontiguousarray(Q.T)          # (nb, nQ, nz, ny, nx) C order = the Fortran memory
-    t_h, _ = s.advance_host(qh, 12)
-    assert t_h == t_d
-    assert np.array_equal(qh, s.to_numpy(q).T)
+    ref = s.to_numpy(q).T
+    for pinned in (False, True):
+        s2 = _solver(cfg)
+        qh0 = np.ascontiguousarray(Q.T).astype(s2.np_dtype)   # (nb, nQ, nz, ny, nx) C order = the Fortran memory
+        if pinned:
+            buf = torch.empty(qh0.shape, dtype=torch.from_numpy(qh0).dtype, pin_memory=True)
+            qh = buf.numpy()
+            qh[...] = qh0
+        else:
+            qh = qh0
+        t_h, _ = s2.advance_host(qh, 5)
+        t_h, _ = s2.advance_host(qh, 7, t=t_h)
+        assert t_h == t_d, (pinned, t_h, t_d)
+        assert np.array_equal(qh, ref), pinned
 
 
 def test_fp32_path_against_fp64_oracle():
