@@ -638,3 +638,21 @@ def test_noise_rollout_gradient_vs_fd():
     fc, err = _fd_coll(lambda c: Rollout(cfg).forward(q0, c, 4)[0], cfg.coll, W)
     assert err <= 1e-5 * abs(fc)
     assert abs(float(ca.grad) - fc) <= TOL * abs(float(ca.grad)) + err, (float(ca.grad), fc, err)
+
+
+def test_argument_checks_of_the_new_entry_points():
+    """hermes_set_noise_stage takes 0..2; hermes_limiter_vjp rejects lam_in
+    aliasing q; both leave the context usable."""
+    from hermeshd_gb300._lib import HermesError
+    from hermeshd_gb300.solver import Solver
+    cfg = _fh_cfg()
+    S = Solver(cfg)
+    for bad in (-1, 3):
+        with pytest.raises(HermesError):
+            S.set_noise_stage(bad)
+    S.set_noise_stage(2)
+    q = S.from_numpy(generic_state(cfg, seed=1, stress_amp=0.0))
+    with pytest.raises(HermesError):
+        S.limiter_vjp(q, q.clone(), out=q)
+    W = _direction(q, 5)
+    assert _torch().equal(S.limiter_vjp(q, W), W)   # no floor within reach: the identity
