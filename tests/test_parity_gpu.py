@@ -205,6 +205,35 @@ def test_host_buffers_equal_device(case):
         assert np.array_equal(qh, ref), pinned
 
 
+def test_ensemble_host_buffers_equal_device():
+    """An ensemble stepped on a pinned host array (the last stage stores into
+    it directly) equals the device path bit for bit."""
+    import torch
+    from hermeshd_gb300.solver import Ensemble
+    base = config.fh_box(6, precision="fp32", seed=0)
+    dims = [(6, 6, 6), (4, 5, 3)]
+    lengths = [(d[0] * 10.0, d[1] * 10.0, d[2] * 10.0) for d in dims]
+
+    def make():
+        e = Ensemble(base, dims, lengths, [5, 6])
+        q = e.new_state()
+        for i in range(len(dims)):
+            v = e.box_view(q, i)
+            v.zero_()
+            v[0, 0].fill_(1.0)
+            v[0, 4].fill_(1.0 / (base.aindex - 1.0))
+        return e, q
+
+    e1, q = make()
+    e1.advance(q, e1.new_state(), 9)
+    e2, q0 = make()
+    buf = torch.empty(q0.shape, dtype=q0.dtype, pin_memory=True)
+    buf.copy_(q0)
+    e2.advance_host(buf.numpy(), 4)
+    e2.advance_host(buf.numpy(), 5)
+    assert torch.equal(buf, q.cpu())
+
+
 def test_fp32_path_against_fp64_oracle():
     cfg = config.isentropic_vortex_2d(n=16, precision="fp32")
     Q = ic.isentropic_vortex(cfg)
