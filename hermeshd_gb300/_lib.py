@@ -13,7 +13,7 @@ from .config import Config
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libhermes_gb300.so")
 
 HERMES_OK = 0
-ABI_VERSION = 7          # HERMES_ABI_VERSION of include/hermes_gb300.h
+ABI_VERSION = 8          # HERMES_ABI_VERSION of include/hermes_gb300.h
 STATUS = {0: "HERMES_OK", 1: "HERMES_ERR_CONFIG", 2: "HERMES_ERR_SHAPE", 3: "HERMES_ERR_DTYPE",
           4: "HERMES_ERR_NONFINITE", 5: "HERMES_ERR_TIMEOUT", 6: "HERMES_ERR_CUDA", 7: "HERMES_ERR_ALLOC",
           8: "HERMES_ERR_ARG"}
@@ -34,7 +34,7 @@ class HermesLaunch(C.Structure):
     _fields_ = [("face_tpb", C.c_int32), ("dt_tpb", C.c_int32), ("steps_per_graph", C.c_int32),
                 ("noise_inline", C.c_int32), ("face_traces", C.c_int32), ("split_update", C.c_int32),
                 ("tile_stage", C.c_int32), ("pdl", C.c_int32),
-                ("faces_merged", C.c_int32), ("update_tpb", C.c_int32)]
+                ("faces_merged", C.c_int32), ("update_tpb", C.c_int32), ("cell_concurrent", C.c_int32)]
 
 
 class HermesOutputUnits(C.Structure):

@@ -30,7 +30,9 @@ include/hermes_gb300.h):
                        has it (nbasis 4, ivis 0/1).  With it on, only
                        steps_per_graph still applies;
 * ``update_tpb``       threads per block of the split update (64/128/256),
-                       tuned where the split update is on.
+                       tuned where the split update is on;
+* ``cell_concurrent``  the split update's volume kernel on a second stream
+                       beside the trace and face kernels (1) or after them (0).
 
 The cell kernel keeps 32 cells per block: its hydro and stress thread groups
 must each fill whole warps (with 16 cells both groups would share one warp and
@@ -62,6 +64,7 @@ KNOBS = {
     "faces_merged": (1, 0),          # the context's default is tried first
     "tile_stage": (0, 1),            # tuned only where the context has the fused stage
     "update_tpb": (128, 64, 256),    # tuned only with the split update
+    "cell_concurrent": (0, 1),       # tuned only with the split update (the context's default first)
 }
 
 
@@ -157,6 +160,9 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
             knobs.pop(k, None)
     if cur["split_update"] == 0:
         knobs.pop("update_tpb", None)
+        knobs.pop("cell_concurrent", None)
+    elif "cell_concurrent" in knobs:
+        knobs["cell_concurrent"] = (cur["cell_concurrent"], 1 - cur["cell_concurrent"])
     elif "update_tpb" in knobs:
         knobs["update_tpb"] = (cur["update_tpb"],) + tuple(u for u in (64, 128, 256) if u != cur["update_tpb"])
     if cur["tile_stage"] == 0 and not _can_tile(solver, cur):

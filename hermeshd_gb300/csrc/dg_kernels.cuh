@@ -638,6 +638,7 @@ struct CellArgs {
     void* accbuf;       // split update: k_cell stores the volume terms here, k_update finishes
     int limit_out;      // k_update (FP64): apply the next stage's positivity limiter to the output
     int utpb = 0;       // threads per block of k_update (0: UPD_TPB)
+    int phase = 0;      // split update: 0 both kernels, 1 the volume kernel only, 2 the update only
 };
 
 // RK combination of integrator.f90:62-86

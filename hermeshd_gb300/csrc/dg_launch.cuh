@@ -150,7 +150,8 @@ struct Launch {
         const T* f = static_cast<const T*>(flux);
         if constexpr (has_split<NOISE>()) {
             if (a.accbuf && a.ph.ivis < 2 && !a.split_source) {
-                launch_k(a.G.pdl, k_cell<T, TB, NOISE, true>, nb, 2 * CELL_CPB, cell_smem(), s, qi, q0, o, f, a);
+                if (a.phase != 2) launch_k(a.G.pdl, k_cell<T, TB, NOISE, true>, nb, 2 * CELL_CPB, cell_smem(), s, qi, q0, o, f, a);
+                if (a.phase == 1) return;
                 if constexpr (std::is_same<T, double>::value) {
                     if (a.limit_out && a.mode == MODE_STAGE) {
                         const unsigned ub = (unsigned)((a.G.ncell + UPD_CPB - 1) / UPD_CPB);

@@ -185,11 +185,11 @@ class Solver:
         return {"face_tpb": l.face_tpb, "dt_tpb": l.dt_tpb, "steps_per_graph": l.steps_per_graph,
                 "noise_inline": l.noise_inline, "face_traces": l.face_traces, "split_update": l.split_update,
                 "tile_stage": l.tile_stage, "pdl": l.pdl,
-                "faces_merged": l.faces_merged, "update_tpb": l.update_tpb}
+                "faces_merged": l.faces_merged, "update_tpb": l.update_tpb, "cell_concurrent": l.cell_concurrent}
 
     def set_launch(self, face_tpb: int = 0, dt_tpb: int = 0, steps_per_graph: int = 1, noise_inline: int = 0,
                    face_traces=None, split_update=None, tile_stage=None, pdl=None,
-                   faces_merged=None, update_tpb: int = 0):
+                   faces_merged=None, update_tpb: int = 0, cell_concurrent=None):
         """face_traces / split_update / tile_stage None keep the context's
         current choice (the trace kernel and the split update are on by
         default where they exist: FP64 nbasis 8/10 without the stochastic
@@ -200,7 +200,9 @@ class Solver:
         below 2^15 cells; 2: one per direction with a thread per face looping
         over its points, nbasis 4 in FP32 from 2^15 cells);
         update_tpb: threads per block of the split update (0: the default,
-        64 in FP32, 128 in FP64)."""
+        64 in FP32, 128 in FP64); cell_concurrent None keeps the current choice
+        (1, the default: the split update's volume kernel on a second stream
+        beside the trace and face kernels; 0: one stream)."""
         cur = self.get_launch()
         if face_traces is None:
             face_traces = cur["face_traces"]
@@ -212,8 +214,11 @@ class Solver:
             pdl = cur["pdl"]
         if faces_merged is None:
             faces_merged = cur["faces_merged"]
+        if cell_concurrent is None:
+            cell_concurrent = cur["cell_concurrent"]
         l = _lib.HermesLaunch(int(face_tpb), int(dt_tpb), int(steps_per_graph), int(noise_inline), int(face_traces),
-                              int(split_update), int(tile_stage), int(pdl), int(faces_merged), int(update_tpb))
+                              int(split_update), int(tile_stage), int(pdl), int(faces_merged), int(update_tpb),
+                              int(cell_concurrent))
         check(lib().hermes_set_launch(self.ctx, C.byref(l)), self.ctx)
 
     def set_noise_step(self, step: int):

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define HERMES_ABI_VERSION 7
+#define HERMES_ABI_VERSION 8
 
 typedef enum hermes_status {
     HERMES_OK = 0,
@@ -211,7 +211,9 @@ int hermes_derived(hermes_ctx *ctx, const void *q, float *out, int32_t nvtk, uin
 
 /* Launch shape of a context, chosen by the autotuner (hermeshd_gb300/autotune.py)
  * or by hand.  No counterpart in the reference (its loops have no launch
- * shape).  Zero fields select the compiled defaults.  Changing face_tpb or
+ * shape).  Zero sizes (face_tpb, dt_tpb, steps_per_graph, update_tpb) select the
+ * compiled defaults; the switches take the values given (start from
+ * hermes_get_launch to change one).  Changing face_tpb or
  * dt_tpb synchronises the context's stream and drops its captured graphs. */
 typedef struct hermes_launch {
     int32_t face_tpb;        /* faces per block of the face kernels: 32, 64 or 128 (default 128) */
@@ -251,6 +253,10 @@ typedef struct hermes_launch {
     int32_t update_tpb;      /* threads per block of the split update's k_update (one thread per cell
                                 and variable): 64, 128 or 256; 0 the default (64 in FP32, 128 in
                                 FP64).  Bit-identical. */
+    int32_t cell_concurrent; /* 1 (default): with the split update, each stage's volume kernel runs on
+                                a second stream beside the trace and face kernels (it needs neither),
+                                and the update joins them, so the face kernels' small blocks fill the
+                                volume kernel's tail; 0: one stream.  Bit-identical. */
 } hermes_launch;
 int hermes_set_launch(hermes_ctx *ctx, const hermes_launch *launch);
 int hermes_get_launch(hermes_ctx *ctx, hermes_launch *launch);

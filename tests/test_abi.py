@@ -51,7 +51,7 @@ def test_library_exports_every_symbol(hermes_lib):
 
 
 def test_abi_version_and_config_layout(hermes_lib):
-    assert hermes_lib.hermes_abi_version() == _lib.ABI_VERSION == 7
+    assert hermes_lib.hermes_abi_version() == _lib.ABI_VERSION == 8
     assert hermes_lib.hermes_config_size() == C.sizeof(_lib.HermesConfig)
 
 

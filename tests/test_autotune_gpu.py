@@ -20,7 +20,7 @@ def test_launch_defaults_and_validation():
     s = Solver(config.sod_1d(nx=64))
     assert s.get_launch() == {"face_tpb": 128, "dt_tpb": 256, "steps_per_graph": 1, "noise_inline": 0,
                               "face_traces": 0, "split_update": 1, "tile_stage": 0, "pdl": 0, "faces_merged": 1,
-                              "update_tpb": 128}   # 1-D: no fused stage by default
+                              "update_tpb": 128, "cell_concurrent": 1}   # 1-D: no fused stage by default
     for bad in ({"face_tpb": 96}, {"face_tpb": 256}, {"dt_tpb": 48}, {"dt_tpb": 512}, {"steps_per_graph": 65},
                 {"update_tpb": 32}, {"update_tpb": 512}):
         with pytest.raises(HermesError):
@@ -28,7 +28,7 @@ def test_launch_defaults_and_validation():
     s.set_launch(face_tpb=32, dt_tpb=64, steps_per_graph=4, update_tpb=256)
     assert s.get_launch() == {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 4, "noise_inline": 0,
                               "face_traces": 0, "split_update": 1, "tile_stage": 0, "pdl": 0, "faces_merged": 1,
-                              "update_tpb": 256}
+                              "update_tpb": 256, "cell_concurrent": 1}
     with pytest.raises(HermesError):   # no trace kernel for nbasis 4
         s.set_launch(face_traces=1)
     s.set_launch(tile_stage=1)          # the fused stage exists for nbasis 4 and may be forced on
@@ -59,7 +59,8 @@ def test_every_launch_shape_is_bit_identical(mk):
     shapes = [{}, {"face_tpb": 32, "dt_tpb": 64, "steps_per_graph": 3},
               {"face_tpb": 64, "dt_tpb": 128, "steps_per_graph": 2, "pdl": 1},
               {"faces_merged": 0}, {"faces_merged": 1}, {"faces_merged": 2},
-              {"faces_merged": 2, "noise_inline": 1}, {"update_tpb": 64}, {"update_tpb": 256}]
+              {"faces_merged": 2, "noise_inline": 1}, {"update_tpb": 64}, {"update_tpb": 256},
+              {"cell_concurrent": 0}, {"cell_concurrent": 0, "steps_per_graph": 3, "faces_merged": 0}]
     if cfg.ivis < 2 and (cfg.precision == "fp32" or not cfg.llns):   # the cell update in one kernel
         shapes.append({"split_update": 0})
     if cfg.llns:   # the stochastic stress drawn inside the face and cell kernels instead of staged
@@ -118,7 +119,8 @@ def test_autotune_resets_state_and_caches(tmp_path, monkeypatch):
     r = autotune.autotune(ens, q, steps=2, repeats=2)
     assert not r["cached"] and r["ms_per_step"] <= r["default_ms_per_step"]
     assert set(r["launch"]) == {"face_tpb", "dt_tpb", "steps_per_graph", "noise_inline", "face_traces",
-                                "split_update", "tile_stage", "pdl", "faces_merged", "update_tpb"}
+                                "split_update", "tile_stage", "pdl", "faces_merged", "update_tpb",
+                                "cell_concurrent"}
     assert ens.get_launch() == r["launch"]
     # tuning stepped copies of q; the context's time and noise counter are reset
     qa, qa1 = q.clone(), ens.new_state()

@@ -190,8 +190,9 @@ def test_host_buffers_equal_device(case):
     q, q1 = s.from_numpy(Q), s.new_state()
     t_d, _ = s.advance(q, q1, 12)
     ref = s.to_numpy(q).T
-    for pinned in (False, True):
+    for pinned, conc in ((False, 0), (True, 0), (True, 1)):
         s2 = _solver(cfg)
+        s2.set_launch(cell_concurrent=conc)
         qh0 = np.ascontiguousarray(Q.T).astype(s2.np_dtype)   # (nb, nQ, nz, ny, nx) C order = the Fortran memory
         if pinned:
             buf = torch.empty(qh0.shape, dtype=torch.from_numpy(qh0).dtype, pin_memory=True)
@@ -201,8 +202,8 @@ def test_host_buffers_equal_device(case):
             qh = qh0
         t_h, _ = s2.advance_host(qh, 5)
         t_h, _ = s2.advance_host(qh, 7, t=t_h)
-        assert t_h == t_d, (pinned, t_h, t_d)
-        assert np.array_equal(qh, ref), pinned
+        assert t_h == t_d, (pinned, conc, t_h, t_d)
+        assert np.array_equal(qh, ref), (pinned, conc)
 
 
 def test_ensemble_host_buffers_equal_device():
