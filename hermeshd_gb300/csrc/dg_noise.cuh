@@ -66,13 +66,16 @@ __global__ void __launch_bounds__(NOISE_TPB) k_noise_face(T* __restrict__ out, N
     for (int c = 0; c < 6; ++c) base[((long long)(side * 6 + c) * TB::NF + P) * nfa + gf] = S[c];
 }
 
+// the interior draws into cellbuf and the face draws into facebuf (a null
+// buffer skips its kernels)
 template <class T, int NB, int NQD>
 cudaError_t noise_launch(void* cellbuf, void* facebuf, const NoiseArgs& a, cudaStream_t s) {
     using TB = hermes_tab::Tab<NB, NQD>;
     auto blocks = [](long long n) { return (unsigned)((n + NOISE_TPB - 1) / NOISE_TPB); };
-    if (a.G.ncell > 0)
+    if (cellbuf && a.G.ncell > 0)
         launch_k(a.G.pdl, k_noise_cell<T, TB>, dim3(blocks(a.G.ncell), 3 * TB::NPG), NOISE_TPB, 0, s,
                  static_cast<T*>(cellbuf), a);
+    if (!facebuf) return cudaGetLastError();
     if (a.G.nface[0] > 0)
         launch_k(a.G.pdl, k_noise_face<T, TB, 0>, dim3(blocks(a.G.nface[0]), 2 * TB::NF), NOISE_TPB, 0, s,
                  static_cast<T*>(facebuf), a);

@@ -414,11 +414,13 @@ bool cell_forks(const hermes_ctx* c, int mode) {
     return c->cell_concurrent && c->split_update && c->side_stream && !c->profiling && c->cfg.ivis < 2 &&
            !(mode == MODE_STAGE && c->cfg.ivis == 3 && c->cfg.iorder == 2);
 }
-void enq_noise(hermes_ctx* c, unsigned stage) {
+// the staged stochastic stress of a stage: interior (cell) and face draws, or
+// one of them (the other's buffer null), on the given stream (null: the context's)
+void enq_noise(hermes_ctx* c, unsigned stage, bool cells = true, bool faces = true, cudaStream_t stream = nullptr) {
     if (!c->noise_staged) return;
     NoiseArgs a{c->G, c->ph, c->d_step, stage};
     ProfScope ps(c, 6);
-    c->noise_fn(c->d_noise_cell, c->d_noise_face, a, c->stream);
+    c->noise_fn(cells ? c->d_noise_cell : nullptr, faces ? c->d_noise_face : nullptr, a, stream ? stream : c->stream);
 }
 // the fused stage: out = comb(q0, E(qin)), with the next stage's limiter
 // applied to out when limit_out (qin must not alias out)
@@ -442,18 +444,22 @@ void enq_stage(hermes_ctx* c, void* qin, const void* q0, void* out, int comb, un
         enq_tile(c, qin, q0, out, MODE_STAGE, comb, stage, 0);
         return;
     }
-    enq_noise(c, stage);
     if (cell_forks(c, MODE_STAGE)) {
+        // the interior draws and the volume kernel on the side stream, the
+        // face draws, traces and face kernels on the context's stream
         cudaEventRecord(c->ev_fork, c->stream);
         cudaStreamWaitEvent(c->side_stream, c->ev_fork, 0);
         if (c->pending_stress) cudaStreamWaitEvent(c->side_stream, c->pending_stress, 0);
+        enq_noise(c, stage, true, false, c->side_stream);
         enq_cell(c, qin, q0, out, MODE_STAGE, comb, stage, limit_out, 1, c->side_stream);
         cudaEventRecord(c->ev_join, c->side_stream);
+        enq_noise(c, stage, false, true);
         enq_faces(c, qin, stage);
         cudaStreamWaitEvent(c->stream, c->ev_join, 0);
         enq_cell(c, qin, q0, out, MODE_STAGE, comb, stage, limit_out, 2);
         return;
     }
+    enq_noise(c, stage);
     enq_faces(c, qin, stage);
     enq_cell(c, qin, q0, out, MODE_STAGE, comb, stage, limit_out);
 }
