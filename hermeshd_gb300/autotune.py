@@ -161,10 +161,11 @@ def autotune(solver, q, steps: int = 4, repeats: int = 3, use_cache: bool = True
     if cur["split_update"] == 0:
         knobs.pop("update_tpb", None)
         knobs.pop("cell_concurrent", None)
-    elif "cell_concurrent" in knobs:
-        knobs["cell_concurrent"] = (cur["cell_concurrent"], 1 - cur["cell_concurrent"])
-    elif "update_tpb" in knobs:
-        knobs["update_tpb"] = (cur["update_tpb"],) + tuple(u for u in (64, 128, 256) if u != cur["update_tpb"])
+    else:   # the context's current choices first
+        if "cell_concurrent" in knobs:
+            knobs["cell_concurrent"] = (cur["cell_concurrent"], 1 - cur["cell_concurrent"])
+        if "update_tpb" in knobs:
+            knobs["update_tpb"] = (cur["update_tpb"],) + tuple(u for u in (64, 128, 256) if u != cur["update_tpb"])
     if cur["tile_stage"] == 0 and not _can_tile(solver, cur):
         knobs.pop("tile_stage", None)
     if "faces_merged" in knobs:
