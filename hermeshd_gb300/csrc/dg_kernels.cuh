@@ -223,8 +223,8 @@ template <class TB, class U, class QA>
 __device__ __forceinline__ bool limit_cell(const Phys& ph, QA& q) {
     // returns true if q was modified
     constexpr int NB = TB::NB;
-    const U rh_floor = U(ph.rh_floor), epsi = U(ph.rh_floor), epsiP = U(ph.rh_floor) * U(ph.T_floor);
-    const U aindm1 = U(ph.aindm1);
+    const U rh_floor = PHC(U, ph, rh_floor), epsi = PHC(U, ph, rh_floor), epsiP = PHC(U, ph, rh_floor) * PHC(U, ph, T_floor);
+    const U aindm1 = PHC(U, ph, aindm1);
     if (q[RH][0] < rh_floor) {
         sfor<NB - 1>([&](auto bb) {
             constexpr int b = decltype(bb)::value + 1;
@@ -312,13 +312,13 @@ __device__ __forceinline__ bool limit_bound_clear(const Phys& ph, const QA& q) {
         B[v] = s;
     });
     const U tol = U(std::is_same<U, double>::value ? 1e-10 : 1e-4);
-    const U epsi = U(ph.rh_floor), epsiP = U(ph.rh_floor) * U(ph.T_floor);
+    const U epsi = PHC(U, ph, rh_floor), epsiP = PHC(U, ph, rh_floor) * PHC(U, ph, T_floor);
     U rlo = q[RH][0] - B[RH];
     if (!(rlo >= epsi + tol * (q[RH][0] + B[RH]))) return false;
     U Elo = q[EN][0] - B[EN];
     U m0 = fabs(q[MX][0]) + B[MX], m1 = fabs(q[MY][0]) + B[MY], m2 = fabs(q[MZ][0]) + B[MZ];
     U ke = U(0.5) * (m0 * m0 + m1 * m1 + m2 * m2) / rlo;
-    U Plo = U(ph.aindm1) * (Elo - ke);
+    U Plo = PHC(U, ph, aindm1) * (Elo - ke);
     return Plo >= epsiP + tol * (fabs(q[EN][0]) + B[EN] + ke);
 }
 
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(LIMIT_TPB) k_limit(T* __restrict__ Q, Geom G, 
             q[v][b] = Qb[(long long)(b * NQ + v) * nc + le];
         });
     });
-    if (q[RH][0] >= T(ph.rh_floor) && limit_bound_clear<TB, T>(ph, q)) return;
+    if (q[RH][0] >= PHC(T, ph, rh_floor) && limit_bound_clear<TB, T>(ph, q)) return;
     bool changed;
     if constexpr (std::is_same<T, double>::value) {
         changed = limit_cell<TB, double>(ph, q);
@@ -808,7 +808,7 @@ __device__ __forceinline__ void cell_volume_linear_stress(const CellArgs& a, Cel
     });
     if (!act) return;
     // K(d, m) di_d: diagonal rows (4/3, -2/3, -2/3) colvis v_d, off-diagonal colvis v_other
-    const T cv = T(ph.colvis), c4 = T(4.0 / 3.0) * cv, c2 = -(T(2.0 / 3.0) * cv);
+    const T cv = PHC(T, ph, colvis), c4 = T(4.0 / 3.0) * cv, c2 = -(T(2.0 / 3.0) * cv);
     sfor<3>([&](auto dd) {
         constexpr int d = decltype(dd)::value;
         const T di = cx.di[d];
@@ -837,7 +837,7 @@ __device__ __forceinline__ void cell_volume_linear_stress(const CellArgs& a, Cel
     });
     if (ph.ivis == 0) {   // sources.f90:37-43, linear: the coefficients themselves (src_gram)
         static_assert(src_gram_is_identity<TB>(), "source projection of a linear field is not the identity");
-        const T mc = -T(ph.coll);
+        const T mc = -PHC(T, ph, coll);
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
             sfor<6>([&](auto mm) {
@@ -956,7 +956,7 @@ __device__ __forceinline__ void cell_volume(const CellArgs& a, CellCtx<T>& cx, T
     // cell_volume_linear_stress
     static_assert(src_gram_is_identity<TB>(), "source projection of a linear field is not the identity");
     if (GRP == 0 && ph.body_force != 0.0) {
-        const T bf = T(ph.body_force);
+        const T bf = PHC(T, ph, body_force);
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
             acc[MX][b] = fma(bf, T(qs[(b * NQ + RH) * CELL_CPB + lc]), acc[MX][b]);
@@ -1083,7 +1083,7 @@ __device__ __forceinline__ void cell_surface_update(const CellArgs& a, CellCtx<T
                 sfor<NB>([&](auto bb) { acc[m][decltype(bb)::value] = r[decltype(bb)::value]; });
                 if constexpr (m == 2) {
                     // integrator.f90:207-218: trace-coupled semi-implicit update
-                    const T coll = T(ph.coll), c1d3 = T(1.0 / 3.0);
+                    const T coll = PHC(T, ph, coll), c1d3 = T(1.0 / 3.0);
                     sfor<NB>([&](auto bb) {
                         constexpr int b = decltype(bb)::value;
                         const T q0 = qs[(b * NQ + PXX) * CELL_CPB + lc], q1 = qs[(b * NQ + PYY) * CELL_CPB + lc];
@@ -1122,7 +1122,7 @@ __device__ __forceinline__ void cell_split_source(const CellArgs& a, CellCtx<T>&
     const T dt = cx.dt;
     T src[6][NB];
     sfor<6>([&](auto mm) { sfor<NB>([&](auto bb) { src[decltype(mm)::value][decltype(bb)::value] = T(0); }); });
-    const T coll = T(ph.coll), oth = T(1.0 / 3.0);
+    const T coll = PHC(T, ph, coll), oth = T(1.0 / 3.0);
     sfor_seq<NPG>([&](auto gg) {
         constexpr int g = decltype(gg)::value;
         T u[4];
@@ -1223,7 +1223,7 @@ __global__ void __launch_bounds__(2 * CELL_CPB, (CellMinBlocks<T, TB::NB>::value
     cx.noise = a.ph.llns != 0;
     cx.nctr = NoiseCtr{cx.noise ? *a.step : 0ull, a.stage};
     cx.dt = cx.act ? T(a.st[cx.bx].dt) : T(0);
-    cx.faci = T(1) / (T(1) + cx.dt * T(a.ph.coll));
+    cx.faci = T(1) / (T(1) + cx.dt * PHC(T, a.ph, coll));
     cx.ob = out + B.q0;
     cx.q0b = Q0 ? Q0 + B.q0 : nullptr;
     cx.bad = false;
@@ -1312,7 +1312,7 @@ __device__ __forceinline__ void update_cell_var(const T* Qin, const T* Q0, T* ou
         for (int b = 0; b < NB; ++b) ob[(long long)(b * NQ + v) * nc + le] = r[b];
         return;
     }
-    const T dt = T(a.st[bx].dt), faci = T(1) / (T(1) + dt * T(a.ph.coll));
+    const T dt = T(a.st[bx].dt), faci = T(1) / (T(1) + dt * PHC(T, a.ph, coll));
     const T* qb = Qin + B.q0;
     const T* q0b = Q0 ? Q0 + B.q0 : nullptr;
     const bool stress_faci = v >= PXX && a.ph.ivis == 1;
@@ -1353,7 +1353,7 @@ __global__ void __launch_bounds__(UPD_CPB * NQ, 3) k_update_limit(const T* Qin, 
     __syncthreads();
     if (v != 0 || !act) return;
     StridedRows<T> q{hyd + lc, NB * UPD_CPB, UPD_CPB};
-    if (!(q[RH][0] >= T(a.ph.rh_floor) && limit_bound_clear<TB, T>(a.ph, q)))
+    if (!(q[RH][0] >= PHC(T, a.ph, rh_floor) && limit_bound_clear<TB, T>(a.ph, q)))
         limit_rows_smem<TB, T>(a.ph, hyd + lc, NB * UPD_CPB, UPD_CPB);
     const int bx = box_of_cell(a.G, gc);
     const Box& B = a.G.boxes[bx];

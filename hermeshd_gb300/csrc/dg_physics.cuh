@@ -104,7 +104,7 @@ __device__ __forceinline__ void random_stress_amp(T eta, T zeta, unsigned long l
 template <class T>
 __device__ __forceinline__ void random_stress(const Phys& ph, unsigned long long seed, NoiseCtr nc, unsigned kind,
                                               unsigned long long site, unsigned pt, T S[6]) {
-    random_stress_amp<T>(T(ph.eta_sd), T(ph.zeta_sd), seed, nc, kind, site, pt, S);
+    random_stress_amp<T>(PHC(T, ph, eta_sd), PHC(T, ph, zeta_sd), seed, nc, kind, site, pt, S);
 }
 
 // ---------------------------------------------------------------------------
@@ -125,10 +125,10 @@ __device__ __forceinline__ Prim<T> primitives(const Phys& ph, const T q[NQ]) {
     w.vy = q[MY] * w.dni;
     w.vz = q[MZ] * w.dni;
     T smsq = q[MX] * q[MX] + q[MY] * q[MY] + q[MZ] * q[MZ];
-    w.P = T(ph.aindm1) * (q[EN] - T(0.5) * w.dni * smsq);
+    w.P = PHC(T, ph, aindm1) * (q[EN] - T(0.5) * w.dni * smsq);
     w.Pig = w.P;
-    if (ph.ieos == 2) w.P = T(ph.P_1) * (pow(w.dn, T(7.2)) - T(1)) + T(ph.P_base) + w.P;
-    const T Pf = T(ph.P_floor);
+    if (ph.ieos == 2) w.P = PHC(T, ph, P_1) * (pow(w.dn, T(7.2)) - T(1)) + PHC(T, ph, P_base) + w.P;
+    const T Pf = PHC(T, ph, P_floor);
     if (w.P < Pf) w.P = Pf;
     // the 10-moment pressure enters only the ivis 2/3 fluxes (flux.f90:91-95)
     if (ph.ivis >= 2) {
@@ -143,7 +143,7 @@ __device__ __forceinline__ Prim<T> primitives(const Phys& ph, const T q[NQ]) {
 // S = {Sxx, Syy, Szz, Sxy, Sxz, Syz} (zero without noise)
 template <class T, int DIR>
 __device__ __forceinline__ void point_flux(const Phys& ph, const T q[NQ], const Prim<T>& w, const T S[6], T f[NQ]) {
-    const T colvis = T(ph.colvis);
+    const T colvis = PHC(T, ph, colvis);
     const T c2d3cv = T(2.0 / 3.0) * colvis, c4d3cv = T(4.0 / 3.0) * colvis;
     const T M_x = q[MX], M_y = q[MY], M_z = q[MZ], Ener = q[EN];
     const T P_xx = q[PXX], P_yy = q[PYY], P_zz = q[PZZ], P_xy = q[PXY], P_xz = q[PXZ], P_yz = q[PYZ];
@@ -231,7 +231,7 @@ __device__ __forceinline__ void point_flux(const Phys& ph, const T q[NQ], const 
 template <class T>
 __device__ __forceinline__ void ten_moment_source(const Phys& ph, const Prim<T>& w, T s[6]) {
     const T vx2 = w.vx * w.vx, vy2 = w.vy * w.vy, vz2 = w.vz * w.vz;
-    const T colldn = T(ph.coll) * w.dn, c1d3 = T(1.0 / 3.0);
+    const T colldn = PHC(T, ph, coll) * w.dn, c1d3 = T(1.0 / 3.0);
     s[0] = colldn * (T(2) * vx2 - vy2 - vz2) * c1d3;
     s[1] = colldn * (T(2) * vy2 - vz2 - vx2) * c1d3;
     s[2] = colldn * (T(2) * vz2 - vx2 - vy2) * c1d3;
@@ -246,11 +246,11 @@ __device__ __forceinline__ T cfcal(const Phys& ph, const T q[NQ]) {
     T dn = q[RH], dni = T(1) / dn;
     T vx = q[MX] * dni, vy = q[MY] * dni, vz = q[MZ] * dni;
     T P;
-    if (ph.ivis == 0 || ph.ivis == 1) P = T(ph.aindm1) * (q[EN] - T(0.5) * dn * (vx * vx + vy * vy + vz * vz));
+    if (ph.ivis == 0 || ph.ivis == 1) P = PHC(T, ph, aindm1) * (q[EN] - T(0.5) * dn * (vx * vx + vy * vy + vz * vz));
     else P = T(1.0 / 3.0) * (q[PXX] + q[PYY] + q[PZZ] - dn * (vx * vx + vy * vy + vz * vz));
     T cs;
-    if (ph.ieos == 1) cs = sqrt(T(ph.aindex) * P * dni);
-    else cs = sqrt(T(7.2) * T(ph.P_1) * pow(dn, T(6.2)));
+    if (ph.ieos == 1) cs = sqrt(PHC(T, ph, aindex) * P * dni);
+    else cs = sqrt(T(7.2) * PHC(T, ph, P_1) * pow(dn, T(6.2)));
     T vd = DIR == 0 ? vx : DIR == 1 ? vy : vz;
     return fabs(vd) + cs;
 }
@@ -271,7 +271,7 @@ __device__ __forceinline__ void hllc(const Phys& ph, const T qL[NQ], const T qR[
     constexpr int IPAR = DIR == 0 ? MX : DIR == 1 ? MY : MZ;
     constexpr int IP1 = DIR == 0 ? MY : DIR == 1 ? MZ : MX;
     constexpr int IP2 = DIR == 0 ? MZ : DIR == 1 ? MX : MY;
-    const T aindex = T(ph.aindex);
+    const T aindex = PHC(T, ph, aindex);
     const T dniL = PL.dni, dniR = PR.dni;
     const T rhoL = qL[RH], rhoR = qR[RH];
     const T uL = DIR == 0 ? PL.vx : DIR == 1 ? PL.vy : PL.vz;
@@ -280,10 +280,10 @@ __device__ __forceinline__ void hllc(const Phys& ph, const T qL[NQ], const T qR[
     T pR = PR.Pig;
     T cL, cR;
     if (ph.ieos == 2) {
-        pL = T(ph.P_1) * (pow(rhoL, T(7.2)) - T(1)) + T(ph.P_base) + pL;
-        pR = T(ph.P_1) * (pow(rhoR, T(7.2)) - T(1)) + T(ph.P_base) + pR;
-        cL = sqrt(T(7.2) * T(ph.P_1) * pow(rhoL, T(6.2)) + pL * rho_i_last);
-        cR = sqrt(T(7.2) * T(ph.P_1) * pow(rhoR, T(6.2)) + pR * rho_i_last);
+        pL = PHC(T, ph, P_1) * (pow(rhoL, T(7.2)) - T(1)) + PHC(T, ph, P_base) + pL;
+        pR = PHC(T, ph, P_1) * (pow(rhoR, T(7.2)) - T(1)) + PHC(T, ph, P_base) + pR;
+        cL = sqrt(T(7.2) * PHC(T, ph, P_1) * pow(rhoL, T(6.2)) + pL * rho_i_last);
+        cR = sqrt(T(7.2) * PHC(T, ph, P_1) * pow(rhoR, T(6.2)) + pR * rho_i_last);
     } else {
         // sqrt(aindex*p/rho) of flux.f90:537-538, with the division taken as
         // a product with 1/rho (one rounding apart; two divisions fewer)
@@ -296,7 +296,7 @@ __device__ __forceinline__ void hllc(const Phys& ph, const T qL[NQ], const T qR[
     T sm_num = rhoR * uR * (sR - uR) - rhoL * uL * (sL - uL);
     sm_num = sm_num + pL - pR;
     T sm_den = rhoR * (sR - uR) - rhoL * (sL - uL);
-    if (sm_den == T(0)) sm_den = T(ph.rh_floor);
+    if (sm_den == T(0)) sm_den = PHC(T, ph, rh_floor);
     const T sM = sm_num / sm_den;
     const T pstar = rhoL * (uL - sL) * (uL - sM) + pL;
     // flux.f90:623-643: the last true condition wins
@@ -315,7 +315,7 @@ __device__ __forceinline__ void hllc(const Phys& ph, const T qL[NQ], const T qR[
         const T* ff = left ? fL : fR;
         const T s = left ? sL : sR, rho = left ? rhoL : rhoR, u = left ? uL : uR, p = left ? pL : pR;
         T den = s - sM;
-        if (den == T(0)) den = T(ph.rh_floor);
+        if (den == T(0)) den = PHC(T, ph, rh_floor);
         const T slrm_i = T(1) / den;
         const T sq = s - u;
         const T Q0 = rho * sq * slrm_i;
@@ -349,7 +349,7 @@ __device__ __forceinline__ bool roe(const Phys& ph, const T qL[NQ], const T qR[N
     constexpr int IP = DIR == 0 ? MX : DIR == 1 ? MY : MZ;
     constexpr int I1 = DIR == 0 ? MY : DIR == 1 ? MZ : MX;
     constexpr int I2 = DIR == 0 ? MZ : DIR == 1 ? MX : MY;
-    const T aindm1 = T(ph.aindm1), cp = T(ph.aindex / ph.aindm1);
+    const T aindm1 = PHC(T, ph, aindm1), cp = PHC(T, ph, roe_cp);
     T skr[2], swr[2][4];
 #pragma unroll
     for (int j9 = 0; j9 < 2; ++j9) {

@@ -258,7 +258,7 @@ __device__ __forceinline__ void limit_rows(const Phys& ph, T (&o)[NQ][TB::NB]) {
     constexpr int NB = TB::NB;
     T q[5][NB];
     sfor<5>([&](auto vv) { sfor<NB>([&](auto bb) { q[decltype(vv)::value][decltype(bb)::value] = o[decltype(vv)::value][decltype(bb)::value]; }); });
-    if (q[RH][0] >= T(ph.rh_floor) && limit_bound_clear<TB, T>(ph, q)) return;
+    if (q[RH][0] >= PHC(T, ph, rh_floor) && limit_bound_clear<TB, T>(ph, q)) return;
     if constexpr (std::is_same<T, double>::value) {
         if (!limit_cell<TB, double>(ph, q)) return;
     } else {
@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(TILE_NT, (TileMinBlocks<T>::value))
     // the ivis 0 relaxation -coll P_ij (sources.f90:37-43) and the body force,
     // projected as the same linear map of the coefficients
     static_assert(src_gram_is_identity<TB>(), "source projection of a linear field is not the identity");
-    const T mc = ph.ivis == 0 ? T(ph.coll) : T(0), bf = T(ph.body_force);
+    const T mc = ph.ivis == 0 ? PHC(T, ph, coll) : T(0), bf = PHC(T, ph, body_force);
     sfor<NQ>([&](auto vv) { sfor<NB>([&](auto bb) {
         constexpr int v = decltype(vv)::value, b = decltype(bb)::value;
         T r = rs[(v * NB + b) * TILE_NT + tid];
@@ -477,7 +477,7 @@ __global__ void __launch_bounds__(TILE_NT, (TileMinBlocks<T>::value))
         }); });
         return;
     }
-    const T dt = T(a.st[bx].dt), faci = T(1) / (T(1) + dt * T(ph.coll));
+    const T dt = T(a.st[bx].dt), faci = T(1) / (T(1) + dt * PHC(T, ph, coll));
     const T* q0b = Q0 ? Q0 + B.q0 : nullptr;
     bool bad = false;
     // one variable at a time: the stress rows are stored as they are made;
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(DT_TPB) k_mindt_limit(T* __restrict__ Q, DtArg
     }
     if (!act || !(a.ph.ieos == 1 || a.ph.ieos == 2)) return;
     // the limiter (k_limit's operations)
-    if (q[RH][0] >= T(a.ph.rh_floor) && limit_bound_clear<TB, T>(a.ph, q)) return;
+    if (q[RH][0] >= PHC(T, a.ph, rh_floor) && limit_bound_clear<TB, T>(a.ph, q)) return;
     bool changed;
     if constexpr (std::is_same<T, double>::value) {
         changed = limit_cell<TB, double>(a.ph, q);

@@ -277,6 +277,7 @@ Phys make_phys(const hermes_config& c) {
     p.ieos = c.ieos;
     p.ihllc = c.ihllc;
     p.llns = c.llns ? 1 : 0;
+    phys_finish(p);
     return p;
 }
 

@@ -56,7 +56,32 @@ struct Phys {
     double eta_sd, zeta_sd, body_force;
     double inflow_u, inflow_rho, inflow_p, inflow_ly;   // parabolic x-low inflow (BC_INFLOW)
     int ivis, ieos, ihllc, llns;
+    double roe_cp;   // aindex / aindm1 (the Roe enthalpy's factor), set by phys_finish
+    // the same constants rounded to float once on the host (phys_finish): the
+    // FP32 kernels read these instead of converting a double per use, a
+    // conversion that runs on the FP64 pipe
+    float f_aindex, f_aindm1, f_rh_floor, f_T_floor, f_P_floor, f_rh_mult, f_coll, f_colvis, f_P_1, f_P_base;
+    float f_eta_sd, f_zeta_sd, f_body_force, f_roe_cp;
 };
+
+// fill the float copies (round to nearest, as a conversion on the device would)
+inline void phys_finish(Phys& p) {
+    p.f_aindex = (float)p.aindex; p.f_aindm1 = (float)p.aindm1; p.f_rh_floor = (float)p.rh_floor;
+    p.f_T_floor = (float)p.T_floor; p.f_P_floor = (float)p.P_floor; p.f_rh_mult = (float)p.rh_mult;
+    p.f_coll = (float)p.coll; p.f_colvis = (float)p.colvis; p.f_P_1 = (float)p.P_1; p.f_P_base = (float)p.P_base;
+    p.f_eta_sd = (float)p.eta_sd; p.f_zeta_sd = (float)p.zeta_sd; p.f_body_force = (float)p.body_force;
+    p.roe_cp = p.aindex / p.aindm1;
+    p.f_roe_cp = (float)p.roe_cp;
+}
+
+// a physics constant in the arithmetic type T: the float copy for T = float,
+// the double converted to T otherwise
+template <class T>
+__host__ __device__ __forceinline__ T phys_const(double d, float f) {
+    if constexpr (std::is_same<T, float>::value) return f;
+    else return T(d);
+}
+#define PHC(T, ph, name) (::hermes::phys_const<T>((ph).name, (ph).f_##name))
 
 // one grid of the run (one realisation of an ensemble)
 struct Box {

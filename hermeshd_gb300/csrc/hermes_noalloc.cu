@@ -188,6 +188,7 @@ extern "C" int hermes_rhs_noalloc(const hermes_config* cfg, void* q, void* rhs, 
     ph.P_1 = c.P_1; ph.P_base = c.P_base; ph.eta_sd = c.eta_sd; ph.zeta_sd = c.zeta_sd;
     ph.body_force = c.body_force; ph.ivis = c.ivis; ph.ieos = c.ieos; ph.ihllc = c.ihllc;
     ph.llns = c.llns ? 1 : 0;
+    phys_finish(ph);
     Geom G{};
     G.boxes = A->box;
     G.nbox = 1;
