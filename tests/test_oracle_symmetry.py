@@ -5,7 +5,7 @@ in every Legendre product) and with the reflection x -> -x (cells in reverse
 order, m_x, P_xy, P_xz and the basis functions odd in x negated): the
 right-hand side comes out transformed the same way, to rounding.  Every
 direction-specific table, flux and index of the restatement, and the
-left/right roles of every face, are exercised against their mirrors.""" 
+left/right roles of every face, are exercised against their mirrors."""
 import numpy as np
 import pytest
 
