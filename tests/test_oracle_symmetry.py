@@ -82,3 +82,35 @@ def test_rhs_commutes_with_the_x_reflection(nb, iq, ivis, ihllc):
     scale = np.abs(R).max()
     assert np.allclose(Rr, reflect_x(R, kin, nb), rtol=0, atol=1e-12 * scale), \
         float(np.abs(Rr - reflect_x(R, kin, nb)).max() / scale)
+
+
+def exchange_xz(Q, kindex, nb):
+    """x <-> z: cell indices, m_x <-> m_z, P_xx <-> P_zz, P_xy <-> P_yz, and the
+    basis functions x <-> z, xy <-> yz, xx <-> zz."""
+    names = ["kx", "ky", "kz", "kyz", "kzx", "kxy", "kxyz", "kxx", "kyy", "kzz"]
+    k = {n: int(kindex[i]) - 1 for i, n in enumerate(names)}
+    perm = list(range(nb))
+    for a, b in (("kx", "kz"), ("kxy", "kyz"), ("kxx", "kzz")):
+        if k[a] < nb and k[b] < nb:
+            perm[k[a]], perm[k[b]] = k[b], k[a]
+    var = [RH, MZ, MY, MX, EN, PZZ, PYY, PXX, PYZ, PXZ, PXY]
+    S = np.transpose(Q, (2, 1, 0, 3, 4))[:, :, :, var, :][:, :, :, :, perm]
+    return np.asfortranarray(S)
+
+
+@pytest.mark.parametrize("nb,iq", [(4, 2), (8, 2), (10, 3)])
+@pytest.mark.parametrize("ivis,ihllc", [(1, 1), (2, 2)])
+def test_rhs_commutes_with_the_xz_exchange(nb, iq, ivis, ihllc):
+    import oracle as O
+    cfg = config.Config(nx=4, ny=3, nz=4, nbasis=nb, iquad=iq, ivis=ivis, ihllc=ihllc, coll=1.3, colvis=0.7,
+                        lx=1.6, ly=1.2, lz=1.6)
+    orc = O.Oracle(cfg)
+    kin = orc.kindex()
+    Q = ic.random_smooth(cfg, seed=3 * nb + ivis, amp=0.05, stress_amp=0.02)
+    if ivis == 2:
+        Q = ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.01, seed=3)
+    R = orc.rhs(np.asfortranarray(Q), limit=False)
+    Rx = orc.rhs(exchange_xz(Q, kin, nb), limit=False)
+    scale = np.abs(R).max()
+    assert np.allclose(Rx, exchange_xz(R, kin, nb), rtol=0, atol=1e-12 * scale), \
+        float(np.abs(Rx - exchange_xz(R, kin, nb)).max() / scale)
