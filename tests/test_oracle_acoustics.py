@@ -53,3 +53,33 @@ def test_sound_wave_travels_at_the_sound_speed(nb, iq, nx, tol):
     assert err <= tol, err
     # a wave at the wrong speed would be out of phase: one at 0.9 c is off by ~0.6
     assert np.linalg.norm(np.roll(d0, nx // 10) - d0) / np.linalg.norm(d0) > 20 * tol
+
+
+@pytest.mark.parametrize("ihllc", [2, 0])
+def test_shear_wave_decays_at_the_navier_stokes_rate(ihllc):
+    """ivis 1 with coll = p / mu and colvis = p relaxes the stress to the
+    Navier-Stokes shear stress -mu dv/dx: a transverse velocity sin(k x) decays
+    as exp(-mu k^2 t / rho) (relaxation time mu / p = 0.01 here, so the
+    10-moment correction is ~0.4 %).  With the Roe and the central flux; the
+    reference's HLLC receives the stress-augmented point flux and is
+    discontinuous at S_M = 0, where a shear wave (v_x = 0) sits at every face,
+    and it amplifies the wave instead (flux.f90:87-89,623-643)."""
+    import oracle as O
+    nx, mu, p0, rho0, eps = 64, 0.01, 1.0, 1.0, 1e-3
+    cfg = config.Config(nx=nx, ny=1, nz=1, nbasis=4, iquad=2, ivis=1, coll=p0 / mu, colvis=p0, ihllc=ihllc, iorder=3,
+                        lx=1.0, ly=1.0 / nx, lz=1.0 / nx)
+    dx = cfg.lx / nx
+    xl = -cfg.lx / 2 + dx * np.arange(nx)
+    k = 2 * math.pi / cfg.lx
+    s = (np.cos(k * xl) - np.cos(k * (xl + dx))) / (k * dx)
+    Q = np.zeros(cfg.shape_f, order="F")
+    Q[:, 0, 0, RH, 0] = rho0
+    Q[:, 0, 0, 2, 0] = rho0 * eps * s                          # m_y
+    Q[:, 0, 0, EN, 0] = p0 / (cfg.aindex - 1) + 0.5 * rho0 * (eps * s) ** 2
+    orc = O.Oracle(cfg)
+    t = 0.0
+    while t < 1.0:
+        t, _ = orc.advance(Q, 20, t=t)
+    amp = float(Q[:, 0, 0, 2, 0] @ s) / float(rho0 * eps * (s @ s))
+    expect = math.exp(-mu * k * k * t / rho0)
+    assert abs(amp / expect - 1.0) < 0.01, (amp, expect, t)
