@@ -50,3 +50,20 @@ def test_uniform_state_rhs_is_minus_the_source(ivis, nb, iq):
         assert np.allclose(r0[RH:EN + 1], 0.0, atol=1e-13 * scale), r0[:5]
         assert np.allclose(r0[PXX:], expect, rtol=1e-13, atol=1e-13 * scale), (r0[PXX:], expect)
         assert np.abs(R[cell + (slice(None), slice(1, None))]).max() <= 1e-12 * scale
+
+
+def test_ten_moment_stage_relaxes_the_deviator_and_keeps_the_trace():
+    """ivis 2's semi-implicit update (integrator.f90:207-224) of a uniform state
+    at rest: the pressure tensor's trace (3 p) is kept and its deviator scaled
+    by faci = 1 / (1 + dt coll) per stage; the off-diagonal stresses likewise."""
+    import oracle as O
+    coll, dt = 3.0, 0.05
+    cfg = config.Config(nx=2, ny=2, nz=2, nbasis=4, iquad=2, ivis=2, coll=coll, colvis=1.0)
+    Q = uniform_state(cfg, v=(0.0, 0.0, 0.0), stress=(1.3, 0.9, 0.8, 0.07, -0.05, 0.02))
+    E = O.Oracle(cfg).euler_step(np.asfortranarray(Q), dt)
+    faci = 1.0 / (1.0 + dt * coll)
+    P0, P1 = Q[0, 0, 0, PXX:PYZ + 1, 0], E[0, 0, 0, PXX:PYZ + 1, 0]
+    assert P1[:3].sum() == pytest.approx(P0[:3].sum(), rel=1e-14)
+    dev0, dev1 = P0[:3] - P0[:3].mean(), P1[:3] - P1[:3].mean()
+    assert np.allclose(dev1, faci * dev0, rtol=1e-13, atol=1e-15)
+    assert np.allclose(P1[3:], faci * P0[3:], rtol=1e-13, atol=1e-15)
