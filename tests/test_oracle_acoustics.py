@@ -83,3 +83,40 @@ def test_shear_wave_decays_at_the_navier_stokes_rate(ihllc):
     amp = float(Q[:, 0, 0, 2, 0] @ s) / float(rho0 * eps * (s @ s))
     expect = math.exp(-mu * k * k * t / rho0)
     assert abs(amp / expect - 1.0) < 0.01, (amp, expect, t)
+
+
+@pytest.mark.parametrize("ihllc", [0, 1])
+def test_tait_sound_wave_travels_at_the_linearised_speed(ihllc):
+    """ieos 2: P = (gamma-1)(E - rho v^2/2) + P_1 (rho^7.2 - 1) + P_base with the
+    energy flux (E + P) v; linearised at rest, c^2 = ((gamma-1)(E0 + P0) +
+    7.2 P_1 rho0^7.2) / rho0.  A right-moving wave of that speed returns after
+    a period, with the central flux and with the reference's HLLC (its stale
+    1/rho only shifts the wave-speed estimates, flux.f90:533-534)."""
+    import oracle as O
+    nx = 64
+    cfg = config.Config(nx=nx, ny=1, nz=1, nbasis=4, iquad=2, ivis=0, coll=0.0, colvis=0.0, ihllc=ihllc, iorder=3,
+                        ieos=2, P_1=0.05, P_base=1.0, lx=1.0, ly=1.0 / nx, lz=1.0 / nx)
+    g, rho0, pig0, eps = cfg.aindex, 1.0, 1.0, 1e-4
+    E0 = pig0 / (g - 1)
+    P0 = pig0 + cfg.P_1 * (rho0 ** 7.2 - 1) + cfg.P_base
+    c2 = ((g - 1) * (E0 + P0) + 7.2 * cfg.P_1 * rho0 ** 7.2) / rho0
+    c = math.sqrt(c2)
+    dx = cfg.lx / nx
+    xl = -cfg.lx / 2 + dx * np.arange(nx)
+    k = 2 * math.pi / cfg.lx
+    s = (np.cos(k * xl) - np.cos(k * (xl + dx))) / (k * dx)
+    rho, u = rho0 + eps * s, eps * c * s / rho0
+    dE = (eps * c2 * s - 7.2 * cfg.P_1 * rho0 ** 6.2 * eps * s) / (g - 1)
+    Q = np.zeros(cfg.shape_f, order="F")
+    Q[:, 0, 0, RH, 0] = rho
+    Q[:, 0, 0, MX, 0] = rho * u
+    Q[:, 0, 0, EN, 0] = E0 + dE + 0.5 * rho * u * u
+    d0 = Q[:, 0, 0, RH, 0] - rho0
+    period = cfg.lx / c
+    n = int(math.ceil(period / (0.1 * dx / c)))
+    n += n % 2
+    orc = O.Oracle(cfg)
+    orc.advance_fixed_dt(Q, period / n, n // 2)
+    assert np.linalg.norm(Q[:, 0, 0, RH, 0] - rho0 + d0) <= 5e-3 * np.linalg.norm(d0)
+    orc.advance_fixed_dt(Q, period / n, n // 2)
+    assert np.linalg.norm(Q[:, 0, 0, RH, 0] - rho0 - d0) <= 5e-3 * np.linalg.norm(d0)
