@@ -92,7 +92,8 @@ class Config:
     # physics switches
     ivis: int = 0                    # 0 explicit, 1 semi-implicit stress, 2 10-moment, 3 Grad closure (E_ij)
     ieos: int = 1                    # 1 ideal gas, 2 Murnaghan-Tait
-    ihllc: int = 1                   # 0 central/LLF, 1 HLLC, 2 Roe (the monolithic code's iroe)
+    ihllc: int = 1                   # 0 central/LLF, 1 HLLC, 2 Roe (the monolithic code's iroe; ideal-gas
+                                     # Roe average: with ieos 2 use 0 or 1)
     aindex: float = 5.0 / 3.0        # gamma
     rh_floor: float = 5.0e-6         # params.f90:93
     T_floor: float = field(default_factory=lambda: Units().T_floor)

@@ -62,7 +62,9 @@ typedef struct hermes_config {
                                   dg_3D_hydro_bitri_ten_moment.f90 (its ivis 0) */
     int32_t ieos;              /* 1 ideal gas, 2 Murnaghan-Tait */
     int32_t ihllc;             /* Riemann solver for rh..en: 0 central/LLF only, 1 HLLC (flux.f90:264-271),
-                                  2 Roe (src/ces/10_moment/dg_3D_hydro_lqc_SEAN.f90:1614-1789) */
+                                  2 Roe (src/ces/10_moment/dg_3D_hydro_lqc_SEAN.f90:1614-1789; its Roe
+                                  average is the ideal-gas one, so with ieos 2 it does not carry the
+                                  Tait sound speed: use 0 or 1 there) */
     int32_t bc[6];             /* xlo, xhi, ylo, yhi, zlo, zhi: HERMES_BC_* */
     int32_t precision;         /* 64 (FP64) or 32 (FP32 bulk, FP64 CFL and limiter fixes) */
     int32_t llns;              /* nonzero: stochastic stress (random.f90:106-145) */
