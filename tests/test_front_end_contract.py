@@ -5,7 +5,7 @@ Fortran-ordered arrays (src/test_hermeshd.py:48-50, nx 50, nbasis 8), which
 run on the FP32 path; float64 arrays run on the FP64 path.
 
 The rejections happen before a context exists, so they run without a GPU;
-the driver loop itself is a GPU test."""
+the reference script's loop itself is a GPU test."""
 import numpy as np
 import pytest
 
