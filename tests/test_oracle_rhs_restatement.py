@@ -1,0 +1,215 @@
+"""The whole right-hand side restated a second time in numpy, against the C
+oracle, on 3-D grids with every basis mode populated: periodic, and with the
+wall, no-slip and outflow boundaries (boundary.f90:76-338 on the traces that
+prepare_step.f90:20-41 hands them).
+
+Independent of the oracle's tables and loops: the basis is evaluated here
+from its definition (initialize.f90:126-217: the families {1, x, y, z},
+{1, x, y, z, yz, zx, xy, xyz} and {1, x, y, z, yz, zx, xy, P2(x), P2(y),
+P2(z)} of unnormalised Legendre products with cbasis = prod(2k + 1)), and the
+operator is written in its general form
+
+  glflux_b = 1/4 cbasis_b sum_d dxi_d [ sum_faces w2 (phi_b(+) F_d,hi - phi_b(-) F_d,lo)
+                                        - sum_points w3 d phi_b/ds_d f_d(Q) ]
+  source_b = 1/8 cbasis_b sum_points w3 phi_b S(Q)
+
+which flux.f90:751-928 (innerintegral2, written out row by row for each basis
+function) and flux.f90:958-972 (glflux) and sources.f90:70-76 spell out.  The
+face fluxes come from the per-state restatement of flux.f90 in
+test_oracle_face_restatement.py.  The C oracle evaluates the same operator
+through its own tables (basis_funcs.f90's bfvals_*), loops and reductions,
+so agreement to rounding (measured 1e-15 to 6e-15 of each variable's scale)
+checks the volume and surface integrals, the face traces, the ghost traces
+and the sources for nb 4/8/10, ivis 0/1/2 and the central, HLLC and Roe
+fluxes."""
+import numpy as np
+import pytest
+
+from hermeshd_gb300 import config, ic
+
+from test_oracle_face_restatement import MX, MZ, face_flux, point_flux, source
+
+NQ = 11
+FAMILIES = {
+    4: [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)],
+    8: [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (0, 1, 1), (1, 0, 1), (1, 1, 0), (1, 1, 1)],
+    10: [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (0, 1, 1), (1, 0, 1), (1, 1, 0), (2, 0, 0), (0, 2, 0),
+         (0, 0, 2)],
+}
+
+
+def leg(k, s):
+    return (1.0, s, 1.5 * s * s - 0.5)[k]
+
+
+def dleg(k, s):
+    return (0.0, 1.0, 3.0 * s)[k]
+
+
+def phi(fam, p):
+    return leg(fam[0], p[0]) * leg(fam[1], p[1]) * leg(fam[2], p[2])
+
+
+def dphi(fam, p, d):
+    out = 1.0
+    for a in range(3):
+        out *= dleg(fam[a], p[a]) if a == d else leg(fam[a], p[a])
+    return out
+
+
+def rule(iquad):
+    s, w = np.polynomial.legendre.leggauss(iquad)
+    return list(s), list(w)
+
+
+def ghost(kind, side, d, interior):
+    """Ghost traces of one boundary face from the interior traces at its
+    points (boundary.f90:76-338): no-slip zeroes every momentum, a wall the
+    normal one; outflow copies the trace and zeroes the normal momentum of
+    all the face's points when any of them flows in (lo: a positive maximum;
+    y/z hi: a negative minimum).  The x-hi outflow routine never copies the
+    trace, so its ghost keeps the zeros it started from."""
+    m = MX + d
+    out = [q.copy() for q in interior]
+    if kind == "noslip":
+        for q in out:
+            q[MX:MZ + 1] = 0.0
+    elif kind == "wall":
+        for q in out:
+            q[m] = 0.0
+    elif kind == "outflow":
+        if side == "hi" and d == 0:
+            return [np.zeros(NQ) for _ in interior]
+        normal = [q[m] for q in out]
+        if (side == "lo" and max(normal) > 0.0) or (side == "hi" and min(normal) < 0.0):
+            for q in out:
+                q[m] = 0.0
+    else:
+        raise ValueError(kind)
+    return out
+
+
+def restated_rhs(cfg, Q):
+    """glflux - source (the oracle's rhs without the limiter), shape of Q."""
+    bcs = ((cfg.xlobc, cfg.xhibc), (cfg.ylobc, cfg.yhibc), (cfg.zlobc, cfg.zhibc))
+    fams = FAMILIES[cfg.nbasis]
+    nb = len(fams)
+    cb = [float((2 * a + 1) * (2 * b + 1) * (2 * c + 1)) for a, b, c in fams]
+    s, w = rule(cfg.iquad)
+    n = (cfg.nx, cfg.ny, cfg.nz)
+    dxi = (cfg.nx / cfg.lx, cfg.ny / cfg.ly, cfg.nz / cfg.lz)
+    interior = [((s[a], s[b], s[c]), w[a] * w[b] * w[c]) for a in range(len(s)) for b in range(len(s))
+                for c in range(len(s))]
+
+    def value(cell, p):
+        return np.array([sum(phi(fams[b], p) * Q[cell + (v, b)] for b in range(nb)) for v in range(NQ)])
+
+    out = np.zeros_like(Q)
+    for i in range(n[0]):
+        for j in range(n[1]):
+            for k in range(n[2]):
+                cell = (i, j, k)
+                g = np.zeros((NQ, nb))
+                src = np.zeros((NQ, nb))
+                # volume terms and sources at the interior points
+                for p, wp in interior:
+                    q = value(cell, p)
+                    f = [point_flux(cfg, q, d) for d in range(3)]
+                    sq = source(cfg, q)
+                    for b in range(nb):
+                        vol = sum(dxi[d] * dphi(fams[b], p, d) * f[d] for d in range(3))
+                        g[:, b] -= 0.25 * cb[b] * wp * vol
+                        src[:, b] += 0.125 * cb[b] * wp * phi(fams[b], p) * sq
+                # surface terms: the hi and lo faces of each direction
+                for d in range(3):
+                    t1, t2 = [a for a in range(3) if a != d]
+                    up = list(cell)
+                    up[d] = (up[d] + 1) % n[d]
+                    dn = list(cell)
+                    dn[d] = (dn[d] - 1) % n[d]
+                    pts = []
+                    for a in range(len(s)):
+                        for c in range(len(s)):
+                            hi = [0.0] * 3
+                            lo = [0.0] * 3
+                            hi[d], lo[d] = 1.0, -1.0
+                            hi[t1] = lo[t1] = s[a]
+                            hi[t2] = lo[t2] = s[c]
+                            pts.append((hi, lo, w[a] * w[c]))
+                    # neighbour traces, or the boundary's ghost traces at the domain's ends
+                    if cell[d] == n[d] - 1 and bcs[d][1] != "periodic":
+                        right = ghost(bcs[d][1], "hi", d, [value(cell, hi) for hi, _, _ in pts])
+                    else:
+                        right = [value(tuple(up), lo) for _, lo, _ in pts]
+                    if cell[d] == 0 and bcs[d][0] != "periodic":
+                        left = ghost(bcs[d][0], "lo", d, [value(cell, lo) for _, lo, _ in pts])
+                    else:
+                        left = [value(tuple(dn), hi) for hi, _, _ in pts]
+                    for m, (hi, lo, w2) in enumerate(pts):
+                        F_hi, _ = face_flux(cfg, value(cell, hi), right[m], d)
+                        F_lo, _ = face_flux(cfg, left[m], value(cell, lo), d)
+                        for b in range(nb):
+                            g[:, b] += 0.25 * cb[b] * dxi[d] * w2 * (phi(fams[b], hi) * F_hi -
+                                                                     phi(fams[b], lo) * F_lo)
+                out[i, j, k] = g - src
+    return out
+
+
+CASES = [
+    # nb, iquad, ivis, ihllc
+    (4, 2, 0, 1),
+    (4, 2, 1, 2),
+    (8, 2, 1, 1),
+    (8, 2, 2, 0),
+    (10, 3, 0, 2),
+    (10, 3, 2, 1),
+    (10, 3, 1, 0),
+]
+
+
+@pytest.mark.parametrize("nb,iq,ivis,ihllc", CASES,
+                         ids=["nb%d_ivis%d_%s" % (c[0], c[2], ("central", "hllc", "roe")[c[3]]) for c in CASES])
+def test_rhs_matches_the_general_form(nb, iq, ivis, ihllc):
+    import oracle as O
+    cfg = config.Config(nx=3, ny=2, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=1, ihllc=ihllc,
+                        coll=0.0 if ivis == 1 else 0.8, colvis=0.3, lx=1.5, ly=0.8, lz=1.1)
+    Q = ic.random_smooth(cfg, seed=10 * nb + ivis, amp=0.2, stress_amp=0.05)
+    if ivis == 2:
+        ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.05, seed=nb)
+    Q = np.asfortranarray(Q)
+    got = O.Oracle(cfg).rhs(Q.copy(order="F"), limit=False)
+    want = restated_rhs(cfg, Q)
+    scale = np.abs(want).max(axis=(0, 1, 2, 4), keepdims=True)      # per variable
+    err = np.abs(got - want) / np.maximum(scale, 1e-300)
+    assert err.max() <= 1e-12, (err.max(), np.unravel_index(err.argmax(), err.shape))
+    assert np.abs(want[..., 1:]).max() > 1e-3 * np.abs(want).max()   # the higher modes carry weight
+
+
+BC_CASES = [
+    # nb, iquad, ivis, ihllc, boundaries (x lo/hi, y lo/hi, z lo/hi)
+    (8, 2, 1, 1, ("periodic", "periodic", "wall", "wall", "periodic", "periodic")),
+    (4, 2, 1, 2, ("periodic", "periodic", "noslip", "noslip", "periodic", "periodic")),
+    (4, 2, 0, 1, ("outflow", "periodic", "outflow", "outflow", "outflow", "outflow")),
+    (10, 3, 2, 1, ("wall", "wall", "outflow", "noslip", "noslip", "wall")),
+]
+
+
+@pytest.mark.parametrize("nb,iq,ivis,ihllc,bc", BC_CASES, ids=["walls_y_nb8", "noslip_y_nb4_roe", "outflow_nb4",
+                                                                "mixed_nb10_ivis2"])
+def test_rhs_with_boundaries(nb, iq, ivis, ihllc, bc):
+    """The ghost traces of the wall, no-slip and outflow boundaries (outflow
+    states on both sides of the normal-velocity sign, so both of its branches
+    run), in the general form."""
+    import oracle as O
+    cfg = config.Config(nx=3, ny=3, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=1, ihllc=ihllc,
+                        coll=0.0 if ivis == 1 else 0.8, colvis=0.3, lx=1.5, ly=1.2, lz=1.1,
+                        xlobc=bc[0], xhibc=bc[1], ylobc=bc[2], yhibc=bc[3], zlobc=bc[4], zhibc=bc[5])
+    Q = ic.random_smooth(cfg, seed=7 * nb + ivis, amp=0.2, stress_amp=0.05)
+    if ivis == 2:
+        ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.05, seed=nb)
+    Q = np.asfortranarray(Q)
+    got = O.Oracle(cfg).rhs(Q.copy(order="F"), limit=False)
+    want = restated_rhs(cfg, Q)
+    scale = np.abs(want).max(axis=(0, 1, 2, 4), keepdims=True)
+    err = np.abs(got - want) / np.maximum(scale, 1e-300)
+    assert err.max() <= 1e-12, (err.max(), np.unravel_index(err.argmax(), err.shape))
