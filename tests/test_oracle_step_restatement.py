@@ -1,0 +1,149 @@
+"""The whole time step restated a second time in numpy, against the C oracle:
+get_min_dt (hermeshd.f90:145-199), the SSP-RK2/RK3 combinations
+(integrator.f90:62-85) of forward-Euler stages that first limit their input
+in place (integrator.f90:93-114, so the combination reads the limited state),
+and the stage update of each ivis (integrator.f90:125-252), on top of the
+general-form right-hand side of test_oracle_rhs_restatement.py and the numpy
+limiter of test_limiter_restatement.py (face-point basis values evaluated here
+from the basis definition).  ivis 2 follows the one deviation the oracle
+states: the reference never writes rh..en of Q_out in that case, and both
+restatements give them the explicit update.
+
+Quirks carried: the sound speed sqrt(gamma (E/rho - v^2/2)) with gamma, not
+gamma - 1; the maximum over cells with density above rh_mult rh_floor; vmax
+adds the LAST cell's sound speed and uses dxi alone; cflm 0.14 (iquad 2) or
+0.08 (iquad 3) (initialize.f90:104-122).  Measured: the time bit-identical and
+the states within 3e-16 to 6e-16 of each variable's scale after three steps."""
+import math
+
+import numpy as np
+import pytest
+
+from hermeshd_gb300 import config, ic
+
+from test_limiter_restatement import limiter_numpy
+from test_oracle_rhs_restatement import FAMILIES, phi, restated_rhs, rule
+
+RH, MX, MY, MZ, EN, PXX = 0, 1, 2, 3, 4, 5
+
+
+def min_dt(cfg, Q):
+    cflm = cfg.cflm if cfg.cflm > 0 else {2: 0.14, 3: 0.08}[cfg.iquad]
+    vmag, cs = 0.0, 0.0
+    for k in range(cfg.nz):
+        for j in range(cfg.ny):
+            for i in range(cfg.nx):
+                dn = Q[i, j, k, RH, 0]
+                dni = 1.0 / dn
+                vx, vy, vz = (Q[i, j, k, m, 0] * dni for m in (MX, MY, MZ))
+                if cfg.ieos == 1:
+                    cs = math.sqrt(cfg.aindex * (Q[i, j, k, EN, 0] * dni - 0.5 * (vx ** 2 + vy ** 2 + vz ** 2)))
+                else:
+                    cs = math.sqrt(7.2 * cfg.P_1 * dn ** 6.2 + cfg.T_floor)
+                v0 = max(abs(vx) + cs, abs(vy) + cs, abs(vz) + cs)
+                if v0 > vmag and dn > 1.01 * cfg.rh_floor:
+                    vmag = v0
+    return cflm / ((vmag + cs) * (cfg.nx / cfg.lx))
+
+
+def face_basis(cfg):
+    """Basis values at the 6 iquad^2 face points (the limiter's edge points)."""
+    fams = FAMILIES[cfg.nbasis]
+    s, _ = rule(cfg.iquad)
+    rows = []
+    for d in range(3):
+        t1, t2 = [a for a in range(3) if a != d]
+        for side in (1.0, -1.0):
+            for a in s:
+                for c in s:
+                    p = [0.0] * 3
+                    p[d], p[t1], p[t2] = side, a, c
+                    rows.append([phi(f, p) for f in fams])
+    return np.array(rows)
+
+
+def euler_stage(cfg, Q_in, dt, B):
+    """Limits Q_in in place, then returns the stage output."""
+    Q_in[...] = limiter_numpy(Q_in, cfg, B)
+    r = restated_rhs(cfg, Q_in)                 # glflux - source
+    out = Q_in - dt * r
+    faci = 1.0 / (1.0 + dt * cfg.coll)
+    if cfg.ivis == 1:
+        out[..., PXX:, :] *= faci
+    elif cfg.ivis == 2:
+        P = Q_in[..., PXX:PXX + 3, :]
+        g = r[..., PXX:PXX + 3, :]
+        # Q_sum - glf_sum + src_sum with r = glflux - source
+        extra = cfg.coll * dt * P.sum(axis=-2) / 3 - cfg.coll * dt ** 2 * g.sum(axis=-2) / 3
+        out[..., PXX:PXX + 3, :] = faci * (P - dt * g + extra[..., None, :])
+        out[..., PXX + 3:, :] *= faci
+    return out
+
+
+def step(cfg, Q, B):
+    dt = min_dt(cfg, Q)
+    q1 = euler_stage(cfg, Q, dt, B)
+    q2 = euler_stage(cfg, q1, dt, B)
+    if cfg.iorder == 2:
+        return 0.5 * (Q + q2), dt
+    q1 = 0.75 * Q + 0.25 * q2
+    q2 = euler_stage(cfg, q1, dt, B)
+    return (1.0 / 3.0) * Q + (2.0 / 3.0) * q2, dt
+
+
+CASES = [
+    # nb, iquad, ivis, ihllc, iorder, y boundaries
+    (4, 2, 0, 1, 2, "periodic"),
+    (4, 2, 1, 2, 3, "wall"),
+    (8, 2, 1, 1, 2, "noslip"),
+    (10, 3, 2, 1, 3, "periodic"),
+    (10, 3, 0, 0, 3, "wall"),
+]
+
+
+@pytest.mark.parametrize("nb,iq,ivis,ihllc,iorder,ybc", CASES,
+                         ids=["nb%d_ivis%d_rk%d_%s" % (c[0], c[2], c[4], c[5]) for c in CASES])
+def test_three_steps_match_the_oracle(nb, iq, ivis, ihllc, iorder, ybc):
+    import oracle as O
+    cfg = config.Config(nx=3, ny=3, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=1, ihllc=ihllc, iorder=iorder,
+                        coll=5.0 if ivis != 0 else 0.8, colvis=0.3, lx=1.5, ly=1.2, lz=1.1, ylobc=ybc, yhibc=ybc)
+    Q = ic.random_smooth(cfg, seed=nb + 3 * ivis, amp=0.2, stress_amp=0.05)
+    if ivis == 2:
+        ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.05, seed=nb)
+    Q = np.asfortranarray(Q)
+    B = face_basis(cfg)
+    mine, t_mine = Q.copy(), 0.0
+    for _ in range(3):
+        mine, dt = step(cfg, mine, B)
+        t_mine += dt
+    ref = Q.copy(order="F")
+    t_ref, dt_ref = O.Oracle(cfg).advance(ref, 3)
+    assert abs(t_ref - t_mine) <= 1e-14 * t_ref
+    scale = np.abs(ref).max(axis=(0, 1, 2, 4), keepdims=True)
+    err = np.abs(ref - mine) / scale
+    assert err.max() <= 1e-12, (err.max(), np.unravel_index(err.argmax(), err.shape))
+    assert np.abs(ref - Q).max() > 1e-3 * np.abs(Q).max()       # the state moved
+
+
+def test_limited_state_enters_the_combination():
+    """A state the limiter changes: the RK2 combination 0.5 (Q + Q_2) reads
+    the LIMITED Q, because the first stage limits its input in place."""
+    import oracle as O
+    cfg = config.Config(nx=3, ny=2, nz=2, nbasis=4, iquad=2, ivis=0, ieos=1, ihllc=1, iorder=2, coll=0.0,
+                        colvis=0.0, lx=1.5, ly=0.8, lz=1.1)
+    Q = ic.random_smooth(cfg, seed=4, amp=0.1)
+    Q[0, 0, 0, RH, 1:] = 0.9                  # face densities far below zero: theta < 1
+    Q = np.asfortranarray(Q)
+    B = face_basis(cfg)
+    lim = limiter_numpy(Q, cfg, B)
+    assert not np.array_equal(lim, Q)
+    mine, _ = step(cfg, Q.copy(), B)
+    ref = Q.copy(order="F")
+    O.Oracle(cfg).advance(ref, 1)
+    assert np.abs(ref - mine).max() <= 1e-12 * np.abs(ref).max()
+    # combining with the unlimited input instead would differ
+    dt = min_dt(cfg, Q)
+    q = Q.copy()
+    q1 = euler_stage(cfg, q, dt, B)
+    q2 = euler_stage(cfg, q1, dt, B)
+    assert np.abs(0.5 * (Q + q2) - ref).max() > 1e-6
