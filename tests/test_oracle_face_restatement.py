@@ -114,10 +114,12 @@ def cfcal(cfg, q, d):
     return abs(v[d]) + cs
 
 
-def hllc(cfg, qL, qR, fL, fR, d, stale=True):
-    """flux_hllc (flux.f90:466-647) of one face point whose call ends with the
-    right state (so the stale 1/rho of the Tait sound speeds is 1/rho_R).
-    Returns the fluxes of rh, mx, my, mz, en."""
+def hllc(cfg, qL, qR, fL, fR, d, stale=True, rho_last=None):
+    """flux_hllc (flux.f90:466-647) of one face point.  The Tait sound speeds
+    take the stale 1/rho of the last point of the reference's call, the right
+    state at the face's last point: rho_last, or this point's right state when
+    every point of the face carries the same states.  Returns the fluxes of
+    rh, mx, my, mz, en."""
     g, ieos = cfg.aindex, cfg.ieos
     ipar, ip1, ip2 = [(MX, MY, MZ), (MY, MZ, MX), (MZ, MX, MY)][d]
     ivar = (RH, ipar, ip1, ip2, EN)
@@ -132,7 +134,7 @@ def hllc(cfg, qL, qR, fL, fR, d, stale=True):
             p = cfg.P_1 * (rho ** 7.2 - 1.0) + cfg.P_base + p
         side.append((rho, vv, p))
     (rL, vL, pL), (rR, vR, pR) = side
-    rho_i = 1.0 / rR                           # the last point of the call is a right state
+    rho_i = 1.0 / (rR if rho_last is None else rho_last)   # the last point of the call: a right state
 
     def speed(rho, p):
         if ieos == 2:
@@ -243,13 +245,13 @@ def roe(cfg, qL, qR, fL, fR, d):
     return res
 
 
-def face_flux(cfg, qL, qR, d, stale=True):
+def face_flux(cfg, qL, qR, d, stale=True, rho_last=None):
     fL, fR = point_flux(cfg, qL, d), point_flux(cfg, qR, d)
     cfr = max(cfcal(cfg, qL, d), cfcal(cfg, qR, d)) if cfg.ivis == 2 else 0.0
     F = 0.5 * (fL + fR) - 0.5 * cfr * (qR - qL)
     waves = None
     if cfg.ihllc == 1:
-        F[RH:EN + 1], waves = hllc(cfg, qL, qR, fL, fR, d, stale)
+        F[RH:EN + 1], waves = hllc(cfg, qL, qR, fL, fR, d, stale, rho_last)
     elif cfg.ihllc == 2:
         r = roe(cfg, qL, qR, fL, fR, d)
         assert r is not None                   # the cases here keep the Roe sound speed real

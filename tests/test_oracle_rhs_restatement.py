@@ -20,8 +20,9 @@ test_oracle_face_restatement.py.  The C oracle evaluates the same operator
 through its own tables (basis_funcs.f90's bfvals_*), loops and reductions,
 so agreement to rounding (measured 1e-15 to 6e-15 of each variable's scale)
 checks the volume and surface integrals, the face traces, the ghost traces
-and the sources for nb 4/8/10, ivis 0/1/2 and the central, HLLC and Roe
-fluxes."""
+and the sources for nb 4/8/10, ivis 0/1/2, the central, HLLC and Roe fluxes,
+and the Tait EOS with HLLC's stale 1/rho taken from the right state at each
+face's last point."""
 import numpy as np
 import pytest
 
@@ -145,9 +146,12 @@ def restated_rhs(cfg, Q):
                         left = ghost(bcs[d][0], "lo", d, [value(cell, lo) for _, lo, _ in pts])
                     else:
                         left = [value(tuple(dn), hi) for hi, _, _ in pts]
+                    # the Tait sound speeds' stale 1/rho: the right state at the face's last
+                    # point, (s_max, s_max) in the reference's point order (basis_funcs.f90:392-423)
+                    r_hi, r_lo = right[-1][0], value(cell, pts[-1][1])[0]
                     for m, (hi, lo, w2) in enumerate(pts):
-                        F_hi, _ = face_flux(cfg, value(cell, hi), right[m], d)
-                        F_lo, _ = face_flux(cfg, left[m], value(cell, lo), d)
+                        F_hi, _ = face_flux(cfg, value(cell, hi), right[m], d, rho_last=r_hi)
+                        F_lo, _ = face_flux(cfg, left[m], value(cell, lo), d, rho_last=r_lo)
                         for b in range(nb):
                             g[:, b] += 0.25 * cb[b] * dxi[d] * w2 * (phi(fams[b], hi) * F_hi -
                                                                      phi(fams[b], lo) * F_lo)
@@ -156,23 +160,27 @@ def restated_rhs(cfg, Q):
 
 
 CASES = [
-    # nb, iquad, ivis, ihllc
-    (4, 2, 0, 1),
-    (4, 2, 1, 2),
-    (8, 2, 1, 1),
-    (8, 2, 2, 0),
-    (10, 3, 0, 2),
-    (10, 3, 2, 1),
-    (10, 3, 1, 0),
+    # nb, iquad, ivis, ihllc, ieos
+    (4, 2, 0, 1, 1),
+    (4, 2, 1, 2, 1),
+    (8, 2, 1, 1, 1),
+    (8, 2, 2, 0, 1),
+    (10, 3, 0, 2, 1),
+    (10, 3, 2, 1, 1),
+    (10, 3, 1, 0, 1),
+    (4, 2, 0, 1, 2),
+    (10, 3, 1, 1, 2),
+    (8, 2, 2, 0, 2),
 ]
 
 
-@pytest.mark.parametrize("nb,iq,ivis,ihllc", CASES,
-                         ids=["nb%d_ivis%d_%s" % (c[0], c[2], ("central", "hllc", "roe")[c[3]]) for c in CASES])
-def test_rhs_matches_the_general_form(nb, iq, ivis, ihllc):
+@pytest.mark.parametrize("nb,iq,ivis,ihllc,ieos", CASES,
+                         ids=["nb%d_ivis%d_%s%s" % (c[0], c[2], ("central", "hllc", "roe")[c[3]],
+                                                    "_tait" if c[4] == 2 else "") for c in CASES])
+def test_rhs_matches_the_general_form(nb, iq, ivis, ihllc, ieos):
     import oracle as O
-    cfg = config.Config(nx=3, ny=2, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=1, ihllc=ihllc,
-                        coll=0.0 if ivis == 1 else 0.8, colvis=0.3, lx=1.5, ly=0.8, lz=1.1)
+    cfg = config.Config(nx=3, ny=2, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=ieos, ihllc=ihllc,
+                        coll=0.0 if ivis == 1 else 0.8, colvis=0.3, lx=1.5, ly=0.8, lz=1.1, P_1=0.05, P_base=1.0)
     Q = ic.random_smooth(cfg, seed=10 * nb + ivis, amp=0.2, stress_amp=0.05)
     if ivis == 2:
         ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.05, seed=nb)

@@ -9,7 +9,8 @@ from the basis definition).  ivis 2 follows the one deviation the oracle
 states: the reference never writes rh..en of Q_out in that case, and both
 restatements give them the explicit update.
 
-Quirks carried: the sound speed sqrt(gamma (E/rho - v^2/2)) with gamma, not
+The Tait EOS (ieos 2) runs through the same stages with its own CFL sound
+speed sqrt(7.2 P_1 rho^6.2 + T_floor).  Quirks carried: the sound speed sqrt(gamma (E/rho - v^2/2)) with gamma, not
 gamma - 1; the maximum over cells with density above rh_mult rh_floor; vmax
 adds the LAST cell's sound speed and uses dxi alone; cflm 0.14 (iquad 2) or
 0.08 (iquad 3) (initialize.f90:104-122).  Measured: the time bit-identical and
@@ -92,21 +93,25 @@ def step(cfg, Q, B):
 
 
 CASES = [
-    # nb, iquad, ivis, ihllc, iorder, y boundaries
-    (4, 2, 0, 1, 2, "periodic"),
-    (4, 2, 1, 2, 3, "wall"),
-    (8, 2, 1, 1, 2, "noslip"),
-    (10, 3, 2, 1, 3, "periodic"),
-    (10, 3, 0, 0, 3, "wall"),
+    # nb, iquad, ivis, ihllc, iorder, y boundaries, ieos
+    (4, 2, 0, 1, 2, "periodic", 1),
+    (4, 2, 1, 2, 3, "wall", 1),
+    (8, 2, 1, 1, 2, "noslip", 1),
+    (10, 3, 2, 1, 3, "periodic", 1),
+    (10, 3, 0, 0, 3, "wall", 1),
+    (4, 2, 0, 1, 2, "wall", 2),
+    (10, 3, 1, 1, 3, "periodic", 2),
 ]
 
 
-@pytest.mark.parametrize("nb,iq,ivis,ihllc,iorder,ybc", CASES,
-                         ids=["nb%d_ivis%d_rk%d_%s" % (c[0], c[2], c[4], c[5]) for c in CASES])
-def test_three_steps_match_the_oracle(nb, iq, ivis, ihllc, iorder, ybc):
+@pytest.mark.parametrize("nb,iq,ivis,ihllc,iorder,ybc,ieos", CASES,
+                         ids=["nb%d_ivis%d_rk%d_%s%s" % (c[0], c[2], c[4], c[5], "_tait" if c[6] == 2 else "")
+                              for c in CASES])
+def test_three_steps_match_the_oracle(nb, iq, ivis, ihllc, iorder, ybc, ieos):
     import oracle as O
-    cfg = config.Config(nx=3, ny=3, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=1, ihllc=ihllc, iorder=iorder,
-                        coll=5.0 if ivis != 0 else 0.8, colvis=0.3, lx=1.5, ly=1.2, lz=1.1, ylobc=ybc, yhibc=ybc)
+    cfg = config.Config(nx=3, ny=3, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=ieos, ihllc=ihllc, iorder=iorder,
+                        coll=5.0 if ivis != 0 else 0.8, colvis=0.3, lx=1.5, ly=1.2, lz=1.1, ylobc=ybc, yhibc=ybc,
+                        P_1=0.05, P_base=1.0)
     Q = ic.random_smooth(cfg, seed=nb + 3 * ivis, amp=0.2, stress_amp=0.05)
     if ivis == 2:
         ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.05, seed=nb)
