@@ -63,17 +63,20 @@ def point_flux(cfg, q, d):
     for j in range(3):
         if cfg.ivis in (0, 1):
             f[MX + j] = M[j] * v[d] + (P if j == d else 0.0) + P_[(j, d)]
-        elif cfg.ivis == 2:
+        else:
             f[MX + j] = (P_[(d, d)] - P10 + P) if j == d else P_[(j, d)]
-    f[EN] = (Ener + P) * v[d] + P_[(d, d)] * v[d] + P_[(d, others[0])] * v[others[0]] + \
-        P_[(d, others[1])] * v[others[1]]
+    if cfg.ivis == 3:      # Grad closure: the energy tensor E_ij does no work (ten_moment.f90:969)
+        f[EN] = (Ener + P) * v[d]
+    else:
+        f[EN] = (Ener + P) * v[d] + P_[(d, d)] * v[d] + P_[(d, others[0])] * v[others[0]] + \
+            P_[(d, others[1])] * v[others[1]]
     cv = cfg.colvis
     if cfg.ivis in (0, 1):
         for j in range(3):
             f[PIJ[(j, j)]] = (4.0 / 3.0) * cv * v[d] if j == d else -(2.0 / 3.0) * cv * v[d]
         for (a, b) in ((0, 1), (0, 2), (1, 2)):
             f[PIJ[(a, b)]] = cv * v[b if a == d else a] if d in (a, b) else 0.0
-    elif cfg.ivis == 2:
+    else:                  # ivis 2, and ivis 3 with E_ij (ten_moment.f90:895-1000)
         vx, vy, vz = v
         Mx, My, Mz = M
         Pxx, Pyy, Pzz, Pxy, Pxz, Pyz = (q[k] for k in (PXX, PYY, PZZ, PXY, PXZ, PYZ))
@@ -102,11 +105,12 @@ def point_flux(cfg, q, d):
 
 
 def cfcal(cfg, q, d):
-    """Freezing speed |v_d| + c_s (flux.f90:1029-1072)."""
+    """Freezing speed |v_d| + c_s (flux.f90:1029-1072; for ivis 3
+    ten_moment.f90:1721-1754, the same with the pressure of E_ij)."""
     dn = q[RH]
     dni = 1.0 / dn
     v = q[MX:MZ + 1] * dni
-    if cfg.ivis == 2:
+    if cfg.ivis >= 2:
         P = (1.0 / 3.0) * (q[PXX] + q[PYY] + q[PZZ] - dn * (v[0] ** 2 + v[1] ** 2 + v[2] ** 2))
     else:
         P = (cfg.aindex - 1) * (q[EN] - 0.5 * dn * (v[0] ** 2 + v[1] ** 2 + v[2] ** 2))
@@ -247,7 +251,7 @@ def roe(cfg, qL, qR, fL, fR, d):
 
 def face_flux(cfg, qL, qR, d, stale=True, rho_last=None):
     fL, fR = point_flux(cfg, qL, d), point_flux(cfg, qR, d)
-    cfr = max(cfcal(cfg, qL, d), cfcal(cfg, qR, d)) if cfg.ivis == 2 else 0.0
+    cfr = max(cfcal(cfg, qL, d), cfcal(cfg, qR, d)) if cfg.ivis >= 2 else 0.0
     F = 0.5 * (fL + fR) - 0.5 * cfr * (qR - qL)
     waves = None
     if cfg.ihllc == 1:

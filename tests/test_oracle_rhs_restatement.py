@@ -20,7 +20,8 @@ test_oracle_face_restatement.py.  The C oracle evaluates the same operator
 through its own tables (basis_funcs.f90's bfvals_*), loops and reductions,
 so agreement to rounding (measured 1e-15 to 6e-15 of each variable's scale)
 checks the volume and surface integrals, the face traces, the ghost traces
-and the sources for nb 4/8/10, ivis 0/1/2, the central, HLLC and Roe fluxes,
+and the sources for nb 4/8/10, ivis 0/1/2/3 (3: the Grad closure of the
+monolithic 10-moment code), the central, HLLC and Roe fluxes,
 and the Tait EOS with HLLC's stale 1/rho taken from the right state at each
 face's last point."""
 import numpy as np
@@ -171,6 +172,9 @@ CASES = [
     (4, 2, 0, 1, 2),
     (10, 3, 1, 1, 2),
     (8, 2, 2, 0, 2),
+    (4, 2, 3, 1, 1),
+    (10, 3, 3, 0, 1),
+    (8, 2, 3, 2, 1),
 ]
 
 
@@ -182,7 +186,7 @@ def test_rhs_matches_the_general_form(nb, iq, ivis, ihllc, ieos):
     cfg = config.Config(nx=3, ny=2, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=ieos, ihllc=ihllc,
                         coll=0.0 if ivis == 1 else 0.8, colvis=0.3, lx=1.5, ly=0.8, lz=1.1, P_1=0.05, P_base=1.0)
     Q = ic.random_smooth(cfg, seed=10 * nb + ivis, amp=0.2, stress_amp=0.05)
-    if ivis == 2:
+    if ivis >= 2:
         ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.05, seed=nb)
     Q = np.asfortranarray(Q)
     got = O.Oracle(cfg).rhs(Q.copy(order="F"), limit=False)

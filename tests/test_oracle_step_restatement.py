@@ -2,7 +2,10 @@
 get_min_dt (hermeshd.f90:145-199), the SSP-RK2/RK3 combinations
 (integrator.f90:62-85) of forward-Euler stages that first limit their input
 in place (integrator.f90:93-114, so the combination reads the limited state),
-and the stage update of each ivis (integrator.f90:125-252), on top of the
+and the stage update of each ivis (integrator.f90:125-252; for the Grad
+closure, ivis 3, the monolithic 10-moment code's advance_time_level_gl and,
+with RK2, its implicit source step after every stage, ten_moment.f90:335-372,
+719-892), on top of the
 general-form right-hand side of test_oracle_rhs_restatement.py and the numpy
 limiter of test_limiter_restatement.py (face-point basis values evaluated here
 from the basis definition).  ivis 2 follows the one deviation the oracle
@@ -71,6 +74,11 @@ def euler_stage(cfg, Q_in, dt, B):
     faci = 1.0 / (1.0 + dt * cfg.coll)
     if cfg.ivis == 1:
         out[..., PXX:, :] *= faci
+    elif cfg.ivis == 3 and cfg.iorder == 2:
+        # the Grad closure's RK2 follows each advection stage by its implicit
+        # source step (ten_moment.f90:342-356,719-892), here on the values
+        # before that step (the reference passes one array as both arguments)
+        out = grad_source_step(cfg, out, dt)
     elif cfg.ivis == 2:
         P = Q_in[..., PXX:PXX + 3, :]
         g = r[..., PXX:PXX + 3, :]
@@ -78,6 +86,38 @@ def euler_stage(cfg, Q_in, dt, B):
         extra = cfg.coll * dt * P.sum(axis=-2) / 3 - cfg.coll * dt ** 2 * g.sum(axis=-2) / 3
         out[..., PXX:PXX + 3, :] = faci * (P - dt * g + extra[..., None, :])
         out[..., PXX + 3:, :] *= faci
+    return out
+
+
+def grad_source_step(cfg, Q, dt):
+    fams = FAMILIES[cfg.nbasis]
+    nb = len(fams)
+    cb = [float((2 * a + 1) * (2 * b + 1) * (2 * c + 1)) for a, b, c in fams]
+    s, w = rule(cfg.iquad)
+    pts = [((s[a], s[b], s[c]), w[a] * w[b] * w[c]) for a in range(len(s)) for b in range(len(s))
+           for c in range(len(s))]
+    out = Q.copy()
+    for i in range(cfg.nx):
+        for j in range(cfg.ny):
+            for k in range(cfg.nz):
+                sr = np.zeros((6, nb))
+                for p, wp in pts:
+                    ph = np.array([phi(f, p) for f in fams])
+                    dn = ph @ Q[i, j, k, RH]
+                    vx, vy, vz = (ph @ Q[i, j, k, m] / dn for m in (MX, MY, MZ))
+                    c = cfg.coll * dn
+                    S = (c * (2 * vx ** 2 - vy ** 2 - vz ** 2) / 3, c * (2 * vy ** 2 - vz ** 2 - vx ** 2) / 3,
+                         c * (2 * vz ** 2 - vx ** 2 - vy ** 2) / 3, c * vx * vy, c * vx * vz, c * vy * vz)
+                    for m in range(6):
+                        sr[m] += 0.125 * np.array(cb) * wp * ph * S[m]
+                E = Q[i, j, k, PXX:PXX + 6].copy()
+                den = 1.0 + dt * cfg.coll
+                esum = cfg.coll * dt * (E[0] + E[1] + E[2]) / 3
+                ssum = cfg.coll * dt ** 2 * (sr[0] + sr[1] + sr[2]) / 3
+                for m in range(3):
+                    out[i, j, k, PXX + m] = (E[m] + dt * sr[m] + esum + ssum) / den
+                for m in range(3, 6):
+                    out[i, j, k, PXX + m] = (E[m] + dt * sr[m]) / den
     return out
 
 
@@ -101,6 +141,9 @@ CASES = [
     (10, 3, 0, 0, 3, "wall", 1),
     (4, 2, 0, 1, 2, "wall", 2),
     (10, 3, 1, 1, 3, "periodic", 2),
+    (4, 2, 3, 1, 2, "periodic", 1),
+    (10, 3, 3, 0, 3, "wall", 1),
+    (8, 2, 3, 2, 2, "noslip", 1),
 ]
 
 
@@ -113,7 +156,7 @@ def test_three_steps_match_the_oracle(nb, iq, ivis, ihllc, iorder, ybc, ieos):
                         coll=5.0 if ivis != 0 else 0.8, colvis=0.3, lx=1.5, ly=1.2, lz=1.1, ylobc=ybc, yhibc=ybc,
                         P_1=0.05, P_base=1.0)
     Q = ic.random_smooth(cfg, seed=nb + 3 * ivis, amp=0.2, stress_amp=0.05)
-    if ivis == 2:
+    if ivis >= 2:
         ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.05, seed=nb)
     Q = np.asfortranarray(Q)
     B = face_basis(cfg)
