@@ -1,6 +1,6 @@
 """The whole right-hand side restated a second time in numpy, against the C
 oracle, on 3-D grids with every basis mode populated: periodic, and with the
-wall, no-slip and outflow boundaries (boundary.f90:76-338 on the traces that
+wall, no-slip, outflow and x-lo inflow boundaries (boundary.f90:76-338 on the traces that
 prepare_step.f90:20-41 hands them).
 
 Independent of the oracle's tables and loops: the basis is evaluated here
@@ -64,16 +64,28 @@ def rule(iquad):
     return list(s), list(w)
 
 
-def ghost(kind, side, d, interior):
+def ghost(kind, side, d, interior, cfg=None, cell=None):
     """Ghost traces of one boundary face from the interior traces at its
     points (boundary.f90:76-338): no-slip zeroes every momentum, a wall the
     normal one; outflow copies the trace and zeroes the normal momentum of
     all the face's points when any of them flows in (lo: a positive maximum;
     y/z hi: a negative minimum).  The x-hi outflow routine never copies the
-    trace, so its ghost keeps the zeros it started from."""
+    trace, so its ghost keeps the zeros it started from.  The x-lo inflow
+    (x_bc_inflow with set_xlobc_inflow's profile, boundary.f90:568-612)
+    copies the trace and sets rho, m_x, E from the parabolic stream at the
+    cell centre's height, m_y = m_z = 0."""
     m = MX + d
     out = [q.copy() for q in interior]
-    if kind == "noslip":
+    if kind == "inflow":
+        assert side == "lo" and d == 0
+        yp = (cell[1] + 0.5) * cfg.ly / cfg.ny                 # yc(j) - lyd
+        vx = 4 * cfg.inflow_u * yp * (cfg.ly - yp) / cfg.ly ** 2
+        den = cfg.inflow_rho
+        pres = cfg.inflow_p if cfg.inflow_p > 0 else den * cfg.T_floor
+        for q in out:
+            q[0], q[MX], q[MX + 1], q[MX + 2] = den, den * vx, 0.0, 0.0
+            q[MZ + 1] = pres / (cfg.aindex - 1) + 0.5 * den * vx ** 2
+    elif kind == "noslip":
         for q in out:
             q[MX:MZ + 1] = 0.0
     elif kind == "wall":
@@ -144,7 +156,7 @@ def restated_rhs(cfg, Q):
                     else:
                         right = [value(tuple(up), lo) for _, lo, _ in pts]
                     if cell[d] == 0 and bcs[d][0] != "periodic":
-                        left = ghost(bcs[d][0], "lo", d, [value(cell, lo) for _, lo, _ in pts])
+                        left = ghost(bcs[d][0], "lo", d, [value(cell, lo) for _, lo, _ in pts], cfg, cell)
                     else:
                         left = [value(tuple(dn), hi) for hi, _, _ in pts]
                     # the Tait sound speeds' stale 1/rho: the right state at the face's last
@@ -203,11 +215,12 @@ BC_CASES = [
     (4, 2, 1, 2, ("periodic", "periodic", "noslip", "noslip", "periodic", "periodic")),
     (4, 2, 0, 1, ("outflow", "periodic", "outflow", "outflow", "outflow", "outflow")),
     (10, 3, 2, 1, ("wall", "wall", "outflow", "noslip", "noslip", "wall")),
+    (8, 2, 1, 2, ("inflow", "wall", "noslip", "noslip", "periodic", "periodic")),
 ]
 
 
 @pytest.mark.parametrize("nb,iq,ivis,ihllc,bc", BC_CASES, ids=["walls_y_nb8", "noslip_y_nb4_roe", "outflow_nb4",
-                                                                "mixed_nb10_ivis2"])
+                                                                "mixed_nb10_ivis2", "inflow_channel_nb8"])
 def test_rhs_with_boundaries(nb, iq, ivis, ihllc, bc):
     """The ghost traces of the wall, no-slip and outflow boundaries (outflow
     states on both sides of the normal-velocity sign, so both of its branches
@@ -215,7 +228,8 @@ def test_rhs_with_boundaries(nb, iq, ivis, ihllc, bc):
     import oracle as O
     cfg = config.Config(nx=3, ny=3, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=1, ihllc=ihllc,
                         coll=0.0 if ivis == 1 else 0.8, colvis=0.3, lx=1.5, ly=1.2, lz=1.1,
-                        xlobc=bc[0], xhibc=bc[1], ylobc=bc[2], yhibc=bc[3], zlobc=bc[4], zhibc=bc[5])
+                        xlobc=bc[0], xhibc=bc[1], ylobc=bc[2], yhibc=bc[3], zlobc=bc[4], zhibc=bc[5],
+                        inflow_u=0.4, inflow_rho=1.1, inflow_p=0.9)
     Q = ic.random_smooth(cfg, seed=7 * nb + ivis, amp=0.2, stress_amp=0.05)
     if ivis == 2:
         ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.05, seed=nb)
