@@ -115,8 +115,13 @@ def restated_rhs(cfg, Q):
     interior = [((s[a], s[b], s[c]), w[a] * w[b] * w[c]) for a in range(len(s)) for b in range(len(s))
                 for c in range(len(s))]
 
+    cache = {}
+
     def value(cell, p):
-        return np.array([sum(phi(fams[b], p) * Q[cell + (v, b)] for b in range(nb)) for v in range(NQ)])
+        key = tuple(p)
+        if key not in cache:
+            cache[key] = np.array([phi(f, p) for f in fams])
+        return Q[cell] @ cache[key]
 
     out = np.zeros_like(Q)
     for i in range(n[0]):
