@@ -97,3 +97,62 @@ def test_smooth_wave_converges_at_the_basis_order(nb, iq, ihllc, grids, order):
     rates = [math.log2(errs[i] / errs[i + 1]) for i in range(len(errs) - 1)]
     assert min(rates) >= order, (errs, rates)
     assert max(rates) <= order + 1.6, (errs, rates)                # not a smaller-than-expected error by accident
+
+
+def _vortex(g, x, y, t):
+    """The isentropic vortex of initialcon.f90:128-183 (version 1: mean flow
+    (1, 1), Rgsqi 0.5, beta 5) carried by the mean flow for a time t on the
+    periodic [-5, 5]^2: conserved rh, mx, my, mz, en at the points (x, y)."""
+    beta, rg = 5.0, 0.5
+    xs = (x - t + 5) % 10 - 5
+    ys = (y - t + 5) % 10 - 5
+    r2 = xs ** 2 + ys ** 2
+    e = np.exp(rg * (1 - r2))
+    vx = 1 - ys * beta / (2 * math.pi) * e
+    vy = 1 + xs * beta / (2 * math.pi) * e
+    te = 1 - (g - 1) * beta ** 2 / (16 * rg * g * math.pi ** 2) * np.exp(2 * rg * (1 - r2))
+    dn = te ** (1 / (g - 1))
+    return np.stack([dn, dn * vx, dn * vy, 0 * dn, dn ** g / (g - 1) + 0.5 * dn * (vx ** 2 + vy ** 2)])
+
+
+# (degree in x, degree in y) of the nb-10 family's modes without z
+_VORTEX_MODES = {0: (0, 0), 1: (1, 0), 2: (0, 1), 6: (1, 1), 7: (2, 0), 8: (0, 2)}
+
+
+def _project_vortex(cfg, t, nq=6):
+    s, w = np.polynomial.legendre.leggauss(nq)
+    dx, dy = cfg.lx / cfg.nx, cfg.ly / cfg.ny
+    xc = -cfg.lx / 2 + dx * (np.arange(cfg.nx) + 0.5)
+    yc = -cfg.ly / 2 + dy * (np.arange(cfg.ny) + 0.5)
+    Q = np.zeros(cfg.shape_f, order="F")
+    for a in range(nq):
+        for b in range(nq):
+            X, Y = np.meshgrid(xc + 0.5 * dx * s[a], yc + 0.5 * dy * s[b], indexing="ij")
+            U = np.moveaxis(_vortex(cfg.aindex, X, Y, t), 0, -1)
+            for m, (kx, ky) in _VORTEX_MODES.items():
+                ph = _legendre(kx, s[a]) * _legendre(ky, s[b])
+                Q[:, :, 0, 0:5, m] += (2 * kx + 1) * (2 * ky + 1) / 4.0 * w[a] * w[b] * ph * U
+    return Q
+
+
+def test_vortex_converges_at_third_order():
+    """The headline configuration (2-D isentropic vortex, nb 10, HLLC, SSP-RK3)
+    from the L2 projection of the exact vortex, advected for t = 1: the density
+    error against the projected exact solution falls at third order (measured
+    5.67e-3, 5.59e-4, 5.94e-5 on 16^2, 32^2, 64^2: rates 3.34, 3.23; the test
+    runs the first two)."""
+    import oracle as O
+    errs = []
+    for n in (16, 32):
+        cfg = config.isentropic_vortex_2d(n=n)
+        Q = _project_vortex(cfg, 0.0)
+        o = O.Oracle(cfg)
+        ns = int(math.ceil(1.0 / o.get_min_dt(Q)))
+        o.advance_fixed_dt(Q, 1.0 / ns, ns)
+        ex = _project_vortex(cfg, 1.0)
+        dx = cfg.lx / n
+        e2 = sum(float(((Q[:, :, 0, RH, m] - ex[:, :, 0, RH, m]) ** 2).sum()) * dx * dx / ((2 * kx + 1) * (2 * ky + 1))
+                 for m, (kx, ky) in _VORTEX_MODES.items())
+        errs.append(math.sqrt(e2))
+    rate = math.log2(errs[0] / errs[1])
+    assert 2.8 <= rate <= 4.0, (errs, rate)
