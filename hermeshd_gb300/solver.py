@@ -159,8 +159,14 @@ class Solver:
         Q(nx,ny,nz,nQ,nb), dtype matching the precision), updated in place."""
         if q_host.dtype != self.np_dtype:
             raise _lib.HermesError(3, "host array dtype does not match the precision")
-        if q_host.size != int(np.prod(self.shape)) or not (q_host.flags.c_contiguous or q_host.flags.f_contiguous):
-            raise _lib.HermesError(2, "host array size/contiguity")
+        # the two views of the same memory; a C-ordered Q(nx,ny,nz,nQ,nb) has the
+        # right size but another layout, and is refused rather than misread
+        sh = tuple(self.shape)
+        if not ((q_host.shape == sh and q_host.flags.c_contiguous) or
+                (q_host.shape == sh[::-1] and q_host.flags.f_contiguous)):
+            raise _lib.HermesError(2, f"expected a C-contiguous {sh} or Fortran-ordered {sh[::-1]} host array, "
+                                      f"got shape {q_host.shape} (C-contiguous {q_host.flags.c_contiguous}, "
+                                      f"Fortran {q_host.flags.f_contiguous})")
         tt, dd = C.c_double(t), C.c_double(0.0)
         check(lib().hermes_advance_host(self.ctx, C.c_void_p(q_host.ctypes.data), int(nsteps), C.byref(tt),
                                         C.byref(dd)), self.ctx)

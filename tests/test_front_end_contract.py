@@ -54,6 +54,24 @@ def test_shape_and_order_mismatch_are_rejected():
     assert m.solver is None
 
 
+def test_solver_host_array_layouts():
+    """Solver.advance_host takes the two views of the state's memory, a
+    C-contiguous (nb,nQ,nz,ny,nx) array or a Fortran-ordered Q(nx,ny,nz,nQ,nb),
+    and refuses a C-ordered Q(nx,ny,nz,nQ,nb) of the right size (another
+    layout) and the wrong dtype, before any call into the library."""
+    from hermeshd_gb300.solver import Solver
+    cfg = config.isentropic_vortex_2d(n=6)
+    s = Solver.__new__(Solver)            # no context: the checks come first
+    s.cfg, s.np_dtype = cfg, np.float64
+    for bad, code in ((np.zeros(cfg.shape_f, order="C"), 2),
+                      (np.zeros(cfg.shape_c, order="F"), 2),
+                      (np.zeros(cfg.shape_c, dtype=np.float32), 3),
+                      (np.zeros(cfg.shape_c)[..., ::2], 2)):
+        with pytest.raises(HermesError) as e:
+            s.advance_host(bad, 1)
+        assert e.value.code == code
+
+
 @pytest.mark.gpu
 def test_reference_driver_loop_with_float32_arrays():
     """src/test_hermeshd.py:44-83 as written: float32 Fortran arrays (nx 50,
