@@ -5,9 +5,9 @@ path must match them without the oracle at run time.
 Tolerances (relative L2): oracle vs fixture 1e-13 (libm differences between
 hosts in the noise path's log/cos); CUDA path: right-hand side 1e-12, state
 after the fixture's steps 1e-11, time 1e-11.  The second, numpy restatement
-of the step (test_oracle_*_restatement.py) reproduces the seven fixtures
-without the stochastic stress or the body force: measured right-hand sides
-within 6e-15, states within 6e-16 (Sod with HLLC 3.6e-13, its contact
+of the step (test_oracle_*_restatement.py) reproduces every fixture,
+the stochastic stress and the body force included: measured right-hand sides
+within 6e-14, states within 6e-16 (Sod with HLLC 3.6e-13, its contact
 branches picked by rounding-level velocities), times within 1e-16.
 """
 import glob
@@ -62,15 +62,11 @@ def test_cuda_path_matches_fixture(name):
     assert t == pytest.approx(float(d["t"]), rel=1e-11)
 
 
-# fixtures without the stochastic stress or the body force (neither has a
-# second restatement): the numpy restatement of the step reproduces them
-# without the C oracle that wrote them -- the right-hand side to 1e-13, the
-# states after the fixture's steps to 1e-11 (the two sum in different orders,
-# and the Sod shock amplifies those roundings to ~4e-13 in 20 steps)
-RESTATED = [n for n in FIXTURES if not n.startswith(("fh_noise", "channel"))]
-
-
-@pytest.mark.parametrize("name", RESTATED)
+# the numpy restatement of the step reproduces every fixture without the C
+# oracle that wrote them -- the right-hand side to 1e-13, the states after the
+# fixture's steps to 1e-11 (the two sum in different orders, and the Sod shock
+# amplifies those roundings to ~4e-13 in 20 steps)
+@pytest.mark.parametrize("name", FIXTURES)
 def test_second_restatement_reproduces_fixture(name):
     from test_limiter_restatement import limiter_numpy
     from test_oracle_rhs_restatement import restated_rhs
@@ -80,8 +76,8 @@ def test_second_restatement_reproduces_fixture(name):
     Q0 = np.asfortranarray(d["Q0"])
     assert rel_l2(restated_rhs(cfg, limiter_numpy(Q0, cfg, B)), d["rhs"]) <= 1e-13
     Q, t = Q0.copy(), 0.0
-    for _ in range(int(d["steps"])):
-        Q, dt = step(cfg, Q, B)
+    for n in range(int(d["steps"])):
+        Q, dt = step(cfg, Q, B, n)
         t += dt
     assert rel_l2(Q, d["Q"]) <= 1e-11
     assert t == pytest.approx(float(d["t"]), rel=1e-13)

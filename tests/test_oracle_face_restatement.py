@@ -41,9 +41,49 @@ PIJ = {(0, 0): PXX, (1, 1): PYY, (2, 2): PZZ, (0, 1): PXY, (1, 0): PXY, (0, 2): 
        (1, 2): PYZ, (2, 1): PYZ}
 
 
-def point_flux(cfg, q, d):
+def philox4x32_10(ctr, key):
+    """Philox-4x32-10 (Salmon et al., SC'11) on Python integers."""
+    c0, c1, c2, c3 = ctr
+    k0, k1 = key
+    M = 0xFFFFFFFF
+    for _ in range(10):
+        p0 = 0xD2511F53 * c0
+        p1 = 0xCD9E8D57 * c2
+        c0, c1, c2, c3 = ((p1 >> 32) ^ c1 ^ k0) & M, p1 & M, ((p0 >> 32) ^ c3 ^ k1) & M, p0 & M
+        k0 = (k0 + 0x9E3779B9) & M
+        k1 = (k1 + 0xBB67AE85) & M
+    return c0, c1, c2, c3
+
+
+def stress_sample(cfg, step, stage, kind, site, pt):
+    """The stochastic stress (Sxx, Syy, Szz, Sxy, Sxz, Syz) of one point of
+    one flux call, restated from the documented counter scheme: key = seed,
+    counter = (site, pt | kind << 8 | block << 12 | stage << 16, step low,
+    step high); each 32-bit word a uniform (w + 1/2) 2^-32; three Box-Muller
+    pairs of the first six words give the diagonal and off-diagonal normals;
+    S = eta (G_ii - tr G / 3) + zeta tr G on the diagonal, eta G_ij off it
+    (random.f90:124-141 with its nine normals' six independent combinations
+    drawn directly)."""
+    key = (cfg.seed & 0xFFFFFFFF, cfg.seed >> 32)
+    w = []
+    for blk in range(2):
+        ctr = (site & 0xFFFFFFFF, (pt & 0xFF) | ((kind & 0xF) << 8) | ((blk & 0xF) << 12) | ((stage & 0xFFFF) << 16),
+               step & 0xFFFFFFFF, step >> 32)
+        w += philox4x32_10(ctr, key)
+    G = []
+    for k in range(3):
+        u1, u2 = (w[2 * k] + 0.5) * 2.0 ** -32, (w[2 * k + 1] + 0.5) * 2.0 ** -32
+        r = math.sqrt(-2.0 * math.log(u1))
+        G += [r * math.cos(2 * math.pi * u2), r * math.sin(2 * math.pi * u2)]
+    tr = G[0] + G[1] + G[2]
+    e, z = cfg.eta_sd, cfg.zeta_sd
+    return np.array([e * (G[0] - tr / 3) + z * tr, e * (G[1] - tr / 3) + z * tr, e * (G[2] - tr / 3) + z * tr,
+                     e * G[3], e * G[4], e * G[5]])
+
+
+def point_flux(cfg, q, d, S=None):
     """flux_calc_pnts_r (flux.f90:23-190) of one state in direction d (0, 1, 2),
-    no stochastic stress."""
+    with the stochastic stress S (Sxx, Syy, Szz, Sxy, Sxz, Syz) or none."""
     g = cfg.aindex
     dn, M, Ener = q[RH], q[MX:MZ + 1], q[EN]
     P_ = {k: q[v] for k, v in PIJ.items()}
@@ -60,16 +100,18 @@ def point_flux(cfg, q, d):
     f = np.zeros(11)
     f[RH] = M[d]
     others = [j for j in range(3) if j != d]
+    S_ = {k: (0.0 if S is None else S[v - PXX]) for k, v in PIJ.items()}
     for j in range(3):
         if cfg.ivis in (0, 1):
-            f[MX + j] = M[j] * v[d] + (P if j == d else 0.0) + P_[(j, d)]
+            f[MX + j] = M[j] * v[d] + (P if j == d else 0.0) + P_[(j, d)] - S_[(j, d)]
         else:
             f[MX + j] = (P_[(d, d)] - P10 + P) if j == d else P_[(j, d)]
     if cfg.ivis == 3:      # Grad closure: the energy tensor E_ij does no work (ten_moment.f90:969)
         f[EN] = (Ener + P) * v[d]
     else:
-        f[EN] = (Ener + P) * v[d] + P_[(d, d)] * v[d] + P_[(d, others[0])] * v[others[0]] + \
-            P_[(d, others[1])] * v[others[1]]
+        f[EN] = (Ener + P) * v[d] + (P_[(d, d)] - S_[(d, d)]) * v[d] + \
+            (P_[(d, others[0])] - S_[(d, others[0])]) * v[others[0]] + \
+            (P_[(d, others[1])] - S_[(d, others[1])]) * v[others[1]]
     cv = cfg.colvis
     if cfg.ivis in (0, 1):
         for j in range(3):
@@ -249,8 +291,8 @@ def roe(cfg, qL, qR, fL, fR, d):
     return res
 
 
-def face_flux(cfg, qL, qR, d, stale=True, rho_last=None):
-    fL, fR = point_flux(cfg, qL, d), point_flux(cfg, qR, d)
+def face_flux(cfg, qL, qR, d, stale=True, rho_last=None, SL=None, SR=None):
+    fL, fR = point_flux(cfg, qL, d, SL), point_flux(cfg, qR, d, SR)
     cfr = max(cfcal(cfg, qL, d), cfcal(cfg, qR, d)) if cfg.ivis >= 2 else 0.0
     F = 0.5 * (fL + fR) - 0.5 * cfr * (qR - qL)
     waves = None
@@ -264,7 +306,12 @@ def face_flux(cfg, qL, qR, d, stale=True, rho_last=None):
 
 
 def source(cfg, q):
+    """sources.f90:36-69 at one point, plus the x body force (a term of this
+    implementation, no reference counterpart: rho g on m_x, m_x g on E)."""
     s = np.zeros(11)
+    if cfg.body_force != 0.0:
+        s[MX] = q[RH] * cfg.body_force
+        s[EN] = q[MX] * cfg.body_force
     if cfg.ivis == 0:
         s[PXX:] = -cfg.coll * q[PXX:]
     elif cfg.ivis == 2:

@@ -29,7 +29,7 @@ import pytest
 
 from hermeshd_gb300 import config, ic
 
-from test_oracle_face_restatement import MX, MZ, face_flux, point_flux, source
+from test_oracle_face_restatement import MX, MZ, face_flux, point_flux, source, stress_sample
 
 NQ = 11
 FAMILIES = {
@@ -103,8 +103,16 @@ def ghost(kind, side, d, interior, cfg=None, cell=None):
     return out
 
 
-def restated_rhs(cfg, Q):
-    """glflux - source (the oracle's rhs without the limiter), shape of Q."""
+def restated_rhs(cfg, Q, step=0, stage=0):
+    """glflux - source (the oracle's rhs without the limiter), shape of Q;
+    with the stochastic stress (cfg.llns) the draws of the given step and
+    stage.  Noise sites: cell i + nx (j + ny k) for the interior calls (one
+    independent draw per direction's call, kinds 3-5); for the faces of
+    direction d (kinds 0-2) the face's index on the grid of faces, where a
+    direction periodic at both ends has n planes (the face at n is the face
+    at 0); points: the interior point index, and for faces the left states'
+    points 0..nface-1 and the right states' nface..2 nface-1, in the
+    reference's face-point order (basis_funcs.f90:392-423)."""
     bcs = ((cfg.xlobc, cfg.xhibc), (cfg.ylobc, cfg.yhibc), (cfg.zlobc, cfg.zhibc))
     fams = FAMILIES[cfg.nbasis]
     nb = len(fams)
@@ -123,6 +131,22 @@ def restated_rhs(cfg, Q):
             cache[key] = np.array([phi(f, p) for f in fams])
         return Q[cell] @ cache[key]
 
+    nf = len(s) ** 2
+    periodic = [bcs[d][0] == "periodic" and bcs[d][1] == "periodic" for d in range(3)]
+
+    def noise(kind, site, pt):
+        return stress_sample(cfg, step, stage, kind, site, pt) if cfg.llns else None
+
+    def face_site(d, face):
+        """face = (i, j, k) with the index along d running 0..n[d]"""
+        f = list(face)
+        ext = [n[0], n[1], n[2]]
+        if periodic[d]:
+            f[d] %= n[d]
+        else:
+            ext[d] += 1
+        return f[0] + ext[0] * (f[1] + ext[1] * f[2])
+
     out = np.zeros_like(Q)
     for i in range(n[0]):
         for j in range(n[1]):
@@ -130,10 +154,11 @@ def restated_rhs(cfg, Q):
                 cell = (i, j, k)
                 g = np.zeros((NQ, nb))
                 src = np.zeros((NQ, nb))
+                site = i + n[0] * (j + n[1] * k)
                 # volume terms and sources at the interior points
-                for p, wp in interior:
+                for gi, (p, wp) in enumerate(interior):
                     q = value(cell, p)
-                    f = [point_flux(cfg, q, d) for d in range(3)]
+                    f = [point_flux(cfg, q, d, noise(3 + d, site, gi)) for d in range(3)]
                     sq = source(cfg, q)
                     for b in range(nb):
                         vol = sum(dxi[d] * dphi(fams[b], p, d) * f[d] for d in range(3))
@@ -146,15 +171,22 @@ def restated_rhs(cfg, Q):
                     up[d] = (up[d] + 1) % n[d]
                     dn = list(cell)
                     dn[d] = (dn[d] - 1) % n[d]
+                    # face points in the reference's order: point o * ne + m has the
+                    # coordinates (y, z) = (m, o) on x faces, (x, z) = (o, m) on y
+                    # faces, (x, y) = (m, o) on z faces
                     pts = []
-                    for a in range(len(s)):
-                        for c in range(len(s)):
+                    for o in range(len(s)):
+                        for m in range(len(s)):
                             hi = [0.0] * 3
                             lo = [0.0] * 3
                             hi[d], lo[d] = 1.0, -1.0
+                            a, c = (m, o) if d != 1 else (o, m)
                             hi[t1] = lo[t1] = s[a]
                             hi[t2] = lo[t2] = s[c]
                             pts.append((hi, lo, w[a] * w[c]))
+                    f_hi = list(cell)
+                    f_hi[d] += 1
+                    s_hi, s_lo = face_site(d, f_hi), face_site(d, cell)
                     # neighbour traces, or the boundary's ghost traces at the domain's ends
                     if cell[d] == n[d] - 1 and bcs[d][1] != "periodic":
                         right = ghost(bcs[d][1], "hi", d, [value(cell, hi) for hi, _, _ in pts])
@@ -168,8 +200,10 @@ def restated_rhs(cfg, Q):
                     # point, (s_max, s_max) in the reference's point order (basis_funcs.f90:392-423)
                     r_hi, r_lo = right[-1][0], value(cell, pts[-1][1])[0]
                     for m, (hi, lo, w2) in enumerate(pts):
-                        F_hi, _ = face_flux(cfg, value(cell, hi), right[m], d, rho_last=r_hi)
-                        F_lo, _ = face_flux(cfg, left[m], value(cell, lo), d, rho_last=r_lo)
+                        F_hi, _ = face_flux(cfg, value(cell, hi), right[m], d, rho_last=r_hi,
+                                            SL=noise(d, s_hi, m), SR=noise(d, s_hi, nf + m))
+                        F_lo, _ = face_flux(cfg, left[m], value(cell, lo), d, rho_last=r_lo,
+                                            SL=noise(d, s_lo, m), SR=noise(d, s_lo, nf + m))
                         for b in range(nb):
                             g[:, b] += 0.25 * cb[b] * dxi[d] * w2 * (phi(fams[b], hi) * F_hi -
                                                                      phi(fams[b], lo) * F_lo)
@@ -244,3 +278,40 @@ def test_rhs_with_boundaries(nb, iq, ivis, ihllc, bc):
     scale = np.abs(want).max(axis=(0, 1, 2, 4), keepdims=True)
     err = np.abs(got - want) / np.maximum(scale, 1e-300)
     assert err.max() <= 1e-12, (err.max(), np.unravel_index(err.argmax(), err.shape))
+
+
+NOISE_CASES = [
+    # nb, iquad, ivis, ihllc, boundaries x, y, z (lo = hi), step, stage
+    (4, 2, 1, 2, ("periodic", "periodic", "periodic"), 0, 0),
+    (8, 2, 0, 1, ("wall", "periodic", "noslip"), 5, 1),
+    (10, 3, 2, 0, ("periodic", "wall", "periodic"), 2 ** 33 + 3, 2),
+]
+
+
+@pytest.mark.parametrize("nb,iq,ivis,ihllc,bc,step,stage", NOISE_CASES, ids=["nb4_roe_periodic", "nb8_hllc_walls",
+                                                                            "nb10_ivis2_central"])
+def test_rhs_with_the_stochastic_stress(nb, iq, ivis, ihllc, bc, step, stage):
+    """The stochastic stress restated from its counter scheme and placed in the
+    point flux as flux.f90:85-100 does (momentum - S, energy - S.v; no S in the
+    10-moment momentum and stress fluxes), at every face side and interior
+    call, against the oracle at a given step and stage."""
+    import oracle as O
+    cfg = config.Config(nx=3, ny=2, nz=2, nbasis=nb, iquad=iq, ivis=ivis, ieos=1, ihllc=ihllc,
+                        coll=0.0 if ivis == 1 else 0.8, colvis=0.3, lx=1.5, ly=0.8, lz=1.1,
+                        xlobc=bc[0], xhibc=bc[0], ylobc=bc[1], yhibc=bc[1], zlobc=bc[2], zhibc=bc[2],
+                        llns=True, eta_sd=0.05, zeta_sd=0.02, seed=(3 << 32) + 11)
+    Q = ic.random_smooth(cfg, seed=nb, amp=0.2, stress_amp=0.05)
+    if ivis >= 2:
+        ic.ten_moment_stress(cfg, Q, p=1.0, amp=0.05, seed=nb)
+    Q = np.asfortranarray(Q)
+    o = O.Oracle(cfg)
+    o.set_noise_counter(step)
+    for _ in range(stage):                 # the stage counter advances with each forward-Euler stage
+        o.euler_step(Q.copy(order="F"), 1e-6)
+    got = o.rhs(Q.copy(order="F"), limit=False)
+    want = restated_rhs(cfg, Q, step, stage)
+    quiet = restated_rhs(cfg.replace(llns=False), Q)
+    scale = np.abs(want).max(axis=(0, 1, 2, 4), keepdims=True)
+    err = np.abs(got - want) / np.maximum(scale, 1e-300)
+    assert err.max() <= 1e-12, (err.max(), np.unravel_index(err.argmax(), err.shape))
+    assert np.abs(want - quiet).max() > 1e-3 * np.abs(want).max()   # the stress moved the result

@@ -66,10 +66,11 @@ def face_basis(cfg):
     return np.array(rows)
 
 
-def euler_stage(cfg, Q_in, dt, B):
-    """Limits Q_in in place, then returns the stage output."""
+def euler_stage(cfg, Q_in, dt, B, step=0, stage=0):
+    """Limits Q_in in place, then returns the stage output (the stochastic
+    stress of the given step and stage)."""
     Q_in[...] = limiter_numpy(Q_in, cfg, B)
-    r = restated_rhs(cfg, Q_in)                 # glflux - source
+    r = restated_rhs(cfg, Q_in, step, stage)    # glflux - source
     out = Q_in - dt * r
     faci = 1.0 / (1.0 + dt * cfg.coll)
     if cfg.ivis == 1:
@@ -121,14 +122,16 @@ def grad_source_step(cfg, Q, dt):
     return out
 
 
-def step(cfg, Q, B):
+def step(cfg, Q, B, n=0):
+    """Step number n (the stochastic stress's step counter; its stage counter
+    is the stage's index in the step)."""
     dt = min_dt(cfg, Q)
-    q1 = euler_stage(cfg, Q, dt, B)
-    q2 = euler_stage(cfg, q1, dt, B)
+    q1 = euler_stage(cfg, Q, dt, B, n, 0)
+    q2 = euler_stage(cfg, q1, dt, B, n, 1)
     if cfg.iorder == 2:
         return 0.5 * (Q + q2), dt
     q1 = 0.75 * Q + 0.25 * q2
-    q2 = euler_stage(cfg, q1, dt, B)
+    q2 = euler_stage(cfg, q1, dt, B, n, 2)
     return (1.0 / 3.0) * Q + (2.0 / 3.0) * q2, dt
 
 
@@ -161,8 +164,8 @@ def test_three_steps_match_the_oracle(nb, iq, ivis, ihllc, iorder, ybc, ieos):
     Q = np.asfortranarray(Q)
     B = face_basis(cfg)
     mine, t_mine = Q.copy(), 0.0
-    for _ in range(3):
-        mine, dt = step(cfg, mine, B)
+    for n in range(3):
+        mine, dt = step(cfg, mine, B, n)
         t_mine += dt
     ref = Q.copy(order="F")
     t_ref, dt_ref = O.Oracle(cfg).advance(ref, 3)
