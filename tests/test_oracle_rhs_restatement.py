@@ -124,12 +124,19 @@ def restated_rhs(cfg, Q, step=0, stage=0):
                 for c in range(len(s))]
 
     cache = {}
+    cbv = np.array(cb)
 
-    def value(cell, p):
+    def basis(p):
         key = tuple(p)
         if key not in cache:
             cache[key] = np.array([phi(f, p) for f in fams])
-        return Q[cell] @ cache[key]
+        return cache[key]
+
+    def value(cell, p):
+        return Q[cell] @ basis(p)
+
+    # d phi_b / ds_d at the interior points, times dxi_d: (npg, 3, nb)
+    dphi_int = np.array([[[dxi[d] * dphi(f, p, d) for f in fams] for d in range(3)] for p, _ in interior])
 
     nf = len(s) ** 2
     periodic = [bcs[d][0] == "periodic" and bcs[d][1] == "periodic" for d in range(3)]
@@ -158,12 +165,9 @@ def restated_rhs(cfg, Q, step=0, stage=0):
                 # volume terms and sources at the interior points
                 for gi, (p, wp) in enumerate(interior):
                     q = value(cell, p)
-                    f = [point_flux(cfg, q, d, noise(3 + d, site, gi)) for d in range(3)]
-                    sq = source(cfg, q)
-                    for b in range(nb):
-                        vol = sum(dxi[d] * dphi(fams[b], p, d) * f[d] for d in range(3))
-                        g[:, b] -= 0.25 * cb[b] * wp * vol
-                        src[:, b] += 0.125 * cb[b] * wp * phi(fams[b], p) * sq
+                    f = np.array([point_flux(cfg, q, d, noise(3 + d, site, gi)) for d in range(3)])  # (3, NQ)
+                    g -= 0.25 * wp * (f.T @ dphi_int[gi]) * cbv
+                    src += 0.125 * wp * np.outer(source(cfg, q), basis(p)) * cbv
                 # surface terms: the hi and lo faces of each direction
                 for d in range(3):
                     t1, t2 = [a for a in range(3) if a != d]
@@ -204,9 +208,7 @@ def restated_rhs(cfg, Q, step=0, stage=0):
                                             SL=noise(d, s_hi, m), SR=noise(d, s_hi, nf + m))
                         F_lo, _ = face_flux(cfg, left[m], value(cell, lo), d, rho_last=r_lo,
                                             SL=noise(d, s_lo, m), SR=noise(d, s_lo, nf + m))
-                        for b in range(nb):
-                            g[:, b] += 0.25 * cb[b] * dxi[d] * w2 * (phi(fams[b], hi) * F_hi -
-                                                                     phi(fams[b], lo) * F_lo)
+                        g += 0.25 * dxi[d] * w2 * (np.outer(F_hi, basis(hi)) - np.outer(F_lo, basis(lo))) * cbv
                 out[i, j, k] = g - src
     return out
 
