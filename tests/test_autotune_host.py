@@ -100,3 +100,24 @@ def test_context_defaults_are_the_first_trial(patched):
     first = r["trials"][0]
     assert (first["faces_merged"], first["update_tpb"], first["cell_concurrent"]) == (2, 64, 0)
     assert r["launch"]["cell_concurrent"] == 1 and r["launch"]["faces_merged"] == 1
+
+
+def test_cache_returns_the_stored_shape_without_timing(patched, monkeypatch, tmp_path):
+    """The first search stores its result under the problem's signature; the
+    next call for the same signature applies the stored shape and times
+    nothing; a corrupt cache file reads as empty."""
+    path = tmp_path / "autotune.json"
+    monkeypatch.setenv("HERMES_AUTOTUNE_CACHE", str(path))
+    timed = []
+    monkeypatch.setattr(autotune, "time_steps", lambda s, q, q1, steps, repeats: timed.append(1) or cost(s.launch))
+    s = FakeSolver()
+    r1 = autotune.autotune(s, FakeQ(), use_cache=True)
+    assert not r1["cached"] and path.exists() and len(timed) > 1
+    n = len(timed)
+    s2 = FakeSolver()
+    r2 = autotune.autotune(s2, FakeQ(), use_cache=True)
+    assert r2["cached"] and len(timed) == n
+    assert s2.launch == r1["launch"] and r2["ms_per_step"] == r1["ms_per_step"]
+    path.write_text("{not json")
+    r3 = autotune.autotune(FakeSolver(), FakeQ(), use_cache=True)
+    assert not r3["cached"] and len(timed) > n
