@@ -89,3 +89,50 @@ def test_empty_and_malformed_inputs_rejected_without_gpu(hermes_lib):
     assert hermes_lib.hermes_create(C.byref(bad), None, C.byref(ctx)) == 1
     bad.bc[3] = 4       # inflow is an x-low boundary only
     assert hermes_lib.hermes_create(C.byref(bad), None, C.byref(ctx)) == 1
+
+
+def _header_prototypes():
+    """name -> (return type text, [parameter type texts]) of every function
+    the header declares."""
+    src = open(os.path.join(ROOT, "include", "hermes_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for m in re.finditer(r"^\s*((?:const\s+)?[\w]+\s*\**)\s*(hermes_\w+)\s*\(([^)]*)\)\s*;", src, flags=re.M):
+        params = [p.strip() for p in m.group(3).replace("\n", " ").split(",")]
+        params = [] if params == ["void"] or params == [""] else params
+        types = [re.sub(r"\b\w+\s*$", "", p).strip() if not p.endswith("*") else p for p in params]
+        out[m.group(2)] = (m.group(1).strip(), types)
+    return out
+
+
+def _kind_c(t):
+    if "*" in t:
+        return "ptr"
+    # size_t is uint64_t on the LP64 hosts this builds for (and ctypes.c_size_t is c_uint64 there)
+    return {"int": "i32", "int32_t": "i32", "uint32_t": "u32", "uint64_t": "u64", "double": "f64",
+            "size_t": "u64"}[t.replace("const", "").strip()]
+
+
+def _kind_ctypes(t):
+    if t in (C.c_void_p, C.c_char_p) or (isinstance(t, type) and issubclass(t, C._Pointer)):
+        return "ptr"
+    return {C.c_int32: "i32", C.c_uint32: "u32", C.c_uint64: "u64", C.c_double: "f64", C.c_size_t: "u64"}[t]
+
+
+def test_ctypes_signatures_match_the_header(hermes_lib):
+    """Every function the Python binding declares has the header's number of
+    parameters and the same kind of each (pointer, 32/64-bit integer,
+    double) and of its result: a mismatch would pass wrong values through
+    ctypes without an error."""
+    protos = _header_prototypes()
+    L = _lib.lib()
+    checked = 0
+    for name, (ret, params) in protos.items():
+        f = getattr(L, name)
+        if f.argtypes is None:
+            continue
+        assert len(f.argtypes) == len(params), (name, params, f.argtypes)
+        assert [_kind_ctypes(a) for a in f.argtypes] == [_kind_c(p) for p in params], name
+        assert _kind_ctypes(f.restype) == _kind_c(ret), (name, ret, f.restype)
+        checked += 1
+    assert checked >= 30
