@@ -136,3 +136,25 @@ def test_ctypes_signatures_match_the_header(hermes_lib):
         assert _kind_ctypes(f.restype) == _kind_c(ret), (name, ret, f.restype)
         checked += 1
     assert checked >= 30
+
+
+def test_fortran_binding_matches_the_config_struct():
+    """The ISO_C_BINDING mirror of hermes_config that INTEGRATION.md gives a
+    Fortran driver has the header's fields in the header's order, each of the
+    same width (uint64_t seed as c_int64_t: Fortran has no unsigned kinds)."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    body = re.search(r"type, bind\(C\) :: hermes_config\n(.*?)\n\s*end type", doc, flags=re.S).group(1)
+    fort = []
+    for line in body.splitlines():
+        kind, names = line.split("::")
+        kind = {"integer(c_int32_t)": "i32", "integer(c_int64_t)": "i64", "real(c_double)": "f64"}[kind.strip()]
+        for n in names.split(","):
+            n = n.strip()
+            m = re.match(r"(\w+)\((\d+)\)", n)
+            fort += [(m.group(1), kind)] * int(m.group(2)) if m else [(n, kind)]
+    width = {"int32_t": "i32", "uint64_t": "i64", "double": "f64"}
+    head = []
+    for name, typ in _header_struct_fields("hermes_config"):
+        m = re.match(r"(\w+)\[(\d+)\]", name)
+        head += [(m.group(1), width[typ])] * int(m.group(2)) if m else [(name, width[typ])]
+    assert fort == head
