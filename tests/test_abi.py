@@ -158,3 +158,15 @@ def test_fortran_binding_matches_the_config_struct():
         m = re.match(r"(\w+)\[(\d+)\]", name)
         head += [(m.group(1), width[typ])] * int(m.group(2)) if m else [(name, width[typ])]
     assert fort == head
+
+
+def test_fortran_interfaces_match_the_prototypes():
+    """The Fortran interface blocks in INTEGRATION.md bind the header's
+    functions with the header's number of arguments."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    protos = _header_prototypes()
+    found = re.findall(r"function (hermes_\w+)\(([^)]*)\) bind\(C, name=\"(hermes_\w+)\"\)", doc)
+    assert len(found) >= 3
+    for fname, args, cname in found:
+        assert fname == cname
+        assert len([a for a in args.split(",") if a.strip()]) == len(protos[cname][1]), cname
