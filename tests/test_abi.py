@@ -170,3 +170,14 @@ def test_fortran_interfaces_match_the_prototypes():
     for fname, args, cname in found:
         assert fname == cname
         assert len([a for a in args.split(",") if a.strip()]) == len(protos[cname][1]), cname
+
+
+def test_integration_python_stub_uses_the_binding():
+    """The ctypes stub INTEGRATION.md shows a maintainer compiles and names
+    only functions the binding exports."""
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    code = re.search(r"```python\n(.*?)```", doc, flags=re.S).group(1)
+    compile(code, "INTEGRATION.md", "exec")
+    used = set(re.findall(r"\b(hermes_\w+)\(", code))
+    assert used and used <= set(_lib.EXPORTS)
+    assert all(hasattr(_lib, n) for n in re.findall(r"_lib\.(\w+)\(", code))
