@@ -181,3 +181,22 @@ def test_integration_python_stub_uses_the_binding():
     used = set(re.findall(r"\b(hermes_\w+)\(", code))
     assert used and used <= set(_lib.EXPORTS)
     assert all(hasattr(_lib, n) for n in re.findall(r"_lib\.(\w+)\(", code))
+
+
+def test_readme_examples_name_real_calls():
+    """The README's Python examples compile, and the methods they call on the
+    front end and the solver exist."""
+    from hermeshd_gb300 import adjoint, hermeshd, solver
+    doc = open(os.path.join(ROOT, "README.md")).read()
+    blocks = re.findall(r"```python\n(.*?)```", doc, flags=re.S)
+    assert len(blocks) >= 3
+    for b in blocks:
+        compile(b, "README.md", "exec")
+    text = "\n".join(blocks)
+    for m in re.findall(r"\bhermeshd\.(\w+)\(", text):
+        assert hasattr(hermeshd.Hermeshd, m), m
+    for m in re.findall(r"\bs\.(\w+)\(", text):
+        assert hasattr(solver.Solver, m), m
+    for m in re.findall(r"\bfrom hermeshd_gb300\.adjoint import ([\w, ]+)", text):
+        for n in m.split(","):
+            assert hasattr(adjoint, n.strip()), n
