@@ -9,8 +9,9 @@ Routines run as written:
   * flux.f90        flux_calc_pnts_r, flux_hllc, cfcal, limiter, calc_flux_x/y/z,
                     innerintegral2, glflux
   * sources.f90     source_calc
-  * prepare_step.f90 exchange_flux;  boundary.f90 apply_boundaries and the
-                    periodic, wall, no-slip and outflow routines
+  * prepare_step.f90 exchange_flux;  boundary.f90 apply_boundaries, the
+                    periodic, wall, no-slip and outflow routines, and the
+                    x-low inflow (x_bc_inflow, set_xlobc_inflow; params.f90 yc)
   * integrator.f90  RK2, RK3, euler_step, prep_advance, calc_rhs,
                     advance_time_level;  hermeshd.f90 get_min_dt
   * src/ces/10_moment/dg_3D_hydro_lqc_SEAN.f90  flux_roe (the Roe variant)
@@ -196,7 +197,18 @@ class ReferenceStep(Reference):
         ns["perform_flux_exchange"] = perform_flux_exchange
         bsrc = source("src/boundary.f90")
         for k, (d, end) in enumerate((("x", "lo"), ("x", "hi"), ("y", "lo"), ("y", "hi"), ("z", "lo"), ("z", "hi"))):
-            ns[f"apply_{d}{end}bc"] = F.translate(bsrc, f"{d}{end}bc_{bc[k]}", ns)
+            if bc[k] != "inflow":
+                ns[f"apply_{d}{end}bc"] = F.translate(bsrc, f"{d}{end}bc_{bc[k]}", ns)
+        if bc[0] == "inflow":
+            # the parabolic x-low inflow of boundary_custom as apply_boundaries' commented-out call
+            # runs it (boundary.f90:759): set_xlobc_inflow once, then x_bc_inflow at every stage
+            ns.update(ly=cfg.ly, lyd=-cfg.ly / 2, loc_lyd=-cfg.ly / 2, dy=cfg.ly / ny, mflowrate=0.0,
+                      qxlo_ext_def=A((ny, nz, nf, nq)))
+            F.translate(source("src/params.f90"), "yc", ns)
+            F.translate(bsrc, "set_xlobc_inflow", ns)(cfg.inflow_u, cfg.inflow_rho, cfg.inflow_pressure,
+                                                       ns["qxlo_ext_def"])
+            inflow = F.translate(bsrc, "x_bc_inflow", ns)
+            ns["apply_xlobc"] = lambda qi, qe: inflow(qi, ns["qxlo_ext_def"], qe)
         F.translate(bsrc, "apply_boundaries", ns)
         F.translate(source("src/prepare_step.f90"), "exchange_flux", ns)
         flux = source("src/flux.f90")
@@ -326,6 +338,9 @@ def step_cases():
     cfg = config.Config(nx=6, ny=4, nz=1, nbasis=4, iquad=2, ieos=2, P_1=0.05, P_base=1.0, xlobc="wall",
                         xhibc="noslip")
     c["tait_walls_rk2_nb4"] = (cfg, ic.random_smooth(cfg, seed=4, amp=0.05), 10)
+    cfg = config.Config(nx=6, ny=4, nz=1, lx=1.5, ly=1.0, nbasis=4, iquad=2, ivis=1, coll=3.0, colvis=1.0,
+                        xlobc="inflow", xhibc="wall", ylobc="noslip", yhibc="noslip", inflow_u=0.3, inflow_p=1.0)
+    c["inflow_channel_rk2_nb4"] = (cfg, ic.channel(cfg, amplitude=1e-3, seed=0), 6)
     return c
 
 
