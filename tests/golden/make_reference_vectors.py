@@ -29,6 +29,8 @@ Fixtures (small, seeded):
   faces.npz               face fluxes F(q_L, q_R) of the point flux + HLLC /
                           Roe / central, per direction, ivis 0/1/2, ieos 1/2,
                           for the states of three-cell periodic lines
+  ivis2_stage.npz         one ivis-2 forward-Euler stage of the reference into a
+                          prefilled output (its rh..en rows stay unwritten)
   step_<case>.npz         the reference's whole step (ReferenceStep): the
                           right-hand side of the initial state and the state,
                           time and time step after the case's steps, in the
@@ -356,8 +358,26 @@ def step_fixture(cfg, Q0, steps):
                 config=json.dumps(dataclasses.asdict(cfg), sort_keys=True))
 
 
+def ivis2_stage():
+    """One euler_step of the reference with ivis 2, into a Q_out prefilled
+    with 7.0: integrator.f90:181-228 writes only the stress rows."""
+    sys.path[:0] = [os.path.dirname(os.path.dirname(HERE))]
+    import dataclasses
+    import json
+    from hermeshd_gb300 import config, ic
+    cfg = config.Config(nx=4, ny=3, nz=2, nbasis=4, iquad=2, ivis=2, coll=1.5, colvis=1.0)
+    Q = np.asfortranarray(ic.ten_moment_stress(cfg, ic.random_smooth(cfg, seed=3, amp=0.05), p=1.0, amp=0.01))
+    r = ReferenceStep(cfg)
+    dt = float(r.get_min_dt(F.FArray(Q.copy(order="F"))))
+    qin = F.FArray(Q.copy(order="F"))
+    qout = F.FArray(np.full_like(Q, 7.0, order="F"))
+    r.ns["euler_step"](qin, qout, dt)
+    return dict(Q_in=Q, dt=dt, Q_out=qout.a, config=json.dumps(dataclasses.asdict(cfg), sort_keys=True))
+
+
 def main():
     os.makedirs(OUT, exist_ok=True)
+    np.savez_compressed(os.path.join(OUT, "ivis2_stage.npz"), **ivis2_stage())
     for name, (cfg, Q0, steps) in step_cases().items():
         np.savez_compressed(os.path.join(OUT, f"step_{name}.npz"), **step_fixture(cfg, Q0, steps))
     for nb, iq in ((4, 2), (8, 2), (10, 3)):

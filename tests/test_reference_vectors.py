@@ -146,3 +146,17 @@ def test_cuda_path_matches_the_references_step(name):
     t, dt = s.advance(q, q1, int(d["steps"]), t=0.0)
     assert rel_l2(s.to_numpy(q), d["Q"]) <= 1e-11
     assert t == pytest.approx(float(d["t"]), rel=1e-11)
+
+
+def test_ivis2_stage_writes_only_the_stresses():
+    """The reference's own ivis-2 stage (integrator.f90:181-228), run into an
+    output prefilled with 7.0, leaves rh..en unwritten -- the deviation the
+    oracle and the CUDA path state (they give those rows the explicit
+    update) -- and its stress rows are the oracle's bit for bit."""
+    import json
+    import oracle as O
+    d = load("ivis2_stage")
+    cfg = config.Config(**json.loads(str(d["config"])))
+    assert np.all(d["Q_out"][..., :5, :] == 7.0)
+    e = O.Oracle(cfg).euler_step(np.asfortranarray(d["Q_in"]).copy(order="F"), float(d["dt"]))
+    assert np.array_equal(e[..., 5:, :], d["Q_out"][..., 5:, :])
