@@ -341,7 +341,7 @@ def translate(source: str, routine: str, ns: dict):
         raise KeyError(routine)
     kind = m.group(1)
     params = [p.strip() for p in (m.group(2) or "").split(",") if p.strip()]
-    end = re.search(r"^\s*end\s+" + kind + r"\s+" + routine.lower() + r"\b", low[m.end():], flags=re.M)
+    end = re.search(r"^\s*end\s+" + kind + r"(\s+" + routine.lower() + r")?\s*$", low[m.end():], flags=re.M)
     body = low[m.end():m.end() + end.start()]
     body = body.split("\n", 1)[1] if "\n" in body else ""
     lines = _logical_lines(body)

@@ -243,6 +243,79 @@ class ReferenceStep(Reference):
         return t, dt
 
 
+class GradFaces(Reference):
+    """Face fluxes of the Grad-closure monolith
+    (src/ces/10_moment/dg_3D_hydro_bitri_ten_moment.f90), whose ivis 0 is the
+    E_ij form (this implementation's ivis 3): its own flux_calc_pnts_r
+    (:894-1080), cfcal (:1721-1754) and flux_hllc, assembled as its flux_cal
+    does (:1127-1160: the freezing-speed LLF on every variable, HLLC over
+    rh..en when ihllc)."""
+
+    def __init__(self, aindex=5.0 / 3.0):
+        super().__init__(4, 2, ivis=0, aindex=aindex)
+        grad = source("src/ces/10_moment/dg_3D_hydro_bitri_ten_moment.f90")
+        self.ns.update(exx=6, eyy=7, ezz=8, exy=9, exz=10, eyz=11, rh_fluid=1.0)
+        self.point_flux = F.translate(grad, "flux_calc_pnts_r", self.ns)
+        self.cfcal = F.translate(grad, "cfcal", self.ns)
+        self.hllc = F.translate(grad, "flux_hllc", self.ns)
+        self.ivis = 2          # flux_cal applies the freezing-speed LLF in this form: take that branch below
+
+
+def faces_grad():
+    recs = {"solver": [], "dir": [], "states": [], "fluxes": []}
+    g = 5.0 / 3.0
+    r = GradFaces(aindex=g)
+    rng = np.random.default_rng(300)
+    for solver in ("hllc", "central"):
+        for d in (1, 2, 3):
+            for _ in range(2):
+                st = line_states(rng, 2, g)                  # full second moments E_ij
+                recs["solver"].append(("central", "hllc").index(solver))
+                recs["dir"].append(d)
+                recs["states"].append(np.array(st))
+                recs["fluxes"].append(np.array([r.face_flux(st[i], st[(i + 1) % 3], d, solver) for i in range(3)]))
+    out = {k: np.array(v) for k, v in recs.items()}
+    out.update(aindex=g, rh_floor=5.0e-6, T_floor=1.0)
+    return out
+
+
+def grad_source_step():
+    """The Grad-closure monolith's implicit source step (source_calc
+    :719-790 and advance_time_level_source :839-890), which its RK2 applies
+    after each advection stage with one array as input and output
+    (:347-348).  Run twice on the same advected state: with distinct input
+    and output arrays (every update reads the values before the step), and
+    aliased as the monolith calls it (each update reads the ones before it
+    in the routine's order).  The advected state is the oracle's RK3 stage
+    of the same problem (the monolith's RK3 applies no source step)."""
+    sys.path[:0] = [os.path.dirname(os.path.dirname(HERE)), os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                          "oracle")]
+    import dataclasses
+    import json
+    import oracle as O
+    from hermeshd_gb300 import config, ic
+    cfg = config.Config(nx=4, ny=3, nz=2, nbasis=4, iquad=2, ivis=3, coll=2.0, iorder=2)
+    Q = np.asfortranarray(ic.ten_moment_stress(cfg, ic.random_smooth(cfg, seed=9, amp=0.05), p=1.0, amp=0.01))
+    o3 = O.Oracle(cfg.replace(iorder=3))
+    dt = o3.get_min_dt(Q)
+    qgl = o3.euler_step(Q.copy(order="F"), dt)
+    r = Reference(4, 2, ivis=0, coll=cfg.coll)
+    grad = source("src/ces/10_moment/dg_3D_hydro_bitri_ten_moment.f90")
+    r.ns.update(exx=6, eyy=7, ezz=8, exy=9, exz=10, eyz=11, nx=cfg.nx, ny=cfg.ny, nz=cfg.nz, dt=dt,
+                source_r=F.FArray((cfg.nx, cfg.ny, cfg.nz, 11, 4)))
+    calc = F.translate(grad, "source_calc", r.ns)
+    step = F.translate(grad, "advance_time_level_source", r.ns)
+    qi = F.FArray(qgl.copy(order="F"))
+    calc(qi, 0.0)
+    qo = F.FArray(qgl.copy(order="F"))
+    step(qi, qo)
+    qa = F.FArray(qgl.copy(order="F"))
+    calc(qa, 0.0)
+    step(qa, qa)
+    return dict(Q=Q, dt=dt, Q_advected=qgl, separate=qo.a, aliased=qa.a,
+                config=json.dumps(dataclasses.asdict(cfg), sort_keys=True))
+
+
 def tables(nb, iq):
     r = Reference(nb, iq)
     ns = r.ns
@@ -388,6 +461,8 @@ def main():
         np.savez_compressed(os.path.join(OUT, f"limiter_nb{nb}.npz"), before=Q, after=after, rh_floor=rf, T_floor=tf,
                  aindex=5.0 / 3.0)
     np.savez_compressed(os.path.join(OUT, "faces.npz"), **faces())
+    np.savez_compressed(os.path.join(OUT, "faces_grad.npz"), **faces_grad())
+    np.savez_compressed(os.path.join(OUT, "grad_source_step.npz"), **grad_source_step())
 
 
 if __name__ == "__main__":
