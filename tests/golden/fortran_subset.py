@@ -169,7 +169,7 @@ def namespace(values: dict) -> dict:
 
 # ---- translation ------------------------------------------------------------
 _NUM = re.compile(r"(\d+\.\d*|\.\d+|\d+)([ed][+-]?\d+)?")
-_TOK = re.compile(r"\s*(\*\*|==|/=|<=|>=|<|>|\.and\.|\.or\.|\.not\.|\.eq\.|\.ne\.|\.lt\.|\.le\.|\.gt\.|\.ge\."
+_TOK = re.compile(r"\s*('[^']*'|\*\*|==|/=|<=|>=|<|>|\.and\.|\.or\.|\.not\.|\.eq\.|\.ne\.|\.lt\.|\.le\.|\.gt\.|\.ge\."
                   r"|\.true\.|\.false\.|[A-Za-z_]\w*|\d+\.\d*(?:[ed][+-]?\d+)?|\.\d+(?:[ed][+-]?\d+)?"
                   r"|\d+(?:[ed][+-]?\d+)?|[-+*/(),:=])")
 _LOGIC = {".and.": " and ", ".or.": " or ", ".not.": " not ", ".eq.": "==", ".ne.": "!=", ".lt.": "<",
@@ -225,6 +225,9 @@ class _Expr:
                 else:
                     out.append(_name(name))
                     i += 1
+            elif tok.startswith("'"):
+                out.append(repr(tok[1:-1]))
+                i += 1
             elif _NUM.fullmatch(low):
                 out.append(low.replace("d", "e"))
                 i += 1

@@ -316,6 +316,48 @@ def grad_source_step():
                 config=json.dumps(dataclasses.asdict(cfg), sort_keys=True))
 
 
+def initial_state(cfg, icid, vis=0.1):
+    """set_ic (initialcon.f90:20-72) for problems 1-5 (isentropic vortex v0,
+    v1; Sod v0, v1; Poiseuille's fluid at rest), with params.f90's cell
+    centres xc, yc, zc on the centred domain (initialize.f90:310-326)."""
+    r = Reference(cfg.nbasis, cfg.iquad, ivis=cfg.ivis, aindex=cfg.aindex, P_base=cfg.P_base,
+                  rh_floor=cfg.rh_floor, T_floor=cfg.T_floor, coll=cfg.coll, colvis=cfg.colvis)
+    ns = r.ns
+    ns.update(nx=cfg.nx, ny=cfg.ny, nz=cfg.nz, lx=cfg.lx, ly=cfg.ly, lz=cfg.lz,
+              lxd=-cfg.lx / 2, lyd=-cfg.ly / 2, lzd=-cfg.lz / 2, loc_lxd=-cfg.lx / 2, loc_lyd=-cfg.ly / 2,
+              loc_lzd=-cfg.lz / 2, dx=cfg.lx / cfg.nx, dy=cfg.ly / cfg.ny, dz=cfg.lz / cfg.nz, vis=vis,
+              mflowrate=0.0, iam=0, qxlo_ext_def=F.FArray((cfg.ny, cfg.nz, cfg.iquad ** 2, 11)),
+              mpi_print=lambda *a: None)
+    params = source("src/params.f90")
+    for f in ("xc", "yc", "zc"):
+        F.translate(params, f, ns)
+    F.translate(source("src/boundary.f90"), "set_xlobc_inflow", ns)
+    ic_src = source("src/initialcon.f90")
+    for f in ("isentropic_vortex", "sod_shock_tube_1d", "poiseuille_flow", "set_ic"):
+        F.translate(ic_src, f, ns)
+    Q = F.FArray((cfg.nx, cfg.ny, cfg.nz, 11, cfg.nbasis))
+    ns["set_ic"](Q, icid)
+    return Q.a
+
+
+def initial_states():
+    sys.path[:0] = [os.path.dirname(os.path.dirname(HERE))]
+    import dataclasses
+    import json
+    from hermeshd_gb300 import config
+    out = {}
+    for icid in (1, 2, 3, 4, 5):
+        if icid in (1, 2):
+            cfg = config.isentropic_vortex_2d(n=12)
+        elif icid in (3, 4):
+            cfg = config.Config(nx=16, ny=6, nz=1, nbasis=4, iquad=2, lx=1.0, ly=0.5, P_base=1.0)
+        else:
+            cfg = config.Config(nx=6, ny=8, nz=1, nbasis=4, iquad=2, ivis=1, coll=10.0, colvis=1.0)
+        out[f"Q_{icid}"] = initial_state(cfg, icid)
+        out[f"config_{icid}"] = json.dumps(dataclasses.asdict(cfg), sort_keys=True)
+    return out
+
+
 def tables(nb, iq):
     r = Reference(nb, iq)
     ns = r.ns
@@ -463,6 +505,7 @@ def main():
     np.savez_compressed(os.path.join(OUT, "faces.npz"), **faces())
     np.savez_compressed(os.path.join(OUT, "faces_grad.npz"), **faces_grad())
     np.savez_compressed(os.path.join(OUT, "grad_source_step.npz"), **grad_source_step())
+    np.savez_compressed(os.path.join(OUT, "initial_states.npz"), **initial_states())
 
 
 if __name__ == "__main__":

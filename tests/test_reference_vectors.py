@@ -205,3 +205,17 @@ def test_grad_closure_source_step_reading():
     assert np.array_equal(e, d["separate"])
     gap = np.abs(e - d["aliased"]).max() / np.abs(e).max()
     assert 1e-8 < gap < 1e-4, gap
+
+
+@pytest.mark.parametrize("icid", [1, 2, 3, 4, 5])
+def test_initial_states_are_the_references(icid):
+    """set_ic (initialcon.f90:20-72) executed for the isentropic vortex v0/v1,
+    the Sod tube v0/v1 and the Poiseuille fluid at rest: the host
+    restatement ic.from_icid, which the device initial states are tested
+    against, reproduces it to one rounding."""
+    import json
+    from hermeshd_gb300 import ic
+    d = load("initial_states")
+    cfg = config.Config(**json.loads(str(d[f"config_{icid}"])))
+    ref = d[f"Q_{icid}"]
+    assert np.allclose(ic.from_icid(cfg, icid), ref, rtol=0, atol=4e-16 * np.abs(ref).max())
