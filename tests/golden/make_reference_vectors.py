@@ -37,6 +37,7 @@ Fixtures (small, seeded):
                           format of the oracle-written golden fixtures
 
 Run from the repository root:  python tests/golden/make_reference_vectors.py
+(add --long for the 256-cell, 100-step Sod fixture alone)
 """
 import os
 import sys
@@ -490,8 +491,21 @@ def ivis2_stage():
     return dict(Q_in=Q, dt=dt, Q_out=qout.a, config=json.dumps(dataclasses.asdict(cfg), sort_keys=True))
 
 
+def long_cases():
+    """The Sod tube of the 100-step parity bar (256 cells, nb 4, HLLC, RK2):
+    about 15 minutes of the executed reference (`--long`)."""
+    sys.path[:0] = [os.path.dirname(os.path.dirname(HERE))]
+    from hermeshd_gb300 import config, ic
+    cfg = config.sod_1d(nx=256)
+    return {"sod_256_hllc_rk2_nb4_100": (cfg, ic.sod(cfg), 100)}
+
+
 def main():
     os.makedirs(OUT, exist_ok=True)
+    if "--long" in sys.argv:
+        for name, (cfg, Q0, steps) in long_cases().items():
+            np.savez_compressed(os.path.join(OUT, f"step_{name}.npz"), **step_fixture(cfg, Q0, steps))
+        return
     np.savez_compressed(os.path.join(OUT, "ivis2_stage.npz"), **ivis2_stage())
     for name, (cfg, Q0, steps) in step_cases().items():
         np.savez_compressed(os.path.join(OUT, f"step_{name}.npz"), **step_fixture(cfg, Q0, steps))
