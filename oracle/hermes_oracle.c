@@ -7,9 +7,14 @@
  * HERMESHD source tree) whose loops it restates.  REAL4 is promoted to double.
  * Layout is the reference's Fortran Q(nx,ny,nz,nQ,nbasis).
  *
- * Parity pinning: no golden vectors exist in the reference and it cannot be
- * compiled here; the oracle is pinned by the reference's basis self-test
- * (basis_funcs.f90:634-992), by analytic solutions and by conservation.
+ * Parity pinning: the reference ships no golden vectors and cannot be
+ * compiled here, so its routines are executed from their Fortran source by a
+ * statement-by-statement translator (tests/golden/fortran_subset.py); the
+ * tables, limiter, face fluxes, right-hand side and whole steps it produces
+ * are this file's bit for bit on the cases in tests/golden/reference/
+ * (tests/test_reference_vectors.py).  Also: the reference's basis self-test
+ * (basis_funcs.f90:634-992), analytic solutions, conservation and a second,
+ * numpy restatement of every routine.
  *
  * Build: gcc -O3 -fopenmp -ffp-contract=off -shared -fPIC (oracle/Makefile).
  * -ffp-contract=off keeps x86 and Arm results identical.

@@ -5,9 +5,11 @@ this module; the product package never does.  The oracle restates the
 reference's step path in C (hermes_oracle.c); arrays are the reference's
 Fortran-ordered Q(nx,ny,nz,nQ,nbasis) float64.
 
-Parity pinning: the reference cannot be built here and ships no golden
-vectors; the oracle is pinned by the reference's basis self-test
-(basis_funcs.f90:634-992), analytic solutions and conservation.
+Parity pinning: the reference cannot be compiled here and ships no golden
+vectors; its routines executed from their Fortran source
+(tests/golden/fortran_subset.py, tests/golden/make_reference_vectors.py)
+produce this oracle's tables, limiter, face fluxes, right-hand sides and steps
+bit for bit on the cases of tests/golden/reference/.
 """
 from __future__ import annotations
 
