@@ -37,7 +37,7 @@ Fixtures (small, seeded):
                           format of the oracle-written golden fixtures
 
 Run from the repository root:  python tests/golden/make_reference_vectors.py
-(add --long for the 256-cell, 100-step Sod fixture alone)
+(add --long [name ...] for the 100-step Sod and vortex fixtures alone)
 """
 import os
 import sys
@@ -497,13 +497,19 @@ def long_cases():
     sys.path[:0] = [os.path.dirname(os.path.dirname(HERE))]
     from hermeshd_gb300 import config, ic
     cfg = config.sod_1d(nx=256)
-    return {"sod_256_hllc_rk2_nb4_100": (cfg, ic.sod(cfg), 100)}
+    c = {"sod_256_hllc_rk2_nb4_100": (cfg, ic.sod(cfg), 100)}
+    cfg = config.isentropic_vortex_2d(n=16)
+    c["vortex_16_rk3_nb10_100"] = (cfg, ic.isentropic_vortex(cfg), 100)   # about an hour
+    return c
 
 
 def main():
     os.makedirs(OUT, exist_ok=True)
     if "--long" in sys.argv:
+        only = [a for a in sys.argv[1:] if not a.startswith("--")]
         for name, (cfg, Q0, steps) in long_cases().items():
+            if only and not any(o in name for o in only):
+                continue
             np.savez_compressed(os.path.join(OUT, f"step_{name}.npz"), **step_fixture(cfg, Q0, steps))
         return
     np.savez_compressed(os.path.join(OUT, "ivis2_stage.npz"), **ivis2_stage())
