@@ -459,6 +459,9 @@ def step_cases():
     cfg = config.Config(nx=6, ny=4, nz=1, lx=1.5, ly=1.0, nbasis=4, iquad=2, ivis=1, coll=3.0, colvis=1.0,
                         xlobc="inflow", xhibc="wall", ylobc="noslip", yhibc="noslip", inflow_u=0.3, inflow_p=1.0)
     c["inflow_channel_rk2_nb4"] = (cfg, ic.channel(cfg, amplitude=1e-3, seed=0), 6)
+    cfg = config.Config(nx=4, ny=3, nz=2, nbasis=10, iquad=3, ivis=1, coll=2.0, colvis=0.5, ieos=2, P_1=0.05,
+                        P_base=1.0, iorder=3, xlobc="wall", xhibc="noslip", ylobc="outflow", yhibc="outflow")
+    c["mixed_nb10_ivis1_tait_rk3"] = (cfg, ic.random_smooth(cfg, seed=8, amp=0.04, stress_amp=0.01), 4)
     return c
 
 
